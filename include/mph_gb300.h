@@ -1,0 +1,186 @@
+/*
+ * mph_gb300.h - C ABI of the GB300 MPH-I time-step engine.
+ *
+ * The reference solver (MphImplicit, source/main.cpp) has no library API: its
+ * boundary is the executable `MphImplicit <data> <grid> <prof%03d> <vtk%03d>
+ * <log> <nthreads>` (main.cpp:313-330) plus the .data/.grid/.prof/.vtk files,
+ * and every stage is a `static void f(void)` acting on file-static globals.
+ * This header is the drop-in replacement for that path: each entry point below
+ * names the reference function(s) it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status (MPH_OK == 0, or an MPH_ERR_* code).
+ *     No C++ exception crosses this boundary.
+ *   - Host arrays are plain pointers; particle vectors are [count][3] doubles
+ *     in the reference's layout (main.cpp:86-88), also for 2D cases.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy stream).
+ *   - A case handle is not thread safe; distinct handles are independent.
+ *   - Particle order: like the reference, a case keeps its particles sorted by
+ *     cell (main.cpp:1316-1378); mph_get_fields returns that order together with
+ *     each particle's id (its index in the input).
+ */
+#ifndef MPH_GB300_H
+#define MPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MPH_OK = 0,
+    MPH_ERR_ARG = 1,          /* bad argument / null pointer                      */
+    MPH_ERR_IO = 2,           /* file cannot be opened or is malformed            */
+    MPH_ERR_INPUT = 3,        /* input violates a reference assumption            */
+    MPH_ERR_CUDA = 4,         /* CUDA runtime error (message via mph_last_error) */
+    MPH_ERR_NOMEM = 5,        /* device allocation failed                          */
+    MPH_ERR_CAPACITY = 6,     /* a size bound was exceeded                         */
+    MPH_ERR_NOT_CONVERGED = 7,/* CR reached its iteration cap                      */
+    MPH_ERR_NAN = 8,          /* non-finite value detected in the solve            */
+    MPH_ERR_STATE = 9         /* call out of order (e.g. stage before its inputs)  */
+};
+
+enum { MPH_TYPE_COUNT = 4 };  /* particle types 0,1 fluid; 2,3 wall (main.cpp:52-56) */
+
+/* Keyword parameters of a .data file (main.cpp:523-563). */
+typedef struct mph_params {
+    double dt;
+    double output_interval;
+    double vtk_output_interval;
+    double end_time;
+    double radius_ratio_a;
+    double radius_ratio_p;
+    double radius_ratio_v;
+    double density[MPH_TYPE_COUNT];
+    double bulk_modulus[MPH_TYPE_COUNT];
+    double bulk_viscosity[MPH_TYPE_COUNT];
+    double shear_viscosity[MPH_TYPE_COUNT];
+    double surface_tension[MPH_TYPE_COUNT];
+    double interaction_ratio[MPH_TYPE_COUNT][MPH_TYPE_COUNT];
+    double gravity[3];
+    double wall_center[MPH_TYPE_COUNT][3];   /* rows 2,3 used */
+    double wall_velocity[MPH_TYPE_COUNT][3];
+    double wall_omega[MPH_TYPE_COUNT][3];
+} mph_params;
+
+/* Particle set of a .grid file (main.cpp:565-669). */
+typedef struct mph_particles {
+    int count;
+    double time;
+    double spacing;
+    double domain_min[3];
+    double domain_max[3];
+    int* type;        /* [count]                              */
+    double* pos;      /* [count][3]                           */
+    double* vel;      /* [count][3]                           */
+    int* id;          /* [count] particle ids, may be NULL    */
+} mph_particles;
+
+/* Per-particle fields returned by mph_get_fields (host buffers, [count] or
+ * [count][3]).  Any pointer may be NULL to skip that field. */
+typedef struct mph_fields {
+    int* id;
+    int* type;
+    double* pos;
+    double* vel;
+    double* force;          /* Force (main.cpp:88)                       */
+    double* vol_strain_p;   /* VolStrainP (main.cpp:147)                 */
+    double* divergence_p;   /* DivergenceP, output steps only            */
+    double* pressure_p;     /* PressureP, output steps only              */
+    double* virial_p;       /* VirialPressureAtParticle, output steps    */
+    int* neighbor_count;    /* NeighborCount                             */
+} mph_fields;
+
+/* Solve statistics of the last step (the reference logs the same numbers,
+ * main.cpp:4381). */
+typedef struct mph_solve_stats {
+    int iterations;
+    double rr0, rr, rs0, rs;
+    int status;
+} mph_solve_stats;
+
+typedef struct mph_case mph_case;
+
+/* Solver precision of a case. */
+enum {
+    MPH_PRECISION_FP64 = 0,   /* plain FP64 form: the reference algorithm as is    */
+    MPH_PRECISION_MIXED = 1   /* FP32 inner CR + V-cycle, FP64 outer refinement      */
+};
+
+/* ---- files (replace readDataFile main.cpp:523, readGridFile main.cpp:565,
+ *      writeProfFile main.cpp:696, writeVtkFile main.cpp:722) ---- */
+int mph_read_data(const char* path, mph_params* out);
+/* First call with buffers NULL to get the count; then with type/pos/vel set. */
+int mph_read_grid(const char* path, mph_particles* out);
+int mph_write_prof(const char* path, const mph_particles* parts);
+int mph_case_write_vtk(mph_case* c, const char* path);
+int mph_case_write_prof(mph_case* c, const char* path);
+
+/* ---- case lifetime ----
+ * mph_case_create replaces readGridFile's allocation + initializeWeight /
+ * initializeFluid / initializeWall / initializeDomain and the initial
+ * calculateCellParticle / calculateNeighbor / density pass of main()
+ * (main.cpp:347-375).  dim is 2 (the -D TWO_DIMENSIONAL build) or 3. */
+int mph_case_create(const mph_params* prm, const mph_particles* parts, int dim,
+                    int precision, void* stream, mph_case** out);
+int mph_case_destroy(mph_case* c);
+int mph_case_set_stream(mph_case* c, void* stream);
+
+/* One or more full time steps (the body of main.cpp:386-474, without the
+ * file output).  Returns MPH_ERR_NOT_CONVERGED if a solve hit its cap. */
+int mph_step(mph_case* c, int nsteps);
+/* Steps of several independent cases, interleaved on their streams. */
+int mph_batch_step(mph_case** cases, int ncases, int nsteps);
+
+int mph_case_count(mph_case* c, int* count, int* fluid_count);
+int mph_case_time(mph_case* c, double* time);
+int mph_get_fields(mph_case* c, mph_fields* out);
+int mph_get_solve_stats(mph_case* c, mph_solve_stats* out);
+
+/* ---- stage entry points (parity tests), in step order ----
+ * step_begin  : calculateConvection, calculateWall, calculatePeriodicBoundary,
+ *               resetForce (main.cpp:1678, 2089, 4741, 1690)
+ * cellsort    : calculateCellParticle (main.cpp:1164)
+ * neighbors   : calculateNeighbor (main.cpp:1382)
+ * explicit    : calculateDensityA .. calculateAcceleration (main.cpp:413-430)
+ * assemble    : calculateMatrixA, calculateMatrixC, multiplyMatrixC
+ *               (main.cpp:2137, 2354, 2562)
+ * mg_build    : calculateMultiGridMatrix (main.cpp:2761)
+ * solve       : solveWithConjugatedGradient (main.cpp:4270)
+ * step_end    : Time += Dt and the wall-centre update (main.cpp:470, 2123)
+ * output_fields: calculateDivergenceP, calculatePressureP,
+ *               calculateViscosityV, calculateVirialStressAtParticle
+ *               (main.cpp:454-457) */
+int mph_stage_step_begin(mph_case* c);
+int mph_stage_cellsort(mph_case* c);
+int mph_stage_neighbors(mph_case* c);
+int mph_stage_explicit(mph_case* c);
+int mph_stage_assemble(mph_case* c);
+int mph_stage_mg_build(mph_case* c);
+int mph_stage_solve(mph_case* c);
+int mph_stage_step_end(mph_case* c);
+int mph_stage_output_fields(mph_case* c);
+
+/* Replace the particle state of a case (positions, velocities, types, ids in
+ * the given order) and the wall centres / time, e.g. to continue from a state
+ * produced elsewhere.  wall_center may be NULL. */
+int mph_case_set_state(mph_case* c, const mph_particles* parts, const double* wall_center /*[4][3]*/);
+
+/* Named device arrays copied to host in the reference's layout, for tests.
+ * kind: 0 int32, 1 int64, 2 double.  With dst == NULL only *count and *kind
+ * are returned.  Names follow the reference globals (e.g. "CellIndex",
+ * "NeighborInd", "CsrCofA", "VectorB", "MultiGridCsrCofA:<level>"). */
+int mph_export(mph_case* c, const char* name, void* dst, long* count, int* kind);
+/* Scalars: fills out[] (capacity n) in the order of mph_scalar_names(). */
+int mph_scalars(mph_case* c, double* out, int n);
+const char* mph_scalar_names(void);
+
+const char* mph_last_error(void);
+const char* mph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPH_GB300_H */
