@@ -103,6 +103,17 @@ class Particles:
         return "".join(lines)
 
 
+def generator_text(parts: "Particles") -> str:
+    """`.grid` text exactly as the reference pre-processor prints it
+    (generator/generator.cpp:199-217)."""
+    dm, dM = parts.domain_min, parts.domain_max
+    lines = ["%f\n" % 0.0,
+             "%d %e  %e %e %e  %e %e %e\n" % (parts.count, parts.spacing, dm[0], dM[0], dm[1], dM[1], dm[2], dM[2])]
+    for i in range(parts.count):
+        lines.append("%d   %e %e %e    %e %e %e\n" % (int(parts.types[i]), *parts.pos[i], *parts.vel[i]))
+    return "".join(lines)
+
+
 def write_case(prefix: str, params: Params, parts: Particles) -> Tuple[str, str]:
     data_path, grid_path = prefix + ".data", prefix + ".grid"
     with open(data_path, "w") as f:

@@ -1,0 +1,458 @@
+// k_assemble.cu - the implicit system of one step.
+//
+//   k_slice_width   : sliced-ELL slice widths (longest fluid row of each
+//                     32-row slice); the row pointers come from the device scan
+//   k_matrix_c      : calculateMatrixC (main.cpp:2462-2507): D coefficients per
+//                     P-neighbour, stored aligned with the P-list
+//   k_vector_p      : the source vector p (main.cpp:2509-2549)
+//   k_matrix_a      : calculateMatrixA (main.cpp:2251-2335) + multiplyMatrixC
+//                     (main.cpp:2574-2642) in one pass per fluid row: viscous
+//                     and inertia blocks, wall velocities into b, b -= C p and
+//                     the C Lambda C^T merge-join of the two sorted P-lists,
+//                     written once into the sliced-ELL block layout.  The same
+//                     pass sums each row's blocks per neighbour cell of the
+//                     level-0 multigrid grid (part[]), so the Galerkin level-0
+//                     matrix (main.cpp:3336-3411) never re-reads A.
+#include "mph_device.cuh"
+
+namespace mph {
+
+__global__ void k_slice_width(int Nf, const int* __restrict__ nfc, int* __restrict__ width32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int v = i < Nf ? nfc[i] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && i < ((Nf + 31) / 32) * 32) width32[i >> 5] = 32 * v;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_matrix_c(DevParams P, const double* __restrict__ pos, const int* __restrict__ ncp,
+                                                  const long long* __restrict__ nptrP, const int* __restrict__ nindP,
+                                                  double* __restrict__ cval)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.Nf) return;
+    double xi[3];
+    load_vec<D>(pos, i, xi);
+    const double rP2 = P.rP * P.rP;
+    const long long b = nptrP[i];
+    const int n = ncp[i];
+    double self[3] = {0, 0, 0};
+    int selfk = 0;
+    for (int a = 0; a < n; ++a) {
+        const int j = nindP[b + a];
+        double cv[3] = {0, 0, 0};
+        if (j == i) {
+            selfk = a;
+        } else {
+            double xj[3], q[3];
+            load_vec<D>(pos, j, xj);
+            sep_vec<D>(P, xj, xi, q);
+            const double r2 = norm2_exact<D>(q);
+            if (r2 != 0.0 && rP2 - r2 > 0) {
+                const double dij = sqrt(r2);
+                const double wd = -dw_quad(P.kfp, dij, P.rP);
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    cv[r] = (q[r] / dij) * wd;
+                    self[r] += cv[r];
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) cval[(b + a) * D + r] = cv[r];
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) cval[(b + selfk) * D + r] = self[r];
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_vector_p(DevParams P, const int* __restrict__ type, const double* __restrict__ pos,
+                                                  const double* __restrict__ vel, const double* __restrict__ vsp,
+                                                  const int* __restrict__ ncp, const long long* __restrict__ nptrP,
+                                                  const int* __restrict__ nindP, double* __restrict__ pvec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const int ti = type[i];
+    const double v0 = vsp[i];
+    double p = 0.0;
+    if (v0 > 0.0) p = (v0 < 0.0 ? 0.0 : P.bulk[ti]) * v0;
+    const bool wi = is_wall(ti);
+    const double lam = P.lambda[ti];
+    double xi[3], vi[3];
+    load_vec<D>(pos, i, xi);
+    load_vec<D>(vel, i, vi);
+    const double rP2 = P.rP * P.rP;
+    double sum = 0.0;
+    const long long b = nptrP[i];
+    for (int a = 0; a < ncp[i]; ++a) {
+        const int j = nindP[b + a];
+        if (j == i) continue;
+        const bool wj = is_wall(type[j]);
+        if (!wi && !wj) continue;
+        double xj[3], q[3];
+        load_vec<D>(pos, j, xj);
+        sep_vec<D>(P, xj, xi, q);
+        const double r2 = norm2_exact<D>(q);
+        if (r2 == 0.0 || !(rP2 - r2 > 0)) continue;
+        const double dij = sqrt(r2);
+        const double wd = -dw_quad(P.kfp, dij, P.rP);
+        double vj[3];
+        if (wj) load_vec<D>(vel, j, vj);
+#pragma unroll
+        for (int s = 0; s < D; ++s) {
+            const double e = q[s] / dij;
+            if (wi) sum += lam * (e * wd) * vi[s];
+            if (wj) sum += lam * (-e * wd) * vj[s];
+        }
+    }
+    pvec[i] = p + sum;
+}
+
+struct Level0Map {
+    int mn[3], cnt[3], st[3];
+    int S;          // st0*st1*st2
+    int folded;     // 1 if some active axis has fewer than 3 grid cells
+};
+
+template <int D>
+__device__ __forceinline__ int stencil_slot(const DevParams& P, const Level0Map& M, const int* gi, int keyj)
+{
+    int jc[3];
+    key_coords(P, keyj, jc);
+    int o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o[d] = ((jc[d] - M.mn[d]) - gi[d] + 1 + M.cnt[d]) % M.cnt[d];
+    return M.st[2] * M.st[1] * o[0] + M.st[2] * o[1] + o[2];
+}
+
+template <int D>
+__device__ __forceinline__ void flush_part(double* __restrict__ prow, int slot, const double (&acc)[D][D], bool add)
+{
+    double* dst = prow + (size_t)slot * D * D;
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int s = 0; s < D; ++s) dst[r * D + s] = add ? dst[r * D + s] + acc[r][s] : acc[r][s];
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, const int* __restrict__ type,
+                                                  const int* __restrict__ key, const double* __restrict__ pos,
+                                                  const double* __restrict__ vel, const double* __restrict__ force,
+                                                  const int* __restrict__ nc, const int* __restrict__ nfc,
+                                                  const long long* __restrict__ nptr, const int* __restrict__ nind,
+                                                  const int* __restrict__ ncp, const long long* __restrict__ nptrP,
+                                                  const int* __restrict__ nindP, const double* __restrict__ cval,
+                                                  const double* __restrict__ pvec, const long long* __restrict__ sptr,
+                                                  int* __restrict__ acol, double* __restrict__ aval,
+                                                  double* __restrict__ bvec, double* __restrict__ invDiag,
+                                                  int* __restrict__ selfk_out, double* __restrict__ part)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.Nf) return;
+    constexpr int DD = D * D;
+    const int lane = i & 31;
+    const long long sbase = sptr[i >> 5];
+    int* colp = acol + sbase + lane;
+    double* valp = aval + sbase * DD + lane;
+
+    const int ti = type[i];
+    const double mui = P.mu[ti];
+    double xi[3], vi[3];
+    load_vec<D>(pos, i, xi);
+    load_vec<D>(vel, i, vi);
+    const double rV2 = P.rV * P.rV;
+
+    // this row's P-list and C rows (used by every merge-join of the row)
+    const long long pbi = nptrP[i];
+    const int npi = ncp[i];
+    const int* Pi = nindP + pbi;
+    const double* Ci = cval + pbi * D;
+
+    // level-0 stencil bookkeeping
+    int gi[3];
+    {
+        int ic[3];
+        key_coords(P, key[i], ic);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gi[d] = ic[d] - M.mn[d];
+    }
+    double* prow = part + (size_t)i * M.S * DD;
+    if (M.folded) {
+        for (int t = 0; t < M.S * DD; ++t) prow[t] = 0.0;
+    }
+    unsigned long long touched = 0ull;
+    int run_slot = -1;
+    double run[D][D];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int s = 0; s < D; ++s) run[r][s] = 0.0;
+
+    double selfc[D][D];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int s = 0; s < D; ++s) selfc[r][s] = 0.0;
+    double sumvec[3] = {0, 0, 0};
+    int self = 0;
+
+    const long long nb = nptr[i];
+    const int n = nc[i];
+    const int nf = nfc[i];
+    for (int k = 0; k < n; ++k) {
+        const int j = nind[nb + k];
+        if (j == i) { self = k; continue; }
+        double V[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) V[r][s] = 0.0;
+        double xj[3], q[3];
+        load_vec<D>(pos, j, xj);
+        sep_vec<D>(P, xj, xi, q);
+        const double r2 = norm2_exact<D>(q);
+        const bool fluid = k < nf;
+        if (r2 != 0.0 && rV2 - r2 > 0) {
+            const double dij = sqrt(r2);
+            const double wd = -dw_quad(P.kfv, dij, P.rV);
+            const double muj = P.mu[type[j]];
+            const double muij = 2.0 * (mui * muj) / (mui + muj);
+            const double inv = 1.0 / dij;
+            double e[3];
+#pragma unroll
+            for (int d = 0; d < D; ++d) e[d] = q[d] * inv;
+            const double f = P.visc * muij * wd * inv;
+            double vj[3];
+            if (!fluid) load_vec<D>(vel, j, vj);
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) {
+                    const double coef = f * e[s] * e[r];
+                    selfc[r][s] += coef;
+                    V[r][s] = coef;
+                    if (!fluid) sumvec[r] += coef * vj[s];
+                }
+        }
+        if (!fluid) continue;
+        // C Lambda C^T for the pair (i, j): merge-join of the sorted P-lists
+        double cc[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) cc[r][s] = 0.0;
+        {
+            const long long pbj = nptrP[j];
+            const int npj = ncp[j];
+            const int* Pj = nindP + pbj;
+            const double* Cj = cval + pbj * D;
+            int a = 0, b = 0;
+            int ka = a < npi ? Pi[a] : 0, kb = b < npj ? Pj[b] : 0;
+            while (a < npi && b < npj) {
+                if (ka == kb) {
+                    const double lam = P.lambda[type[ka]];
+                    double ci[3], cj[3];
+#pragma unroll
+                    for (int r = 0; r < D; ++r) { ci[r] = Ci[(long long)a * D + r] * lam; cj[r] = Cj[(long long)b * D + r]; }
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int s = 0; s < D; ++s) cc[r][s] += ci[r] * cj[s];
+                    ++a; ++b;
+                    ka = a < npi ? Pi[a] : 0;
+                    kb = b < npj ? Pj[b] : 0;
+                } else if (ka < kb) {
+                    ++a;
+                    ka = a < npi ? Pi[a] : 0;
+                } else {
+                    ++b;
+                    kb = b < npj ? Pj[b] : 0;
+                }
+            }
+        }
+        double blk[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) blk[r][s] = -V[r][s] + cc[r][s];
+        colp[(long long)k * 32] = j;
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) valp[((long long)k * DD + r * D + s) * 32] = blk[r][s];
+        // per-cell partial sums of the row (runs of equal stencil slot)
+        const int slot = stencil_slot<D>(P, M, gi, key[j]);
+        if (slot != run_slot) {
+            if (run_slot >= 0) {
+                flush_part<D>(prow, run_slot, run, M.folded != 0);
+                touched |= 1ull << run_slot;
+            }
+            run_slot = slot;
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) run[r][s] = blk[r][s];
+        } else {
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) run[r][s] += blk[r][s];
+        }
+    }
+    if (run_slot >= 0) {
+        flush_part<D>(prow, run_slot, run, M.folded != 0);
+        touched |= 1ull << run_slot;
+    }
+    // self block: viscous sum, inertia, C Lambda C^T(i, i)
+    const double m = P.density[ti] * P.vol;
+    const double inert = m / P.vol / P.dt;
+    {
+        double cc[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) cc[r][s] = 0.0;
+        for (int a = 0; a < npi; ++a) {
+            const double lam = P.lambda[type[Pi[a]]];
+            double ci[3];
+#pragma unroll
+            for (int r = 0; r < D; ++r) ci[r] = Ci[(long long)a * D + r];
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) cc[r][s] += ci[r] * lam * ci[s];
+        }
+        double blk[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) blk[r][s] = (selfc[r][s] + (r == s ? inert : 0.0)) + cc[r][s];
+        colp[(long long)self * 32] = i;
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int s = 0; s < D; ++s) valp[((long long)self * DD + r * D + s) * 32] = blk[r][s];
+#pragma unroll
+        for (int r = 0; r < D; ++r) invDiag[(size_t)i * D + r] = blk[r][r] != 0.0 ? 1.0 / blk[r][r] : 0.0;
+        selfk_out[i] = self;
+        // the own cell's slot received this row's other blocks already
+        const int cslot = stencil_slot<D>(P, M, gi, key[i]);
+        if (M.folded || (touched >> cslot) & 1ull) {
+            double* dst = prow + (size_t)cslot * DD;
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) dst[r * D + s] += blk[r][s];
+        } else {
+            flush_part<D>(prow, cslot, blk, false);
+        }
+        touched |= 1ull << cslot;
+    }
+    if (!M.folded) {
+        for (int t = 0; t < M.S; ++t) {
+            if ((touched >> t) & 1ull) continue;
+            double* dst = prow + (size_t)t * DD;
+#pragma unroll
+            for (int r = 0; r < DD; ++r) dst[r] = 0.0;
+        }
+    }
+    // right-hand side: wall terms, inertia, then b -= C p
+    double bv[3];
+#pragma unroll
+    for (int r = 0; r < D; ++r) bv[r] = sumvec[r] + inert * vi[r];
+    for (int a = 0; a < npi; ++a) {
+        const double pj = pvec[Pi[a]];
+#pragma unroll
+        for (int r = 0; r < D; ++r) bv[r] -= Ci[(long long)a * D + r] * pj;
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] = bv[r];
+}
+
+// ---- launcher ---------------------------------------------------------------
+static int ensure(void** p, long long* cap, long long need, size_t elem)
+{
+    if (need <= *cap) return MPH_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const long long n = need + need / 8 + 1024;
+    cudaError_t e = cudaMalloc(p, (size_t)n * elem);
+    if (e != cudaSuccess) return cuda_check(e, "cudaMalloc(assembly)");
+    *cap = n;
+    return MPH_OK;
+}
+
+int launch_assemble(mph_case* c)
+{
+    const DevParams& P = c->dp;
+    const int Nf = P.Nf;
+    const int D = c->dim;
+    // slice pointers
+    c->nslices = (Nf + 31) / 32;
+    k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth);
+    MPH_TRY(launch_scan_i32_to_i64(c, c->d.swidth, c->d.sptr, c->nslices));
+    long long h_slots = 0;
+    MPH_CUDA(cudaMemcpyAsync(&h_slots, c->d.sptr + c->nslices, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    c->nslots = h_slots;
+    {
+        long long cap = c->d.cap_slots;
+        void* p = c->d.acol;
+        MPH_TRY(ensure(&p, &cap, h_slots, sizeof(int)));
+        c->d.acol = (int*)p;
+        if (cap != c->d.cap_slots) {
+            if (c->d.aval) cudaFree(c->d.aval);
+            c->d.aval = nullptr;
+            MPH_CUDA(cudaMalloc(&c->d.aval, (size_t)cap * D * D * sizeof(double)));
+            if (c->precision == MPH_PRECISION_MIXED) {
+                if (c->d.aval32) cudaFree(c->d.aval32);
+                c->d.aval32 = nullptr;
+                MPH_CUDA(cudaMalloc(&c->d.aval32, (size_t)cap * D * D * sizeof(float)));
+            }
+            c->d.cap_slots = cap;
+        }
+    }
+    // C values for the fluid rows (aligned with the P-list)
+    long long h_cn = 0;
+    MPH_CUDA(cudaMemcpyAsync(&h_cn, c->d.nptrP + Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    {
+        void* p = c->d.cval;
+        MPH_TRY(ensure(&p, &c->d.cap_cval, h_cn * D, sizeof(double)));
+        c->d.cval = (double*)p;
+    }
+    const unsigned gf = grid_for(Nf, 128);
+    const unsigned ga = grid_for(P.N, 128);
+    Level0Map M{};
+    const mph::LevelGeom& g0 = c->lv[0];
+    M.S = 1;
+    M.folded = 0;
+    for (int d = 0; d < 3; ++d) {
+        M.mn[d] = g0.mn[d];
+        M.cnt[d] = g0.cnt[d];
+        M.st[d] = g0.st[d];
+        M.S *= g0.st[d];
+        if (d < D && g0.cnt[d] < 3) M.folded = 1;
+    }
+    if (D == 2) {
+        k_matrix_c<2><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval);
+        k_vector_p<2><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec);
+        k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
+                                                 c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
+                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part);
+    } else {
+        k_matrix_c<3><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval);
+        k_vector_p<3><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec);
+        k_matrix_a<3><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
+                                                 c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
+                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part);
+    }
+    return MPH_OK;
+}
+
+}  // namespace mph

@@ -1,0 +1,121 @@
+// mph_capi.cpp - the extern "C" boundary (include/mph_gb300.h).  Every entry
+// point catches C++ exceptions and turns them into status codes.
+#include <exception>
+#include <new>
+
+#include "mph_internal.h"
+
+namespace mph {
+int read_data(const char* path, mph_params* o);
+int read_grid(const char* path, mph_particles* o);
+int write_prof(const char* path, const mph_particles* p);
+int case_write_prof(mph_case* c, const char* path);
+int case_write_vtk(mph_case* c, const char* path);
+}  // namespace mph
+
+#define GUARD(expr)                                                              \
+    try {                                                                        \
+        return (expr);                                                           \
+    } catch (const std::bad_alloc&) {                                            \
+        return mph::fail(MPH_ERR_NOMEM, "host allocation failed");               \
+    } catch (const std::exception& e) {                                          \
+        return mph::fail(MPH_ERR_STATE, e.what());                               \
+    } catch (...) {                                                              \
+        return mph::fail(MPH_ERR_STATE, "unknown exception");                    \
+    }
+
+#define NEED(c) if (!(c)) return mph::fail(MPH_ERR_ARG, "null case handle")
+
+extern "C" {
+
+int mph_read_data(const char* path, mph_params* out) { GUARD(mph::read_data(path, out)) }
+int mph_read_grid(const char* path, mph_particles* out) { GUARD(mph::read_grid(path, out)) }
+int mph_write_prof(const char* path, const mph_particles* parts) { GUARD(mph::write_prof(path, parts)) }
+int mph_case_write_vtk(mph_case* c, const char* path) { NEED(c); GUARD(mph::case_write_vtk(c, path)) }
+int mph_case_write_prof(mph_case* c, const char* path) { NEED(c); GUARD(mph::case_write_prof(c, path)) }
+
+int mph_case_create(const mph_params* prm, const mph_particles* parts, int dim, int precision, void* stream, mph_case** out)
+{
+    GUARD(mph::case_create(prm, parts, dim, precision, stream, out))
+}
+int mph_case_destroy(mph_case* c) { GUARD(mph::case_destroy(c)) }
+int mph_case_set_stream(mph_case* c, void* stream)
+{
+    NEED(c);
+    c->stream = (cudaStream_t)stream;
+    return MPH_OK;
+}
+
+int mph_step(mph_case* c, int nsteps)
+{
+    NEED(c);
+    if (nsteps < 0) return mph::fail(MPH_ERR_ARG, "negative step count");
+    GUARD(mph::case_step(c, nsteps))
+}
+
+int mph_batch_step(mph_case** cases, int ncases, int nsteps)
+{
+    if (!cases || ncases < 0) return mph::fail(MPH_ERR_ARG, "bad case list");
+    try {
+        int last = MPH_OK;
+        for (int s = 0; s < nsteps; ++s)
+            for (int k = 0; k < ncases; ++k) {
+                NEED(cases[k]);
+                const int st = mph::case_step(cases[k], 1);
+                if (st != MPH_OK && st != MPH_ERR_NOT_CONVERGED) return st;
+                if (st != MPH_OK) last = st;
+            }
+        return last;
+    } catch (...) {
+        return mph::fail(MPH_ERR_STATE, "exception in batch step");
+    }
+}
+
+int mph_case_count(mph_case* c, int* count, int* fluid_count)
+{
+    NEED(c);
+    if (count) *count = c->dp.N;
+    if (fluid_count) *fluid_count = c->dp.Nf;
+    return MPH_OK;
+}
+int mph_case_time(mph_case* c, double* time)
+{
+    NEED(c);
+    if (time) *time = c->time;
+    return MPH_OK;
+}
+int mph_get_fields(mph_case* c, mph_fields* out) { NEED(c); GUARD(mph::case_get_fields(c, out)) }
+int mph_get_solve_stats(mph_case* c, mph_solve_stats* out)
+{
+    NEED(c);
+    if (!out) return mph::fail(MPH_ERR_ARG, "null output");
+    *out = c->stats;
+    return MPH_OK;
+}
+
+int mph_stage_step_begin(mph_case* c) { NEED(c); GUARD(mph::stage_step_begin(c)) }
+int mph_stage_cellsort(mph_case* c) { NEED(c); GUARD(mph::stage_cellsort(c)) }
+int mph_stage_neighbors(mph_case* c) { NEED(c); GUARD(mph::stage_neighbors(c)) }
+int mph_stage_explicit(mph_case* c) { NEED(c); GUARD(mph::stage_explicit(c)) }
+int mph_stage_assemble(mph_case* c) { NEED(c); GUARD(mph::stage_assemble(c)) }
+int mph_stage_mg_build(mph_case* c) { NEED(c); GUARD(mph::stage_mg_build(c)) }
+int mph_stage_solve(mph_case* c) { NEED(c); GUARD(mph::stage_solve(c)) }
+int mph_stage_step_end(mph_case* c) { NEED(c); GUARD(mph::stage_step_end(c)) }
+int mph_stage_output_fields(mph_case* c) { NEED(c); GUARD(mph::stage_output_fields(c)) }
+
+int mph_case_set_state(mph_case* c, const mph_particles* parts, const double* wall_center)
+{
+    NEED(c);
+    GUARD(mph::case_set_state(c, parts, wall_center))
+}
+int mph_export(mph_case* c, const char* name, void* dst, long* count, int* kind)
+{
+    NEED(c);
+    GUARD(mph::case_export(c, name, dst, count, kind))
+}
+int mph_scalars(mph_case* c, double* out, int n) { NEED(c); GUARD(mph::case_scalars(c, out, n)) }
+const char* mph_scalar_names(void) { return mph::scalar_names(); }
+const char* mph_last_error(void) { return mph::last_error(); }
+const char* mph_version(void) { return "mph_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+// mph_internal.h - internal types of the GB300 MPH-I engine.
+//
+// Device data layout (DIM = D in {2,3}; particles in cell order, fluid first):
+//   positions / velocities / forces : double[N][VS], VS = 2 (2D) or 4 (3D,
+//                                      padded so one particle is one 32-byte sector)
+//   pos32                           : float[N][VS] copy used only to pre-classify
+//                                      neighbour candidates (exact FP64 decides
+//                                      every pair near a radius)
+//   neighbour lists                 : CSR, int64 row pointers, int32 columns,
+//                                      as the reference (main.cpp:92-97)
+//   matrix A                        : sliced ELL of DxD blocks, 32 block rows per
+//                                      slice, slice width = longest row; inside a
+//                                      slice value (k, comp, lane) sits at
+//                                      base + (k*D*D + comp)*32 + lane, so a warp
+//                                      (one lane per row) reads 256 contiguous bytes
+//   matrix C                        : per fluid particle, D values per P-neighbour,
+//                                      aligned with the P-list (row-contiguous)
+//   multigrid level L               : dense 3^D-cell block stencil per grid cell,
+//                                      value (cell, r, slot, s) at
+//                                      ((cell*D + r)*S + slot)*D + s, S = 3^D.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mph_gb300.h"
+
+namespace mph {
+
+constexpr int kTypeCount = 4;
+constexpr int kSliceRows = 32;         // rows per sliced-ELL slice (one warp)
+constexpr int kMaxLevels = 24;
+
+// Parameters every kernel reads, passed by value.
+struct DevParams {
+    int dim;
+    int N, Nf, nPow, powExp;
+    int cc[3], T;
+    double dmin[3], dw[3], hw[3], wsafe[3];   // wsafe: Mod fast-path bound
+    double cw[3];
+    double l0, vol, dt;
+    double rA, rG, rP, rV, maxR;
+    double maxR2, rP2;
+    double kfa, kfg, kfp, kfv;                 // (1/Sw)/h^dim per kernel
+    double N0a, N0p, R2g, cofK;
+    double cofA[kTypeCount];
+    double density[kTypeCount], bulk[kTypeCount], lambda[kTypeCount], mu[kTypeCount];
+    double ratio[kTypeCount][kTypeCount];
+    double gravity[3];
+    double visc;                               // 8 (2D) or 10 (3D)
+    float maxR2_lo, maxR2_hi, rP2_lo, rP2_hi;  // FP32 pre-classification band
+    float w32[3], hw32[3];
+    int exact_only;                            // 1: skip the FP32 pre-classification
+    int surface;                               // 1 if any CofA != 0
+};
+
+struct LevelGeom {
+    int mn[3], mx[3], cnt[3], st[3];
+    int cells, rows;      // rows = D*cells
+    long off_vec;         // offset into the level vector pool (rows)
+    long off_cof;         // offset into the level coefficient pool
+};
+
+// Device buffers of one case.
+struct DeviceState {
+    // particles
+    double *pos = nullptr, *vel = nullptr, *force = nullptr;
+    double *pos_alt = nullptr, *vel_alt = nullptr;
+    float* pos32 = nullptr;
+    int *type = nullptr, *id = nullptr, *type_alt = nullptr, *id_alt = nullptr;
+    double *densA = nullptr, *gcen = nullptr, *presA = nullptr, *vsp = nullptr;
+    double *divP = nullptr, *presP = nullptr, *virP = nullptr, *virS = nullptr;
+    // cell list
+    int *key = nullptr, *perm = nullptr, *bucket = nullptr;   // bucket: [2T+1] starts
+    // neighbours
+    int *nc = nullptr, *nfc = nullptr, *ncp = nullptr;
+    long long *nptr = nullptr, *nptrP = nullptr;
+    int *nind = nullptr, *nindP = nullptr;
+    long long cap_nind = 0, cap_nindP = 0;
+    // matrix A (sliced ELL)
+    long long *sptr = nullptr;     // [nslices+1], block slots
+    int* swidth = nullptr;         // [nslices]
+    int* acol = nullptr;           // [slots]
+    double* aval = nullptr;        // [slots*D*D]
+    float* aval32 = nullptr;       // mixed precision copy
+    long long cap_slots = 0;
+    double *bvec = nullptr, *invDiag = nullptr;
+    int* selfk = nullptr;          // position of the self block in each row
+    // matrix C and source p
+    double *cval = nullptr, *pvec = nullptr;
+    long long cap_cval = 0;
+    // level-0 partial stencils per fluid row: [Nf][S][D*D]
+    double* part = nullptr;
+    // multigrid
+    double *mg_cof = nullptr, *mg_invd = nullptr;
+    double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr;
+    float *mg_cof32 = nullptr, *mg_invd32 = nullptr;
+    long long cap_mg_cof = 0, cap_mg_vec = 0;
+    // solver vectors [D*Nf]
+    double *x = nullptr, *r = nullptr, *s = nullptr, *y = nullptr, *p = nullptr, *q = nullptr, *u = nullptr;
+    double* partials = nullptr;     // block partial sums for reductions
+    double* scal = nullptr;         // solver scalars on device
+    int* flags = nullptr;           // device status flags
+    // misc
+    int* bbox = nullptr;            // fluid-cell bounding box (6 ints)
+    long long* totals = nullptr;    // scan totals read back by the host
+    void* scan_tmp = nullptr;
+    size_t scan_tmp_bytes = 0;
+};
+
+}  // namespace mph
+
+// Opaque handle of the C ABI.
+struct mph_case {
+    int dim = 3;
+    int precision = MPH_PRECISION_FP64;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    mph_params prm{};
+    mph::DevParams dp{};
+    double time = 0.0;
+    double z_plane = 0.0;               // z of every particle of a 2D case
+    double wallC[4][3]{}, wallV[4][3]{}, wallW[4][3]{}, wallR[4][3][3]{};
+    double Swa = 1, Swg = 1, Swp = 1, Swv = 1;
+    int fB = 0, fE = 0, wB = 0, wE = 0;
+    long long nnb = 0, nnbP = 0;        // neighbour list totals of the current step
+    int nslices = 0;
+    long long nslots = 0;
+    int depth = 0;
+    std::vector<mph::LevelGeom> lv;
+    long mg_rows_total = 0, mg_cof_total = 0;
+    int bbox[6]{};
+    // stage bookkeeping
+    int stage = 0;                      // last completed stage
+    bool have_output = false;
+    mph_solve_stats stats{};
+    int iter_cap = 0;
+    mph::DeviceState d;
+    std::vector<void*> allocations;
+};
+
+namespace mph {
+
+// error helper: set the thread-local message and return the status
+int fail(int status, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+
+#define MPH_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return ::mph::cuda_check(e_, #call); \
+    } while (0)
+
+#define MPH_TRY(call)                  \
+    do {                               \
+        int s_ = (call);               \
+        if (s_ != MPH_OK) return s_;   \
+    } while (0)
+
+// host-side case API (mph_case.cu)
+int case_create(const mph_params* prm, const mph_particles* parts, int dim, int precision, void* stream, mph_case** out);
+int case_destroy(mph_case* c);
+int case_step(mph_case* c, int nsteps);
+const char* last_error();
+int case_export(mph_case* c, const char* name, void* dst, long* count, int* kind);
+int case_scalars(mph_case* c, double* out, int n);
+const char* scalar_names();
+int case_get_fields(mph_case* c, mph_fields* out);
+int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_center);
+
+// host-side stages (mph_case.cu)
+int case_alloc_particles(mph_case* c);
+int stage_step_begin(mph_case* c);
+int stage_cellsort(mph_case* c);
+int stage_neighbors(mph_case* c);
+int stage_explicit(mph_case* c);
+int stage_assemble(mph_case* c);
+int stage_mg_build(mph_case* c);
+int stage_solve(mph_case* c);
+int stage_step_end(mph_case* c);
+int stage_output_fields(mph_case* c);
+
+// kernel launchers (k_*.cu)
+void launch_step_begin(mph_case* c);
+void launch_cell_keys(mph_case* c);
+void launch_bitonic_sort(mph_case* c);
+void launch_cell_ranges_and_permute(mph_case* c);
+void launch_fluid_bbox(mph_case* c);
+void launch_neighbor_count(mph_case* c);
+int launch_scan_i32_to_i64(mph_case* c, const int* in, long long* out, int n);
+void launch_neighbor_fill(mph_case* c);
+void launch_explicit(mph_case* c);
+void launch_explicit_density_only(mph_case* c);
+void launch_output_fields(mph_case* c);
+int launch_assemble(mph_case* c);
+void launch_mg_level0(mph_case* c);
+void launch_mg_coarse(mph_case* c, int L);
+void launch_mg_invd(mph_case* c);
+int run_cr_solve(mph_case* c);
+int run_mixed_solve(mph_case* c);
+bool mixed_available();
+
+}  // namespace mph

@@ -1,0 +1,126 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol declared
+in include/*.h, and its host-only entry points (file formats, argument
+checks) behave like the reference's readers and writers."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from mphimplicit_gb300 import build, casegen, engine
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return engine.load_library()
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(mph_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version_and_error_string(lib):
+    assert b"sm_103a" in lib.mph_version()
+    assert lib.mph_step(None, 1) == 1            # MPH_ERR_ARG on a null handle
+    assert b"null" in lib.mph_last_error()
+
+
+def test_grid_and_data_roundtrip(tmp_path, lib):
+    p, parts = casegen.square_drop_2d(scale=0.05, seed=7)
+    p.surface_tension = (0.072, 0.0, 0.0, 0.0)
+    p.wall3 = (0.1, 0.2, 0.0, 0.01, 0.0, 0.0, 0.0, 0.0, 1.5)
+    d, g = casegen.write_case(str(tmp_path / "c"), p, parts)
+    q = engine.read_data(d)
+    assert q == p
+    back = engine.read_grid(g)
+    assert back.count == parts.count
+    assert np.array_equal(back.types, parts.types)
+    assert np.array_equal(back.pos, parts.pos) and np.array_equal(back.vel, parts.vel)
+    assert np.array_equal(back.domain_min, parts.domain_min) and np.array_equal(back.domain_max, parts.domain_max)
+
+
+def test_reference_data_keywords(tmp_path, lib):
+    # keyword lines as in the reference's sample files (two spaces after WallN)
+    txt = """#######
+Dt\t\t\t\t2.0e-3
+OutputInterval\t\t\t1.0
+VtkOutputInterval\t\t5.0e-2
+EndTime\t\t\t\t1.0
+RadiusRatioA\t\t\t\t\t3.5
+RadiusRatioP\t\t\t\t\t1.75
+RadiusRatioV\t\t\t\t\t3.5
+Density\t\t\t\t\t\t\t1.0e+3\t\t1.0e+3\t\t1.0e+3\t\t1.0e+3
+BulkModulus 1e6 1e6 1e6 1e6
+BulkViscosity 2e3 2e3 2e3 2e3
+ShearViscosity 1e3 1e3 1e3 1e3
+SurfaceTension 0 0 0 0
+InteractionRatio(Type0) 1 1 1 1
+InteractionRatio(Type1) 1 1 1 1
+InteractionRatio(Type2) 1 1 1 1
+InteractionRatio(Type3) 1 1 1 1
+Gravity                         0.0 -1.0 0.0
+Wall2    Center 0.0 0.0 0.0    Velocity 0.0 0.0 0.0    Omega 0.0 0.0 0.0
+Wall3    Center 1.0 2.0 3.0    Velocity 4.0 5.0 6.0    Omega 7.0 8.0 9.0
+Density 1 2 3
+garbage line
+"""
+    f = tmp_path / "x.data"
+    f.write_text(txt)
+    q = engine.read_data(str(f))
+    assert q.dt == 2.0e-3 and q.radius_ratio_p == 1.75 and q.density == (1000.0,) * 4   # 3-value line ignored
+    assert q.gravity == (0.0, -1.0, 0.0)
+    assert q.wall3 == (1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 7.0, 8.0, 9.0)
+
+
+def test_short_grid_is_an_error(tmp_path, lib):
+    f = tmp_path / "short.grid"
+    f.write_text("0.0\n3 0.01 0 1 0 1 0 1\n0 0.1 0.1 0 0 0 0\n")
+    with pytest.raises(engine.MphError) as e:
+        parts = casegen.Particles(0, 0, np.zeros(3), np.zeros(3), np.zeros(3, np.int32), np.zeros((3, 3)), np.zeros((3, 3)))
+        from mphimplicit_gb300.cabi import MphParticles, np_ptr
+        s = MphParticles()
+        s.count = 3
+        s.type = np_ptr(parts.types, ctypes.c_int)
+        s.pos = np_ptr(parts.pos)
+        s.vel = np_ptr(parts.vel)
+        engine._check(lib.mph_read_grid(str(f).encode(), ctypes.byref(s)))
+    assert e.value.status == 2
+    with pytest.raises(engine.MphError):
+        engine.read_grid(str(tmp_path / "missing.grid"))
+
+
+def test_case_validation_without_gpu(lib):
+    """Inputs the reference cannot run are refused before any device work."""
+    p, parts = casegen.square_drop_2d(scale=0.05)
+    bad = casegen.Particles(parts.time, parts.spacing, parts.domain_min, parts.domain_max,
+                            parts.types.copy(), parts.pos.copy(), parts.vel.copy())
+    bad.types[0] = 7
+    with pytest.raises(engine.MphError) as e:
+        engine.Case(p, bad, 2)
+    assert e.value.status == 3
+    bad = casegen.Particles(parts.time, parts.spacing, parts.domain_min, parts.domain_max,
+                            parts.types.copy(), parts.pos.copy(), parts.vel.copy())
+    bad.vel[0, 2] = 1.0   # a z velocity in a 2D case
+    with pytest.raises(engine.MphError) as e:
+        engine.Case(p, bad, 2)
+    assert e.value.status == 3
+    with pytest.raises(engine.MphError) as e:
+        engine.Case(p, parts, 4)
+    assert e.value.status == 1
