@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Throughput of the MPH-I time step on GB300 (particle-steps/s).
+
+Workload (default): the 3D cube collapse of 100^3 fluid particles (l0 =
+0.005 m) in a 3-layer wall tank around a 160x110x110 interior, gravity -9.8 in
+z, dt = 5e-5 s, lambda*dt/(rho*l0^2) = 100, seeded +-0.01 l0 jitter:
+1,297,696 particles.  Synthetic inputs generated here stand in for the case
+files.  One step = the full reference step (sort, neighbours, explicit
+physics, assembly, multigrid build, CR solve).
+
+  value : particle-steps/s with the state resident in HBM, CUDA events on the
+          case stream around K steps (the matrix alone is ~14 GB, far above L2)
+  e2e   : the same metric through the public API with host buffers: every
+          step uploads the particle state (mph_case_set_state) and reads back
+          positions and velocities (mph_get_fields)
+  --impl reference : the CPU restatement of the reference (the oracle,
+          OpenMP over all host cores) on a bounded sample of the workload
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [REPO, os.path.join(REPO, "oracle")]
+
+from mphimplicit_gb300 import casegen  # noqa: E402
+
+METRIC = "particle-steps/sec at <=1e-6 rel. err vs FP64 (mixed/batched vs plain GPU); p50/p99 step ms"
+UNIT = "particle-steps/s"
+
+
+def workload(name: str):
+    if name == "cube3d_100":
+        p, parts = casegen.cube_collapse_3d(100, seed=0)
+        return 3, p, parts, "3D cube collapse, 100^3 fluid in a 3-layer tank around 160x110x110 (config 1)"
+    m = re.match(r"cube3d_(\d+)$", name)
+    if m:
+        n = int(m.group(1))
+        p, parts = casegen.cube_collapse_3d(n, seed=0)
+        return 3, p, parts, f"3D cube collapse, {n}^3 fluid (config-1 geometry scaled)"
+    if name == "dam2d_100":
+        p, parts = casegen.square_drop_2d(1.0, seed=0)
+        return 2, p, parts, "2D dam, 100x100 fluid in a 3-layer box around 200x150 (config 0)"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` on the bench workload from the
+    committed ncu summary (profiles/), or None."""
+    path = os.path.join(REPO, "profiles", f"{kernel}_cube3d_100.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_launch_full:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.TemporaryFile(mode="w+")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def spmv_bytes(prof, scal, dim):
+    """Algorithmic bytes of one block SpMV: every block once (D*D values + a
+    column index), row lengths and slice pointers, x once, y written once."""
+    nf = int(scal["FluidParticleEnd"])
+    blocks = scal["NonzeroCountA"] / (dim * dim)
+    nsl = (nf + 31) // 32
+    return blocks * (dim * dim * 8 + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * 8
+
+
+def assemble_bytes(prof, scal, dim):
+    nf = int(scal["FluidParticleEnd"])
+    n = int(scal["ParticleCount"])
+    blocks = scal["NonzeroCountA"] / (dim * dim)
+    return (blocks * (dim * dim * 8 + 4) + 4 * prof["nnb"] + 4 * prof["nnbP"] + 64 * n
+            + dim * 8 * scal["NonzeroCountC"] / dim)
+
+
+def cpu_sample(threads: int, steps: int = 1, fluid: int = 60, check_gpu: bool = False):
+    """Time the oracle (OpenMP, `threads` threads) on the config-1 geometry
+    scaled to `fluid`^3 fluid particles; optionally run the GPU engine on the
+    same sample and report its velocity error against the oracle."""
+    import oracle as orc
+    orc.build_oracle()
+    p, parts = casegen.cube_collapse_3d(fluid, seed=0)
+    o = orc.Oracle(p, parts, 3, threads=threads)
+    o.init()
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    out = {"value": parts.count * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"3D cube collapse {fluid}^3 fluid ({parts.count} particles), {steps} step(s) after the initial pass, "
+                     f"{dt:.1f} s wall"}
+    if check_gpu:
+        from mphimplicit_gb300 import engine
+        g = engine.Case(p, parts, 3)
+        g.step(steps)
+        vo = o.array("Velocity").reshape(-1, 3)[:g.fluid_count]
+        vg = g.export("Velocity").reshape(-1, 3)[:g.fluid_count]
+        ido, idg = o.array("ParticleIndex")[:g.fluid_count], g.export("ParticleIndex")[:g.fluid_count]
+        vo, vg = vo[np.argsort(ido)], vg[np.argsort(idg)]
+        out["gpu_err_vs_oracle"] = float(np.linalg.norm(vg - vo) / np.linalg.norm(vo))
+        out["iters_oracle_gpu"] = [o.solve_stats()["iter"], g.solve_stats()["iter"]]
+        g.close()
+    return out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    import oracle as orc
+    orc.build_oracle()
+    fluid = args.ref_fluid
+    p, parts = casegen.cube_collapse_3d(fluid, seed=0)
+    o = orc.Oracle(p, parts, 3, threads=threads)
+    o.init()
+    for _ in range(args.warmup):
+        o.step(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step(1)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = parts.count * args.steps / tot
+    sample = (f"3D cube collapse {fluid}^3 fluid ({parts.count} particles; config-1 geometry scaled down), "
+              f"{args.steps} timed steps after {args.warmup} warm-up steps")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "sample": sample, "threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cube3d_100")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-fluid", type=int, default=60)
+    ap.add_argument("--ref-fluid", type=int, default=50)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    from mphimplicit_gb300 import build, engine
+    from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
+    if rank == 0 or world == 1:
+        build.build()
+    if dist:
+        dist.barrier()
+    dim, params, parts, desc = workload(args.workload)
+    stream = torch.cuda.Stream()
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    case = engine.Case(params, parts, dim, precision=prec, stream=stream.cuda_stream)
+    N, Nf = case.count, case.fluid_count
+    for _ in range(args.warmup):
+        case.step(1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    case.profile(True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    iters = []
+    l0 = engine.launch_count()
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        evs[0].record(stream)
+        for k in range(args.steps):
+            case.step(1)
+            evs[k + 1].record(stream)
+            iters.append(case.solve_stats()["iter"])
+        torch.cuda.synchronize()
+    launches = engine.launch_count() - l0
+    if dist:
+        dist.barrier()
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_s = sum(step_ms) / 1000.0
+    prof = case.profile_read()
+    case.profile(False)
+    scal = case.scalars()
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = N * args.steps * world / total_s
+
+    # end to end through the public API with host buffers
+    fields = case.fields(("id", "type", "pos", "vel"))
+    host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
+                             fields["vel"])
+    ids = fields["id"]
+    wc = case.export("WallCenter")
+    vs = 2 if dim == 2 else 4
+    h2d = N * (vs * 8 * 2 + 4 + 4)
+    d2h = N * (vs * 8 * 2 + 4 + 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        case.set_state(host, ids, wc)
+        case.step(1)
+        f = case.fields(("id", "type", "pos", "vel"))
+        host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, f["type"], f["pos"], f["vel"])
+        ids = f["id"]
+        wc = case.export("WallCenter")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = N * args.e2e_steps * world / e2e_s
+
+    # roofline of the dominant kernel (CUDA events on the case stream)
+    peak, peak_kind = measured_peaks()
+    kern = {"spmv": ("k_spmv", spmv_bytes), "assemble_a": ("k_matrix_a", assemble_bytes)}
+    dom = max(kern, key=lambda k: prof[f"kern_ms_{k}"])
+    nlaunch = max(prof[f"kern_n_{dom}"], 1)
+    avg_s = prof[f"kern_ms_{dom}"] / 1000.0 / nlaunch
+    bytes_per = kern[dom][1](prof, scal, dim)
+    achieved = bytes_per / avg_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic(kern[dom][0]), "kernel": kern[dom][0], "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": bytes_per, "avg_launch_ms": avg_s * 1000.0, "launches": nlaunch}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample(os.cpu_count() or 1, 1, args.cpu_fluid, check_gpu=True)
+
+    stage_total = sum(prof[f"stage_ms_{s}"] for s in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == PRECISION_FP64 else "f32-inner/f64-outer", "data": "synthetic",
+        "config": {"workload": args.workload, "description": desc, "dim": dim, "particles": N, "fluid": Nf,
+                   "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (the block matrix alone exceeds 129 MB by ~100x)",
+                   "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+                   "cr_iterations": iters,
+                   "stage_ms_per_step": {s: prof[f"stage_ms_{s}"] / args.steps for s in
+                                         ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve")},
+                   "stage_sum_ms_per_step": stage_total / args.steps},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": args.e2e_steps},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    case.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

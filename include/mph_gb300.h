@@ -177,6 +177,21 @@ int mph_export(mph_case* c, const char* name, void* dst, long* count, int* kind)
 int mph_scalars(mph_case* c, double* out, int n);
 const char* mph_scalar_names(void);
 
+/* Measurement support (no counterpart in the reference, which times its
+ * phases with clock(), main.cpp:310-311 and 480-491).
+ * mph_case_profile: enable (1) / disable (0) CUDA-event timing on the case
+ * stream and reset the accumulators.
+ * mph_case_profile_read: fills out[] with the accumulated milliseconds of the
+ * stages step_begin, cellsort, neighbors, explicit, assemble, mg_build, solve
+ * (7 values), then the milliseconds and launch counts of the kernel classes
+ * SpMV, V-cycle, A assembly, neighbour search (4 + 4 values), then the
+ * sliced-ELL slot count, the neighbour and P-neighbour list lengths of the
+ * last step.  Returns the number of values available. */
+int mph_case_profile(mph_case* c, int enable);
+int mph_case_profile_read(mph_case* c, double* out, int n);
+/* Number of kernel launches this library has issued since it was loaded. */
+long long mph_launch_count(void);
+
 const char* mph_last_error(void);
 const char* mph_version(void);
 

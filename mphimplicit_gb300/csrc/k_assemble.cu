@@ -394,7 +394,7 @@ int launch_assemble(mph_case* c)
     const int D = c->dim;
     // slice pointers
     c->nslices = (Nf + 31) / 32;
-    k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth);
+    { k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth); MPH_COUNT_LAUNCH(); }
     MPH_TRY(launch_scan_i32_to_i64(c, c->d.swidth, c->d.sptr, c->nslices));
     long long h_slots = 0;
     MPH_CUDA(cudaMemcpyAsync(&h_slots, c->d.sptr + c->nslices, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
@@ -440,17 +440,23 @@ int launch_assemble(mph_case* c)
         if (d < D && g0.cnt[d] < 3) M.folded = 1;
     }
     if (D == 2) {
-        k_matrix_c<2><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval);
-        k_vector_p<2><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec);
-        k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
+        { k_matrix_c<2><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval); MPH_COUNT_LAUNCH(); }
+        { k_vector_p<2><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec); MPH_COUNT_LAUNCH(); }
+        cudaEvent_t pe = nullptr;
+        const int pon = prof_begin(c, 2, &pe);
+        { k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
                                                  c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
-                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part);
+                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
+        if (pon) prof_end(c, 2, pe);
     } else {
-        k_matrix_c<3><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval);
-        k_vector_p<3><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec);
-        k_matrix_a<3><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
+        { k_matrix_c<3><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval); MPH_COUNT_LAUNCH(); }
+        { k_vector_p<3><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec); MPH_COUNT_LAUNCH(); }
+        cudaEvent_t pe = nullptr;
+        const int pon = prof_begin(c, 2, &pe);
+        { k_matrix_a<3><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
                                                  c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
-                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part);
+                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
+        if (pon) prof_end(c, 2, pe);
     }
     return MPH_OK;
 }

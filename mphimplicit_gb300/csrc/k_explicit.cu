@@ -316,22 +316,22 @@ void launch_explicit(mph_case* c)
     const DevParams& P = c->dp;
     const unsigned g = grid_for(P.N, 128);
     if (c->dim == 2)
-        k_density<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp);
+        { k_density<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
     else
-        k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp);
-    k_pressure_a<<<grid_for(P.N, 256), 256, 0, c->stream>>>(P, c->d.type, c->d.densA, c->d.presA);
+        { k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
+    { k_pressure_a<<<grid_for(P.N, 256), 256, 0, c->stream>>>(P, c->d.type, c->d.densA, c->d.presA); MPH_COUNT_LAUNCH(); }
     if (P.surface) {
         if (c->dim == 2)
-            k_surface_forces<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.presA, c->d.gcen, c->d.force);
+            { k_surface_forces<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.presA, c->d.gcen, c->d.force); MPH_COUNT_LAUNCH(); }
         else
-            k_surface_forces<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.presA, c->d.gcen, c->d.force);
+            { k_surface_forces<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.presA, c->d.gcen, c->d.force); MPH_COUNT_LAUNCH(); }
     }
     const int nf = c->fE - c->fB;
     if (nf > 0) {
         if (c->dim == 2)
-            k_accelerate<2><<<grid_for(nf, 256), 256, 0, c->stream>>>(P, c->fB, c->fE, c->d.type, c->d.force, c->d.vel);
+            { k_accelerate<2><<<grid_for(nf, 256), 256, 0, c->stream>>>(P, c->fB, c->fE, c->d.type, c->d.force, c->d.vel); MPH_COUNT_LAUNCH(); }
         else
-            k_accelerate<3><<<grid_for(nf, 256), 256, 0, c->stream>>>(P, c->fB, c->fE, c->d.type, c->d.force, c->d.vel);
+            { k_accelerate<3><<<grid_for(nf, 256), 256, 0, c->stream>>>(P, c->fB, c->fE, c->d.type, c->d.force, c->d.vel); MPH_COUNT_LAUNCH(); }
     }
 }
 
@@ -341,9 +341,9 @@ void launch_explicit_density_only(mph_case* c)
     const DevParams& P = c->dp;
     const unsigned g = grid_for(P.N, 128);
     if (c->dim == 2)
-        k_density<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp);
+        { k_density<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
     else
-        k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp);
+        { k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_output_fields(mph_case* c)
@@ -351,13 +351,13 @@ void launch_output_fields(mph_case* c)
     const DevParams& P = c->dp;
     const unsigned g = grid_for(P.N, 128);
     if (c->dim == 2) {
-        k_div_pressure<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.nptr, c->d.nind, c->d.vsp, c->d.divP, c->d.presP);
-        k_output_forces<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind,
-                                                     c->d.nindP, c->d.presP, c->d.presA, c->d.gcen, c->d.force, c->d.virS, c->d.virP);
+        { k_div_pressure<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.nptr, c->d.nind, c->d.vsp, c->d.divP, c->d.presP); MPH_COUNT_LAUNCH(); }
+        { k_output_forces<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind,
+                                                     c->d.nindP, c->d.presP, c->d.presA, c->d.gcen, c->d.force, c->d.virS, c->d.virP); MPH_COUNT_LAUNCH(); }
     } else {
-        k_div_pressure<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.nptr, c->d.nind, c->d.vsp, c->d.divP, c->d.presP);
-        k_output_forces<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind,
-                                                     c->d.nindP, c->d.presP, c->d.presA, c->d.gcen, c->d.force, c->d.virS, c->d.virP);
+        { k_div_pressure<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.nptr, c->d.nind, c->d.vsp, c->d.divP, c->d.presP); MPH_COUNT_LAUNCH(); }
+        { k_output_forces<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.nc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind,
+                                                     c->d.nindP, c->d.presP, c->d.presA, c->d.gcen, c->d.force, c->d.virS, c->d.virP); MPH_COUNT_LAUNCH(); }
     }
 }
 

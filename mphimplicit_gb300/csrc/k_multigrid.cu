@@ -134,8 +134,8 @@ void launch_mg_level0(mph_case* c)
     const LevelK L = level_k(c, 0);
     const long long n = (long long)L.rows * L.width;
     double* cof = c->d.mg_cof + c->lv[0].off_cof;
-    if (c->dim == 2) k_mg_level0<2><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof);
-    else k_mg_level0<3><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof);
+    if (c->dim == 2) { k_mg_level0<2><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof); MPH_COUNT_LAUNCH(); }
+    else { k_mg_level0<3><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_mg_coarse(mph_case* c, int lvl)
@@ -144,16 +144,16 @@ void launch_mg_coarse(mph_case* c, int lvl)
     const long long n = (long long)L.rows * L.width;
     const double* cofS = c->d.mg_cof + c->lv[lvl - 1].off_cof;
     double* cofL = c->d.mg_cof + c->lv[lvl].off_cof;
-    if (c->dim == 2) k_mg_coarse<2><<<grid_for(n, 256), 256, 0, c->stream>>>(S_, L, cofS, cofL);
-    else k_mg_coarse<3><<<grid_for(n, 256), 256, 0, c->stream>>>(S_, L, cofS, cofL);
+    if (c->dim == 2) { k_mg_coarse<2><<<grid_for(n, 256), 256, 0, c->stream>>>(S_, L, cofS, cofL); MPH_COUNT_LAUNCH(); }
+    else { k_mg_coarse<3><<<grid_for(n, 256), 256, 0, c->stream>>>(S_, L, cofS, cofL); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_mg_invd(mph_case* c)
 {
     for (int l = 0; l < c->depth; ++l) {
         const LevelK L = level_k(c, l);
-        k_mg_invd<<<grid_for(L.rows, 256), 256, 0, c->stream>>>(L.rows, L.width, c->d.mg_cof + c->lv[l].off_cof,
-                                                               c->d.mg_invd + c->lv[l].off_vec);
+        { k_mg_invd<<<grid_for(L.rows, 256), 256, 0, c->stream>>>(L.rows, L.width, c->d.mg_cof + c->lv[l].off_cof,
+                                                               c->d.mg_invd + c->lv[l].off_vec); MPH_COUNT_LAUNCH(); }
     }
 }
 
@@ -292,30 +292,30 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     std::vector<T*> cur(depth), oth(depth);
     for (int l = 0; l < depth; ++l) { cur[l] = Sa + off_v(l); oth[l] = Sb + off_v(l); }
     auto jacobi = [&](int l) {
-        k_mg_jacobi<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + off_c(l), invd + off_v(l), Qp + off_v(l),
-                                                                     cur[l], oth[l], flags);
+        { k_mg_jacobi<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + off_c(l), invd + off_v(l), Qp + off_v(l),
+                                                                     cur[l], oth[l], flags); MPH_COUNT_LAUNCH(); }
         std::swap(cur[l], oth[l]);
     };
     // pre-smoothing, going down
-    k_mg_p2g<D, T, TQ><<<grid_for(L[0].rows, 128), 128, 0, st>>>(c->dp, L[0], c->d.bucket, q, invd + off_v(0), Qp + off_v(0),
-                                                                 cur[0], flags);
+    { k_mg_p2g<D, T, TQ><<<grid_for(L[0].rows, 128), 128, 0, st>>>(c->dp, L[0], c->d.bucket, q, invd + off_v(0), Qp + off_v(0),
+                                                                 cur[0], flags); MPH_COUNT_LAUNCH(); }
     jacobi(0);                                   // 2 sweeps on level 0
     for (int l = 1; l < depth; ++l) {
-        k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cof + off_c(l - 1), Qp + off_v(l - 1),
-                                                                       cur[l - 1], invd + off_v(l), Qp + off_v(l), cur[l], flags);
+        { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cof + off_c(l - 1), Qp + off_v(l - 1),
+                                                                       cur[l - 1], invd + off_v(l), Qp + off_v(l), cur[l], flags); MPH_COUNT_LAUNCH(); }
         const int sweeps = (l == depth - 1) ? 5 : 3;   // coarsest: 4 sweeps + one more update
         for (int k = 1; k < sweeps; ++k) jacobi(l);
     }
     // post-smoothing, going up
     for (int l = depth - 1; l >= 1; --l) {
-        k_mg_prolong<D, T><<<grid_for(L[l - 1].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cur[l], cur[l - 1], flags);
+        { k_mg_prolong<D, T><<<grid_for(L[l - 1].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cur[l], cur[l - 1], flags); MPH_COUNT_LAUNCH(); }
         const int sweeps = (l - 1 == 0) ? 2 : 3;
         for (int k = 0; k < sweeps; ++k) jacobi(l - 1);
     }
     const int n = c->dp.Nf * D;
     const int blocks = std::min<int>(grid_for(n, 256), kReduceBlocks);
-    k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
-                                                   (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags);
+    { k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
+                                                   (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags); MPH_COUNT_LAUNCH(); }
 }
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)

@@ -224,9 +224,9 @@ int launch_scan_i32_to_i64(mph_case* c, const int* in, long long* out, int n)
         MPH_CUDA(cudaMemsetAsync(out, 0, sizeof(long long), c->stream));
         return MPH_OK;
     }
-    k_scan_reduce<<<nb, kScanThreads, 0, c->stream>>>(in, n, bsum);
-    k_scan_blocks<<<1, kScanThreads, 0, c->stream>>>(bsum, nb);
-    k_scan_apply<<<nb, kScanThreads, 0, c->stream>>>(in, n, bsum, out);
+    { k_scan_reduce<<<nb, kScanThreads, 0, c->stream>>>(in, n, bsum); MPH_COUNT_LAUNCH(); }
+    { k_scan_blocks<<<1, kScanThreads, 0, c->stream>>>(bsum, nb); MPH_COUNT_LAUNCH(); }
+    { k_scan_apply<<<nb, kScanThreads, 0, c->stream>>>(in, n, bsum, out); MPH_COUNT_LAUNCH(); }
     return MPH_OK;
 }
 
@@ -246,11 +246,11 @@ void launch_neighbor_count(mph_case* c)
     neighbor_ranges(c, r);
     const unsigned g = grid_for(c->dp.N, 128);
     if (c->dim == 2)
-        k_neighbors<2, false><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
-                                                       c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, nullptr, nullptr, nullptr, nullptr);
+        { k_neighbors<2, false><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
+                                                       c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, nullptr, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     else
-        k_neighbors<3, false><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
-                                                       c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, nullptr, nullptr, nullptr, nullptr);
+        { k_neighbors<3, false><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
+                                                       c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, nullptr, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_neighbor_fill(mph_case* c)
@@ -259,11 +259,11 @@ void launch_neighbor_fill(mph_case* c)
     neighbor_ranges(c, r);
     const unsigned g = grid_for(c->dp.N, 128);
     if (c->dim == 2)
-        k_neighbors<2, true><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
-                                                      c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind, c->d.nindP);
+        { k_neighbors<2, true><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
+                                                      c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind, c->d.nindP); MPH_COUNT_LAUNCH(); }
     else
-        k_neighbors<3, true><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
-                                                      c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind, c->d.nindP);
+        { k_neighbors<3, true><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
+                                                      c->d.pos32, c->d.nc, c->d.nfc, c->d.ncp, c->d.nptr, c->d.nptrP, c->d.nind, c->d.nindP); MPH_COUNT_LAUNCH(); }
 }
 
 }  // namespace mph

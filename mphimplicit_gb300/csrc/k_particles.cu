@@ -201,16 +201,16 @@ void launch_step_begin(mph_case* c)
         }
     const unsigned g = grid_for(c->dp.N, 256);
     if (c->dim == 2)
-        k_step_begin<2><<<g, 256, 0, c->stream>>>(c->dp, W, c->d.pos, c->d.vel, c->d.force, c->fB, c->fE, c->wB, c->wE, c->d.type);
+        { k_step_begin<2><<<g, 256, 0, c->stream>>>(c->dp, W, c->d.pos, c->d.vel, c->d.force, c->fB, c->fE, c->wB, c->wE, c->d.type); MPH_COUNT_LAUNCH(); }
     else
-        k_step_begin<3><<<g, 256, 0, c->stream>>>(c->dp, W, c->d.pos, c->d.vel, c->d.force, c->fB, c->fE, c->wB, c->wE, c->d.type);
+        { k_step_begin<3><<<g, 256, 0, c->stream>>>(c->dp, W, c->d.pos, c->d.vel, c->d.force, c->fB, c->fE, c->wB, c->wE, c->d.type); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_cell_keys(mph_case* c)
 {
     const unsigned g = grid_for(c->dp.nPow, 256);
-    if (c->dim == 2) k_cell_keys<2><<<g, 256, 0, c->stream>>>(c->dp, c->d.pos, c->d.type, c->d.key, c->d.perm);
-    else k_cell_keys<3><<<g, 256, 0, c->stream>>>(c->dp, c->d.pos, c->d.type, c->d.key, c->d.perm);
+    if (c->dim == 2) { k_cell_keys<2><<<g, 256, 0, c->stream>>>(c->dp, c->d.pos, c->d.type, c->d.key, c->d.perm); MPH_COUNT_LAUNCH(); }
+    else { k_cell_keys<3><<<g, 256, 0, c->stream>>>(c->dp, c->d.pos, c->d.type, c->d.key, c->d.perm); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_bitonic_sort(mph_case* c)
@@ -222,15 +222,15 @@ void launch_bitonic_sort(mph_case* c)
     while ((1 << tileExp) < tile) ++tileExp;
     const int ntiles = n / tile;
     // every stage of m < tileExp stays inside a tile
-    k_bitonic_tile<<<ntiles, kTileThreads, 0, c->stream>>>(c->d.key, c->d.perm, tile, 0, (k < tileExp ? k : tileExp) - 1, 1);
+    { k_bitonic_tile<<<ntiles, kTileThreads, 0, c->stream>>>(c->d.key, c->d.perm, tile, 0, (k < tileExp ? k : tileExp) - 1, 1); MPH_COUNT_LAUNCH(); }
     for (int m = tileExp; m < k; ++m) {
         for (int s = 0; s <= m; ++s) {
             const int dist = 1 << (m - s);
             if (dist < tile) {
-                k_bitonic_tile<<<ntiles, kTileThreads, 0, c->stream>>>(c->d.key, c->d.perm, tile, m, m, dist);
+                { k_bitonic_tile<<<ntiles, kTileThreads, 0, c->stream>>>(c->d.key, c->d.perm, tile, m, m, dist); MPH_COUNT_LAUNCH(); }
                 break;
             }
-            k_bitonic_global<<<grid_for(n / 2, 256), 256, 0, c->stream>>>(c->d.key, c->d.perm, n / 2, m, dist);
+            { k_bitonic_global<<<grid_for(n / 2, 256), 256, 0, c->stream>>>(c->d.key, c->d.perm, n / 2, m, dist); MPH_COUNT_LAUNCH(); }
         }
     }
 }
@@ -238,14 +238,14 @@ void launch_bitonic_sort(mph_case* c)
 void launch_cell_ranges_and_permute(mph_case* c)
 {
     const int N = c->dp.N;
-    k_bucket_starts<<<grid_for(N + 1, 256), 256, 0, c->stream>>>(c->d.key, N, c->dp.T, c->d.bucket);
+    { k_bucket_starts<<<grid_for(N + 1, 256), 256, 0, c->stream>>>(c->d.key, N, c->dp.T, c->d.bucket); MPH_COUNT_LAUNCH(); }
     const unsigned g = grid_for(N, 256);
     if (c->dim == 2)
-        k_permute<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
-                                                c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32);
+        { k_permute<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
+                                                c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32); MPH_COUNT_LAUNCH(); }
     else
-        k_permute<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
-                                                c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32);
+        { k_permute<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
+                                                c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32); MPH_COUNT_LAUNCH(); }
     std::swap(c->d.id, c->d.id_alt);
     std::swap(c->d.type, c->d.type_alt);
     std::swap(c->d.pos, c->d.pos_alt);
@@ -254,7 +254,7 @@ void launch_cell_ranges_and_permute(mph_case* c)
 
 void launch_fluid_bbox(mph_case* c)
 {
-    k_fluid_bbox<<<grid_for(c->dp.T, 256), 256, 0, c->stream>>>(c->d.bucket, c->dp, c->d.bbox);
+    { k_fluid_bbox<<<grid_for(c->dp.T, 256), 256, 0, c->stream>>>(c->d.bucket, c->dp, c->d.bbox); MPH_COUNT_LAUNCH(); }
 }
 
 }  // namespace mph

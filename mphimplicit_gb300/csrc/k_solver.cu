@@ -167,11 +167,11 @@ static int cr_solve_t(mph_case* c)
     MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
 
-    k_cr_init<D><<<rb, kReduceThreads, 0, st>>>(Nf, c->d.type, c->d.vel, c->d.force, c->d.bvec, c->d.x, c->dp.density[0],
-                                                c->dp.density[1], c->dp.vol, c->dp.dt, part, counter, scal + kSRR0);
+    { k_cr_init<D><<<rb, kReduceThreads, 0, st>>>(Nf, c->d.type, c->d.vel, c->d.force, c->d.bvec, c->d.x, c->dp.density[0],
+                                                c->dp.density[1], c->dp.vol, c->dp.dt, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.bvec, c->d.s, scal + kSRS0);
-    k_spmv<D, 0><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.x, c->d.bvec, c->d.r, scal, flags, 0,
-                                     0, part, counter, scal + kSRR);
+    { k_spmv<D, 0><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.x, c->d.bvec, c->d.r, scal, flags, 0,
+                                     0, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.r, c->d.s, scal + kSQU);
 
     const int cap = n;   // the reference iterates at most N = D*Nf times
@@ -179,22 +179,34 @@ static int cr_solve_t(mph_case* c)
     int host_flags[kFlagCount];
     int it = 0;
     bool done = false;
+    // (iteration | class bit, events) of timed SpMV / V-cycle launches; only
+    // launches of iterations that ran are kept (later ones return at once)
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
     while (!done) {
         const int m = std::min(chunk, cap + 1 - it);
         for (int k = 0; k < m; ++k, ++it) {
-            k_spmv<D, 1><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.s, nullptr, c->d.y, scal, flags,
-                                             it, cap, part, counter, scal + rho_slot(it));
-            k_update_pq<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.s, c->d.y, c->d.p, c->d.q, scal, flags);
+            cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+            const bool pon = prof_begin(c, 0, &e[0]) != 0;
+            { k_spmv<D, 1><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.s, nullptr, c->d.y, scal, flags,
+                                             it, cap, part, counter, scal + rho_slot(it)); MPH_COUNT_LAUNCH(); }
+            if (pon) prof_begin(c, 0, &e[1]);
+            { k_update_pq<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.s, c->d.y, c->d.p, c->d.q, scal, flags); MPH_COUNT_LAUNCH(); }
+            if (pon) prof_begin(c, 1, &e[2]);
             vcycle_fp64(c, c->d.q, c->d.u, scal + kSQU);
-            k_update_xrs<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.x, c->d.r, c->d.s, c->d.p, c->d.q, c->d.u, scal, flags, part,
-                                                        counter);
+            if (pon) {
+                prof_begin(c, 1, &e[3]);
+                timed.push_back({it, {e[0], e[1]}});
+                timed.push_back({it | (1 << 30), {e[2], e[3]}});
+            }
+            { k_update_xrs<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.x, c->d.r, c->d.s, c->d.p, c->d.q, c->d.u, scal, flags, part,
+                                                        counter); MPH_COUNT_LAUNCH(); }
         }
         MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
         MPH_CUDA(cudaStreamSynchronize(st));
         done = host_flags[kFlagDone] != 0 || it > cap;
     }
-    k_dot<<<rb, kReduceThreads, 0, st>>>(n, c->d.r, c->d.s, part, counter, scal + kSRS);
-    k_store_velocity<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, c->d.x, c->d.vel);
+    { k_dot<<<rb, kReduceThreads, 0, st>>>(n, c->d.r, c->d.s, part, counter, scal + kSRS); MPH_COUNT_LAUNCH(); }
+    { k_store_velocity<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, c->d.x, c->d.vel); MPH_COUNT_LAUNCH(); }
     double hs[8];
     MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
     MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
@@ -205,6 +217,16 @@ static int cr_solve_t(mph_case* c)
     c->stats.rs0 = hs[kSRS0];
     c->stats.rs = hs[kSRS];
     c->stats.status = host_flags[kFlagBad] ? MPH_ERR_NAN : (host_flags[kFlagDone] && host_flags[kFlagIter] < cap ? MPH_OK : MPH_ERR_NOT_CONVERGED);
+    for (auto& t : timed) {
+        const int iter = t.first & ((1 << 30) - 1);
+        const int cls = (t.first >> 30) & 1;
+        if (iter < c->stats.iterations) {
+            c->prof.pending.push_back({cls, t.second});
+        } else {
+            c->prof.pool.push_back(t.second.first);
+            c->prof.pool.push_back(t.second.second);
+        }
+    }
     return MPH_OK;
 }
 

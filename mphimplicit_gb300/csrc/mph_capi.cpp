@@ -115,6 +115,14 @@ int mph_export(mph_case* c, const char* name, void* dst, long* count, int* kind)
 }
 int mph_scalars(mph_case* c, double* out, int n) { NEED(c); GUARD(mph::case_scalars(c, out, n)) }
 const char* mph_scalar_names(void) { return mph::scalar_names(); }
+int mph_case_profile(mph_case* c, int enable) { NEED(c); GUARD(mph::case_profile(c, enable)) }
+int mph_case_profile_read(mph_case* c, double* out, int n)
+{
+    NEED(c);
+    if (!out) return mph::fail(MPH_ERR_ARG, "null output");
+    GUARD(mph::case_profile_read(c, out, n))
+}
+long long mph_launch_count(void) { return mph::g_launch_count; }
 const char* mph_last_error(void) { return mph::last_error(); }
 const char* mph_version(void) { return "mph_gb300 0.1 (sm_103a)"; }
 

@@ -17,6 +17,53 @@
 namespace mph {
 
 static thread_local std::string g_error;
+long long g_launch_count = 0;
+
+// ---- profiling (CUDA events on the case stream) ------------------------------
+static cudaEvent_t take_event(mph_case* c)
+{
+    cudaEvent_t e;
+    if (!c->prof.pool.empty()) {
+        e = c->prof.pool.back();
+        c->prof.pool.pop_back();
+    } else {
+        cudaEventCreate(&e);
+    }
+    return e;
+}
+
+int prof_begin(mph_case* c, int k, cudaEvent_t* e0)
+{
+    (void)k;
+    if (!c->prof.on) return 0;
+    *e0 = take_event(c);
+    cudaEventRecord(*e0, c->stream);
+    return 1;
+}
+
+void prof_end(mph_case* c, int k, cudaEvent_t e0)
+{
+    if (!c->prof.on) return;
+    cudaEvent_t e1 = take_event(c);
+    cudaEventRecord(e1, c->stream);
+    c->prof.pending.push_back({k, {e0, e1}});
+}
+
+int prof_collect(mph_case* c)
+{
+    if (c->prof.pending.empty()) return MPH_OK;
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& p : c->prof.pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        c->prof.kern_ms[p.first] += ms;
+        c->prof.kern_n[p.first] += 1;
+        c->prof.pool.push_back(p.second.first);
+        c->prof.pool.push_back(p.second.second);
+    }
+    c->prof.pending.clear();
+    return MPH_OK;
+}
 
 int fail(int status, const std::string& msg)
 {
@@ -401,7 +448,10 @@ int stage_cellsort(mph_case* c)
 int stage_neighbors(mph_case* c)
 {
     const int N = c->dp.N;
+    cudaEvent_t pe = nullptr;
+    int pon = prof_begin(c, 3, &pe);
     launch_neighbor_count(c);
+    if (pon) prof_end(c, 3, pe);
     MPH_TRY(launch_scan_i32_to_i64(c, c->d.nc, c->d.nptr, N));
     MPH_TRY(launch_scan_i32_to_i64(c, c->d.ncp, c->d.nptrP, N));
     long long tot[2];
@@ -416,7 +466,9 @@ int stage_neighbors(mph_case* c)
     p = c->d.nindP;
     MPH_TRY(grow(&p, &c->d.cap_nindP, tot[1], sizeof(int)));
     c->d.nindP = (int*)p;
+    pon = prof_begin(c, 3, &pe);
     launch_neighbor_fill(c);
+    if (pon) prof_end(c, 3, pe);
     MPH_CUDA(cudaGetLastError());
     c->stage = 3;
     return MPH_OK;
@@ -539,6 +591,11 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_cof32,
                     (void*)d.mg_invd32, d.scan_tmp})
         if (p) cudaFree(p);
+    for (auto& p : c->prof.pending) {
+        cudaEventDestroy(p.second.first);
+        cudaEventDestroy(p.second.second);
+    }
+    for (cudaEvent_t e : c->prof.pool) cudaEventDestroy(e);
     delete c;
     return MPH_OK;
 }
@@ -547,17 +604,67 @@ int case_step(mph_case* c, int nsteps)
 {
     int last = MPH_OK;
     for (int s = 0; s < nsteps; ++s) {
+        cudaEvent_t ev[8];
+        int ne = 0;
+        auto mark = [&]() {
+            if (!c->prof.on) return;
+            ev[ne] = take_event(c);
+            cudaEventRecord(ev[ne], c->stream);
+            ++ne;
+        };
+        mark();
         MPH_TRY(stage_step_begin(c));
+        mark();
         MPH_TRY(stage_cellsort(c));
+        mark();
         MPH_TRY(stage_neighbors(c));
+        mark();
         MPH_TRY(stage_explicit(c));
+        mark();
         MPH_TRY(stage_assemble(c));
+        mark();
         MPH_TRY(stage_mg_build(c));
+        mark();
         MPH_TRY(stage_solve(c));
+        mark();
         MPH_TRY(stage_step_end(c));
+        if (c->prof.on) {
+            MPH_CUDA(cudaStreamSynchronize(c->stream));
+            for (int k = 0; k + 1 < ne; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                c->prof.stage_ms[k] += ms;
+            }
+            for (int k = 0; k < ne; ++k) c->prof.pool.push_back(ev[k]);
+            MPH_TRY(prof_collect(c));
+        }
         if (c->stats.status != MPH_OK) last = c->stats.status;
     }
     return last;
+}
+
+int case_profile(mph_case* c, int enable)
+{
+    MPH_TRY(prof_collect(c));
+    c->prof.on = enable != 0;
+    for (double& v : c->prof.stage_ms) v = 0.0;
+    for (double& v : c->prof.kern_ms) v = 0.0;
+    for (long long& v : c->prof.kern_n) v = 0;
+    return MPH_OK;
+}
+
+int case_profile_read(mph_case* c, double* out, int n)
+{
+    MPH_TRY(prof_collect(c));
+    std::vector<double> v;
+    for (int k = 0; k < 7; ++k) v.push_back(c->prof.stage_ms[k]);
+    for (int k = 0; k < kProfKernels; ++k) v.push_back(c->prof.kern_ms[k]);
+    for (int k = 0; k < kProfKernels; ++k) v.push_back((double)c->prof.kern_n[k]);
+    v.push_back((double)c->nslots);
+    v.push_back((double)c->nnb);
+    v.push_back((double)c->nnbP);
+    for (int k = 0; k < n && k < (int)v.size(); ++k) out[k] = v[k];
+    return (int)v.size();
 }
 
 }  // namespace mph

@@ -110,6 +110,22 @@ struct DeviceState {
     size_t scan_tmp_bytes = 0;
 };
 
+// Kernel launches issued by this library (host-side count).
+extern long long g_launch_count;
+#define MPH_COUNT_LAUNCH() (++::mph::g_launch_count)
+
+// Optional CUDA-event timing on the case stream: per stage and per launch of
+// the hot kernels.
+enum { kProfStages = 8, kProfKernels = 4 };                 // kernels: spmv, vcycle, assemble_a, neighbors
+struct Profile {
+    bool on = false;
+    double stage_ms[kProfStages] = {};
+    double kern_ms[kProfKernels] = {};
+    long long kern_n[kProfKernels] = {};
+    std::vector<cudaEvent_t> pool;                           // free events
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+};
+
 }  // namespace mph
 
 // Opaque handle of the C ABI.
@@ -139,6 +155,7 @@ struct mph_case {
     int iter_cap = 0;
     mph::DeviceState d;
     std::vector<void*> allocations;
+    mph::Profile prof;
 };
 
 namespace mph {
@@ -169,6 +186,13 @@ int case_scalars(mph_case* c, double* out, int n);
 const char* scalar_names();
 int case_get_fields(mph_case* c, mph_fields* out);
 int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_center);
+int case_profile(mph_case* c, int enable);
+int case_profile_read(mph_case* c, double* out, int n);
+
+// profiling helpers (mph_case.cu): bracket a launch sequence of kernel class k
+int prof_begin(mph_case* c, int k, cudaEvent_t* e0);
+void prof_end(mph_case* c, int k, cudaEvent_t e0);
+int prof_collect(mph_case* c);
 
 // host-side stages (mph_case.cu)
 int case_alloc_particles(mph_case* c);

@@ -58,6 +58,9 @@ def load_library(path: str = LIB_PATH):
         "mph_export": ([vp, cp, vp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ip)], ip),
         "mph_scalars": ([vp, ctypes.POINTER(ctypes.c_double), ip], ip),
         "mph_scalar_names": ([], cp),
+        "mph_case_profile": ([vp, ip], ip),
+        "mph_case_profile_read": ([vp, ctypes.POINTER(ctypes.c_double), ip], ip),
+        "mph_launch_count": ([], ctypes.c_longlong),
         "mph_last_error": ([], cp),
         "mph_version": ([], cp),
     }
@@ -165,11 +168,16 @@ class Case:
         _check(self.lib.mph_case_time(self.h, ctypes.byref(t)))
         return t.value
 
-    def fields(self) -> Dict[str, np.ndarray]:
+    def fields(self, which=None) -> Dict[str, np.ndarray]:
+        """Per-particle fields (cell order) copied to host; `which` selects a
+        subset of id, type, pos, vel, force, vol_strain_p, divergence_p,
+        pressure_p, virial_p, neighbor_count."""
         n = self.count
         out = {"id": np.empty(n, np.int32), "type": np.empty(n, np.int32), "pos": np.empty((n, 3)), "vel": np.empty((n, 3)),
                "force": np.empty((n, 3)), "vol_strain_p": np.empty(n), "divergence_p": np.empty(n),
                "pressure_p": np.empty(n), "virial_p": np.empty(n), "neighbor_count": np.empty(n, np.int32)}
+        if which is not None:
+            out = {k: v for k, v in out.items() if k in which}
         f = MphFields()
         for k, a in out.items():
             setattr(f, k, np_ptr(a, ctypes.c_int if a.dtype == np.int32 else ctypes.c_double))
@@ -183,11 +191,32 @@ class Case:
         _check(self.lib.mph_case_set_state(self.h, ctypes.byref(ps.struct),
                                            None if wc is None else wc.ctypes.data_as(ctypes.c_void_p)))
 
+    def profile(self, enable: bool = True):
+        _check(self.lib.mph_case_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> Dict[str, float]:
+        buf = (ctypes.c_double * 32)()
+        n = self.lib.mph_case_profile_read(self.h, buf, 32)
+        if n < 0 or n > 32:
+            _check(n)
+        v = list(buf)
+        stages = ["step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"]
+        kern = ["spmv", "vcycle", "assemble_a", "neighbors"]
+        out = {f"stage_ms_{s}": v[k] for k, s in enumerate(stages)}
+        out.update({f"kern_ms_{s}": v[7 + k] for k, s in enumerate(kern)})
+        out.update({f"kern_n_{s}": int(v[11 + k]) for k, s in enumerate(kern)})
+        out.update({"slots": int(v[15]), "nnb": int(v[16]), "nnbP": int(v[17])})
+        return out
+
     def write_vtk(self, path: str):
         _check(self.lib.mph_case_write_vtk(self.h, path.encode()))
 
     def write_prof(self, path: str):
         _check(self.lib.mph_case_write_prof(self.h, path.encode()))
+
+
+def launch_count() -> int:
+    return int(load_library().mph_launch_count())
 
 
 def batch_step(cases, nsteps: int = 1) -> int:
