@@ -121,13 +121,14 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def spmv_bytes(prof, scal, dim):
-    """Algorithmic bytes of one block SpMV: every block once (D*D values + a
-    column index), row lengths and slice pointers, x once, y written once."""
+def spmv_bytes(prof, scal, dim, vb=8):
+    """Algorithmic bytes of one block SpMV: every block once (D*D values of vb
+    bytes + a column index), row lengths and slice pointers, x once, y
+    written once (vb = 8 for the FP64 form, 4 for the FP32 inner solve)."""
     nf = int(scal["FluidParticleEnd"])
     blocks = scal["NonzeroCountA"] / (dim * dim)
     nsl = (nf + 31) // 32
-    return blocks * (dim * dim * 8 + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * 8
+    return blocks * (dim * dim * vb + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * vb
 
 
 def assemble_bytes(prof, scal, dim):
@@ -206,6 +207,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cube3d_100")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--inner-tol", type=float, default=1e-3,
+                    help="mixed form: relative residual reduction of each FP32 inner solve")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
@@ -234,6 +237,8 @@ def main():
     stream = torch.cuda.Stream()
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
     case = engine.Case(params, parts, dim, precision=prec, stream=stream.cuda_stream)
+    if prec == PRECISION_MIXED:
+        case.set_solver(1e-6, args.inner_tol, 50)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)
@@ -290,7 +295,9 @@ def main():
 
     # roofline of the dominant kernel (CUDA events on the case stream)
     peak, peak_kind = measured_peaks()
-    kern = {"spmv": ("k_spmv", spmv_bytes), "assemble_a": ("k_matrix_a", assemble_bytes)}
+    vb = 4 if prec == PRECISION_MIXED else 8
+    kern = {"spmv": ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
+            "assemble_a": ("k_assemble_cells", assemble_bytes)}
     dom = max(kern, key=lambda k: prof[f"kern_ms_{k}"])
     nlaunch = max(prof[f"kern_n_{dom}"], 1)
     avg_s = prof[f"kern_ms_{dom}"] / 1000.0 / nlaunch
@@ -316,7 +323,10 @@ def main():
                    "cr_iterations": iters,
                    "stage_ms_per_step": {s: prof[f"stage_ms_{s}"] / args.steps for s in
                                          ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve")},
-                   "stage_sum_ms_per_step": stage_total / args.steps},
+                   "stage_sum_ms_per_step": stage_total / args.steps,
+                   "kernel_avg_ms": {k: (prof[f"kern_ms_{k}"] / prof[f"kern_n_{k}"] if prof[f"kern_n_{k}"] else None)
+                                     for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
+                   "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "vcycle", "assemble_a", "neighbors")}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": args.e2e_steps},
         "gpu_launches": launches,

@@ -96,9 +96,10 @@ typedef struct mph_fields {
 /* Solve statistics of the last step (the reference logs the same numbers,
  * main.cpp:4381). */
 typedef struct mph_solve_stats {
-    int iterations;
+    int iterations;          /* CR iterations (mixed form: inner FP32 iterations, summed) */
     double rr0, rr, rs0, rs;
     int status;
+    int outer_iterations;    /* mixed form: FP64 refinement steps (0 for the FP64 form) */
 } mph_solve_stats;
 
 typedef struct mph_case mph_case;
@@ -133,6 +134,19 @@ int mph_case_set_stream(mph_case* c, void* stream);
 int mph_step(mph_case* c, int nsteps);
 /* Steps of several independent cases, interleaved on their streams. */
 int mph_batch_step(mph_case** cases, int ncases, int nsteps);
+
+/* Solver tolerances.  outer_rel_residual: stop when ||b - A x|| / ||b|| is
+ * below it (the reference stops at 1e-6: rr/rr0 < 1e-12, main.cpp:4346; this
+ * is the default and the only value the FP64 form uses).  Mixed form only:
+ * inner_rel_residual (relative reduction of each FP32 inner solve, default
+ * 1e-3) and max_outer (refinement steps, default 50).  No counterpart in the
+ * reference, whose tolerance is a constant. */
+int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel_residual, int max_outer);
+
+/* Engine options (no counterpart in the reference):
+ *   "cell_assembly" 1 (default) / 0: assemble A with the cell-block kernel
+ *   where it applies, or with the per-row kernel only (same matrix). */
+int mph_case_set_option(mph_case* c, const char* name, double value);
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);
 int mph_case_time(mph_case* c, double* time);

@@ -26,6 +26,15 @@ __global__ void k_slice_width(int Nf, const int* __restrict__ nfc, int* __restri
     if ((threadIdx.x & 31) == 0 && i < ((Nf + 31) / 32) * 32) width32[i >> 5] = 32 * v;
 }
 
+__global__ void k_max_int(const int* __restrict__ v, int n, int* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int m = i < n ? v[i] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
 template <int D>
 __global__ void __launch_bounds__(128) k_matrix_c(DevParams P, const double* __restrict__ pos, const int* __restrict__ ncp,
                                                   const long long* __restrict__ nptrP, const int* __restrict__ nindP,
@@ -51,11 +60,11 @@ __global__ void __launch_bounds__(128) k_matrix_c(DevParams P, const double* __r
             sep_vec<D>(P, xj, xi, q);
             const double r2 = norm2_exact<D>(q);
             if (r2 != 0.0 && rP2 - r2 > 0) {
-                const double dij = sqrt(r2);
-                const double wd = -dw_quad(P.kfp, dij, P.rP);
+                const double inv = rsqrt(r2);
+                const double wd = -P.kfp * (P.m2h_rp * (1.0 - (r2 * inv) * P.inv_rp));
 #pragma unroll
                 for (int r = 0; r < D; ++r) {
-                    cv[r] = (q[r] / dij) * wd;
+                    cv[r] = (q[r] * inv) * wd;
                     self[r] += cv[r];
                 }
             }
@@ -97,13 +106,13 @@ __global__ void __launch_bounds__(128) k_vector_p(DevParams P, const int* __rest
         sep_vec<D>(P, xj, xi, q);
         const double r2 = norm2_exact<D>(q);
         if (r2 == 0.0 || !(rP2 - r2 > 0)) continue;
-        const double dij = sqrt(r2);
-        const double wd = -dw_quad(P.kfp, dij, P.rP);
+        const double inv = rsqrt(r2);
+        const double wd = -P.kfp * (P.m2h_rp * (1.0 - (r2 * inv) * P.inv_rp));
         double vj[3];
         if (wj) load_vec<D>(vel, j, vj);
 #pragma unroll
         for (int s = 0; s < D; ++s) {
-            const double e = q[s] / dij;
+            const double e = q[s] * inv;
             if (wi) sum += lam * (e * wd) * vi[s];
             if (wj) sum += lam * (-e * wd) * vj[s];
         }
@@ -139,7 +148,8 @@ __device__ __forceinline__ void flush_part(double* __restrict__ prow, int slot, 
 }
 
 template <int D>
-__global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, const int* __restrict__ type,
+__global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, const int* __restrict__ only_cells,
+                                                  const int* __restrict__ type,
                                                   const int* __restrict__ key, const double* __restrict__ pos,
                                                   const double* __restrict__ vel, const double* __restrict__ force,
                                                   const int* __restrict__ nc, const int* __restrict__ nfc,
@@ -148,19 +158,20 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
                                                   const int* __restrict__ nindP, const double* __restrict__ cval,
                                                   const double* __restrict__ pvec, const long long* __restrict__ sptr,
                                                   int* __restrict__ acol, double* __restrict__ aval,
-                                                  double* __restrict__ bvec, double* __restrict__ invDiag,
+                                                  float* __restrict__ aval32, double* __restrict__ bvec, double* __restrict__ invDiag,
                                                   int* __restrict__ selfk_out, double* __restrict__ part)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.Nf) return;
+    if (only_cells && !only_cells[key[i]]) return;   // row assembled by the cell-block kernel
     constexpr int DD = D * D;
     const int lane = i & 31;
     const long long sbase = sptr[i >> 5];
     int* colp = acol + sbase + lane;
     double* valp = aval + sbase * DD + lane;
+    float* valp32 = aval32 ? aval32 + sbase * DD + lane : nullptr;   // mixed form: FP32 copy
 
     const int ti = type[i];
-    const double mui = P.mu[ti];
     double xi[3], vi[3];
     load_vec<D>(pos, i, xi);
     load_vec<D>(vel, i, vi);
@@ -217,11 +228,12 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
         const double r2 = norm2_exact<D>(q);
         const bool fluid = k < nf;
         if (r2 != 0.0 && rV2 - r2 > 0) {
-            const double dij = sqrt(r2);
-            const double wd = -dw_quad(P.kfv, dij, P.rV);
-            const double muj = P.mu[type[j]];
-            const double muij = 2.0 * (mui * muj) / (mui + muj);
-            const double inv = 1.0 / dij;
+            // one reciprocal square root per pair (FP64 divide and sqrt are
+            // slow on this part); -dw/dr = -kf (-2/h) (1 - r/h)
+            const double inv = rsqrt(r2);
+            const double dij = r2 * inv;
+            const double wd = -P.kfv * (P.m2h_rv * (1.0 - dij * P.inv_rv));
+            const double muij = P.muij[ti][type[j]];
             double e[3];
 #pragma unroll
             for (int d = 0; d < D; ++d) e[d] = q[d] * inv;
@@ -283,7 +295,10 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
 #pragma unroll
         for (int r = 0; r < D; ++r)
 #pragma unroll
-            for (int s = 0; s < D; ++s) valp[((long long)k * DD + r * D + s) * 32] = blk[r][s];
+            for (int s = 0; s < D; ++s) {
+                valp[((long long)k * DD + r * D + s) * 32] = blk[r][s];
+                if (valp32) valp32[((long long)k * DD + r * D + s) * 32] = (float)blk[r][s];
+            }
         // per-cell partial sums of the row (runs of equal stencil slot)
         const int slot = stencil_slot<D>(P, M, gi, key[j]);
         if (slot != run_slot) {
@@ -335,7 +350,10 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
 #pragma unroll
         for (int r = 0; r < D; ++r)
 #pragma unroll
-            for (int s = 0; s < D; ++s) valp[((long long)self * DD + r * D + s) * 32] = blk[r][s];
+            for (int s = 0; s < D; ++s) {
+                valp[((long long)self * DD + r * D + s) * 32] = blk[r][s];
+                if (valp32) valp32[((long long)self * DD + r * D + s) * 32] = (float)blk[r][s];
+            }
 #pragma unroll
         for (int r = 0; r < D; ++r) invDiag[(size_t)i * D + r] = blk[r][r] != 0.0 ? 1.0 / blk[r][r] : 0.0;
         selfk_out[i] = self;
@@ -395,10 +413,15 @@ int launch_assemble(mph_case* c)
     // slice pointers
     c->nslices = (Nf + 31) / 32;
     { k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth); MPH_COUNT_LAUNCH(); }
+    MPH_CUDA(cudaMemsetAsync(c->d.dmax, 0, sizeof(int), c->stream));
+    { k_max_int<<<grid_for(c->nslices, 256), 256, 0, c->stream>>>(c->d.swidth, c->nslices, c->d.dmax); MPH_COUNT_LAUNCH(); }
     MPH_TRY(launch_scan_i32_to_i64(c, c->d.swidth, c->d.sptr, c->nslices));
     long long h_slots = 0;
+    int h_width = 0;
     MPH_CUDA(cudaMemcpyAsync(&h_slots, c->d.sptr + c->nslices, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaMemcpyAsync(&h_width, c->d.dmax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MPH_CUDA(cudaStreamSynchronize(c->stream));
+    const int kmax_rows = h_width / 32;   // longest fluid row
     c->nslots = h_slots;
     {
         long long cap = c->d.cap_slots;
@@ -442,22 +465,28 @@ int launch_assemble(mph_case* c)
     if (D == 2) {
         { k_matrix_c<2><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval); MPH_COUNT_LAUNCH(); }
         { k_vector_p<2><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec); MPH_COUNT_LAUNCH(); }
-        cudaEvent_t pe = nullptr;
-        const int pon = prof_begin(c, 2, &pe);
-        { k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
-                                                 c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
-                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
-        if (pon) prof_end(c, 2, pe);
     } else {
         { k_matrix_c<3><<<gf, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval); MPH_COUNT_LAUNCH(); }
         { k_vector_p<3><<<ga, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.vel, c->d.vsp, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.pvec); MPH_COUNT_LAUNCH(); }
-        cudaEvent_t pe = nullptr;
-        const int pon = prof_begin(c, 2, &pe);
-        { k_matrix_a<3><<<gf, 128, 0, c->stream>>>(P, M, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc, c->d.nptr,
-                                                 c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
-                                                 c->d.acol, c->d.aval, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
-        if (pon) prof_end(c, 2, pe);
     }
+    // A: the cell-block kernel where it applies; the per-row kernel for the
+    // rows of cells it flags (or for every row when it does not apply)
+    cudaEvent_t pe = nullptr;
+    const int pon = prof_begin(c, 2, &pe);
+    bool cells = false;
+    if (c->cell_assembly) MPH_TRY(launch_assemble_cells(c, kmax_rows, &cells));
+    const int* only = cells ? c->d.cell_flags : nullptr;
+    float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;
+    if (D == 2) {
+        { k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, only, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc,
+                                                 c->d.nptr, c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
+                                                 c->d.acol, c->d.aval, a32, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_matrix_a<3><<<gf, 128, 0, c->stream>>>(P, M, only, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc,
+                                                 c->d.nptr, c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
+                                                 c->d.acol, c->d.aval, a32, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
+    }
+    if (pon) prof_end(c, 2, pe);
     return MPH_OK;
 }
 

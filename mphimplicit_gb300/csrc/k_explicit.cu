@@ -311,7 +311,36 @@ __global__ void __launch_bounds__(128) k_output_forces(DevParams P, const int* _
     virP[i] = -1.0 / (double)D * tr;
 }
 
-void launch_explicit(mph_case* c)
+// calculateDensityP alone over the P-list.  The P-list holds exactly the
+// pairs with r^2 <= RadiusP^2, in the full list's order, so the sum is
+// bit-identical to the full-list pass.
+template <int D>
+__global__ void __launch_bounds__(128) k_density_p(DevParams P, const double* __restrict__ pos, const int* __restrict__ ncp,
+                                                   const long long* __restrict__ nptrP, const int* __restrict__ nindP,
+                                                   double* __restrict__ vsp)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    double xi[3];
+    load_vec<D>(pos, i, xi);
+    const double rP2 = DMUL(P.rP, P.rP);
+    double sp = 0.0;
+    const long long b = nptrP[i];
+    const int n = ncp[i];
+    for (int k = 0; k < n; ++k) {
+        const int j = nindP[b + k];
+        if (j == i) continue;
+        double xj[3], q[3];
+        load_vec<D>(pos, j, xj);
+        sep_vec<D>(P, xj, xi, q);
+        const double r2 = norm2_exact<D>(q);
+        if (rP2 - r2 >= 0) sp = DADD(sp, w_quad(P.kfp, __dsqrt_rn(r2), P.rP));
+    }
+    vsp[i] = DSUB(sp, P.N0p);
+}
+
+// The full density pass (DensityA, GravityCenter, DensityP) and PressureA.
+void launch_density_full(mph_case* c)
 {
     const DevParams& P = c->dp;
     const unsigned g = grid_for(P.N, 128);
@@ -320,6 +349,31 @@ void launch_explicit(mph_case* c)
     else
         { k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
     { k_pressure_a<<<grid_for(P.N, 256), 256, 0, c->stream>>>(P, c->d.type, c->d.densA, c->d.presA); MPH_COUNT_LAUNCH(); }
+    c->densa_valid = true;
+}
+
+// DensityA, GravityCenter and PressureA only act through the surface-tension
+// coefficients CofA.  With every CofA zero they are dead in the step, so the
+// step computes DensityP alone; they are computed from the same positions and
+// lists when a reader (export, output fields) asks for them.
+void ensure_density_a(mph_case* c)
+{
+    if (!c->densa_valid) launch_density_full(c);
+}
+
+void launch_explicit(mph_case* c)
+{
+    const DevParams& P = c->dp;
+    const unsigned g = grid_for(P.N, 128);
+    if (P.surface) {
+        launch_density_full(c);
+    } else {
+        if (c->dim == 2)
+            { k_density_p<2><<<g, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.vsp); MPH_COUNT_LAUNCH(); }
+        else
+            { k_density_p<3><<<g, 128, 0, c->stream>>>(P, c->d.pos, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.vsp); MPH_COUNT_LAUNCH(); }
+        c->densa_valid = false;
+    }
     if (P.surface) {
         if (c->dim == 2)
             { k_surface_forces<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.presA, c->d.gcen, c->d.force); MPH_COUNT_LAUNCH(); }
@@ -338,16 +392,12 @@ void launch_explicit(mph_case* c)
 // the density pass alone: the initial pass of main() (main.cpp:371-373)
 void launch_explicit_density_only(mph_case* c)
 {
-    const DevParams& P = c->dp;
-    const unsigned g = grid_for(P.N, 128);
-    if (c->dim == 2)
-        { k_density<2><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
-    else
-        { k_density<3><<<g, 128, 0, c->stream>>>(P, c->d.type, c->d.pos, c->d.nc, c->d.nptr, c->d.nind, c->d.densA, c->d.gcen, c->d.vsp); MPH_COUNT_LAUNCH(); }
+    launch_density_full(c);
 }
 
 void launch_output_fields(mph_case* c)
 {
+    ensure_density_a(c);
     const DevParams& P = c->dp;
     const unsigned g = grid_for(P.N, 128);
     if (c->dim == 2) {

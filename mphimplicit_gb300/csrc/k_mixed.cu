@@ -1,3 +1,342 @@
-// k_mixed.cu - mixed-precision solve (FP32 inner CR + V-cycle, FP64 outer
-// iterative refinement).  Placeholder translation unit until it is built.
+// k_mixed.cu - mixed-precision solve of the step's system: FP32 inner
+// conjugate residual + FP32 V-cycle, FP64 outer iterative refinement.
+//
+//   x = v* - F/m dt ; r = b - A x                       (FP64, as the reference)
+//   while rr/rr0 >= tol_outer^2:                          (rr0 = (b,b), FP64)
+//       r32 = r / ||r||                                   (scaled to unit norm)
+//       z = CR_32(A32, r32; M32) to ||r_in|| < tol_inner  (FP32 vectors and
+//                                                          matrices, FP64 dots)
+//       x += ||r|| z ; r = b - A x ; rr = (r,r)           (FP64)
+//   v = x
+//
+// FP64 on the device is confined to the outer residual b - A x, the solution
+// update and the dot products / norms, which also carry both convergence
+// tests.  The inner CR runs the reference's recurrences (main.cpp:4344-4377)
+// from z = 0.  The default outer tolerance is the reference's
+// ||r||/||b|| < 1e-6; mph_case_set_solver tightens it (e.g. 1e-10).
 #include "mph_device.cuh"
+#include "mph_solver.cuh"
+
+namespace mph {
+
+bool mixed_available() { return true; }
+
+__host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
+enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSScale = 19 };
+
+template <int D, int MODE>
+__global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
+                                                const int* __restrict__ acol, const float* __restrict__ aval,
+                                                const float* __restrict__ xin, float* __restrict__ yout,
+                                                double* __restrict__ scal, int* __restrict__ flags, int it, int cap,
+                                                double tol2, double* __restrict__ partials, unsigned* __restrict__ counter,
+                                                double* __restrict__ out)
+{
+    constexpr int DD = D * D;
+    if (flags[kFlagDone]) return;
+    const double rr0 = scal[kSIn0];
+    const double rr = it == 0 ? rr0 : scal[kSIn];   // the inner solve starts from z = 0: r_in = r32
+    const bool bad = !(rr == rr);
+    if (it >= cap || rr / rr0 < tol2 || bad) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            flags[kFlagDone] = 1;
+            flags[kFlagIter] = it;
+            if (bad) flags[kFlagBad] = 1;
+        }
+        return;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (i < Nf) {
+        const int lane = i & 31;
+        const long long base = sptr[i >> 5];
+        const int* cp = acol + base + lane;
+        const float* vp = aval + base * DD + lane;
+        float y[3] = {0.f, 0.f, 0.f};
+        const int n = nfc[i];
+#pragma unroll 4
+        for (int k = 0; k < n; ++k) {
+            const int col = cp[(long long)k * 32];
+            float xv[3];
+#pragma unroll
+            for (int s = 0; s < D; ++s) xv[s] = xin[(size_t)col * D + s];
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < D; ++s) y[r] += vp[((long long)k * DD + r * D + s) * 32] * xv[s];
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            const size_t k = (size_t)i * D + r;
+            yout[k] = y[r];
+            acc += (double)xin[k] * (double)y[r];
+        }
+    }
+    (void)MODE;
+    reduce_finalize(acc, partials, counter, out);
+}
+
+__global__ void k_pq32(int n, int it, const float* __restrict__ s, const float* __restrict__ y, float* __restrict__ p,
+                       float* __restrict__ q, const double* __restrict__ scal, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    if (it == 0) {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            p[k] = s[k];
+            q[k] = y[k];
+        }
+        return;
+    }
+    const float beta = (float)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        p[k] = beta * p[k] + s[k];
+        q[k] = beta * q[k] + y[k];
+    }
+}
+
+__global__ void k_xrs32(int n, int it, float* __restrict__ z, float* __restrict__ r, float* __restrict__ s,
+                        const float* __restrict__ p, const float* __restrict__ q, const float* __restrict__ u,
+                        double* __restrict__ scal, const int* __restrict__ flags, double* __restrict__ partials,
+                        unsigned* __restrict__ counter)
+{
+    if (flags[kFlagDone]) return;
+    const float alpha = (float)(scal[rho32_slot(it)] / scal[kSQU32]);
+    double acc = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        z[k] += alpha * p[k];
+        const float rk = r[k] - alpha * q[k];
+        r[k] = rk;
+        s[k] -= alpha * u[k];
+        acc += (double)rk * (double)rk;
+    }
+    reduce_finalize(acc, partials, counter, scal + kSIn);
+}
+
+// r32 = r / sqrt(rr), z = 0, and the inner reference norm (r32, r32)
+__global__ void k_to32(int n, const double* __restrict__ r, float* __restrict__ r32, float* __restrict__ z,
+                       double* __restrict__ scal, double* __restrict__ partials, unsigned* __restrict__ counter)
+{
+    const double sc = 1.0 / sqrt(scal[kSRR]);
+    double acc = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float v = (float)(r[k] * sc);
+        r32[k] = v;
+        z[k] = 0.f;
+        acc += (double)v * (double)v;
+    }
+    reduce_finalize(acc, partials, counter, scal + kSIn0);
+}
+
+// x += ||r|| z  (FP64 update)
+__global__ void k_refine(int n, double* __restrict__ x, const float* __restrict__ z, const double* __restrict__ scal)
+{
+    const double sc = sqrt(scal[kSRR]);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += sc * (double)z[k];
+}
+
+// r = b - A x in FP64 (the outer residual), (r,r) -> scal[kSRR]
+template <int D>
+__global__ void __launch_bounds__(128) k_resid64(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
+                                                 const int* __restrict__ acol, const double* __restrict__ aval,
+                                                 const double* __restrict__ x, const double* __restrict__ b,
+                                                 double* __restrict__ r, double* __restrict__ partials,
+                                                 unsigned* __restrict__ counter, double* __restrict__ out)
+{
+    constexpr int DD = D * D;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (i < Nf) {
+        const int lane = i & 31;
+        const long long base = sptr[i >> 5];
+        const int* cp = acol + base + lane;
+        const double* vp = aval + base * DD + lane;
+        double y[3] = {0.0, 0.0, 0.0};
+        const int n = nfc[i];
+#pragma unroll 2
+        for (int k = 0; k < n; ++k) {
+            const int col = cp[(long long)k * 32];
+            double xv[3];
+#pragma unroll
+            for (int s = 0; s < D; ++s) xv[s] = x[(size_t)col * D + s];
+#pragma unroll
+            for (int rr = 0; rr < D; ++rr)
+#pragma unroll
+                for (int s = 0; s < D; ++s) y[rr] += vp[((long long)k * DD + rr * D + s) * 32] * xv[s];
+        }
+#pragma unroll
+        for (int rr = 0; rr < D; ++rr) {
+            const size_t k = (size_t)i * D + rr;
+            const double v = b[k] - y[rr];
+            r[k] = v;
+            acc += v * v;
+        }
+    }
+    reduce_finalize(acc, partials, counter, out);
+}
+
+template <typename TI, typename TO>
+__global__ void k_convert(long long n, const TI* __restrict__ a, TO* __restrict__ b)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        b[k] = (TO)a[k];
+}
+
+template <int D>
+__global__ void k_store_velocity_m(int Nf, const double* __restrict__ x, double* __restrict__ vel)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Nf * D) return;
+    vel[(size_t)(k / D) * (D == 2 ? 2 : 4) + k % D] = x[k];
+}
+
+template <int D>
+__global__ void k_x0(int Nf, const int* __restrict__ type, const double* __restrict__ vel, const double* __restrict__ force,
+                     const double* __restrict__ b, double* __restrict__ x, DevParams P, double* __restrict__ partials,
+                     unsigned* __restrict__ counter, double* __restrict__ out)
+{
+    double acc = 0.0;
+    const int n = Nf * D;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = k / D, r = k % D;
+        const double m = P.density[type[i]] * P.vol;
+        const int VSD = D == 2 ? 2 : 4;
+        x[k] = vel[(size_t)i * VSD + r] - force[(size_t)i * VSD + r] / m * P.dt;
+        acc += b[k] * b[k];
+    }
+    reduce_finalize(acc, partials, counter, out);
+}
+
+// ---- host side ---------------------------------------------------------------------
+static int grow_f(float** p, long long* cap, long long need)
+{
+    if (need <= *cap) return MPH_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const long long n = need + need / 8 + 256;
+    MPH_CUDA(cudaMalloc((void**)p, (size_t)n * sizeof(float)));
+    *cap = n;
+    return MPH_OK;
+}
+
+// FP32 copies of the multigrid levels and of D^-1 (after the FP64 build)
+int mixed_prepare(mph_case* c)
+{
+    DeviceState& d = c->d;
+    MPH_TRY(grow_f(&d.mg_cof32, &d.cap_mg_cof32, c->mg_cof_total));
+    if (c->mg_rows_total > d.cap_mg_vec32) {
+        for (float** b : {&d.mg_invd32, &d.mg_q32, &d.mg_s32, &d.mg_r32, &d.mg_res32}) {
+            if (*b) cudaFree(*b);
+            *b = nullptr;
+        }
+        const long long n = c->mg_rows_total + c->mg_rows_total / 8 + 256;
+        for (float** b : {&d.mg_invd32, &d.mg_q32, &d.mg_s32, &d.mg_r32, &d.mg_res32}) MPH_CUDA(cudaMalloc((void**)b, n * sizeof(float)));
+        d.cap_mg_vec32 = n;
+    }
+    const long long nv = (long long)c->dp.Nf * c->dim;
+    if (!d.v32) {
+        MPH_CUDA(cudaMalloc((void**)&d.v32, (size_t)nv * 8 * sizeof(float)));
+    }
+    cudaStream_t st = c->stream;
+    { k_convert<double, float><<<grid_for(c->mg_cof_total, 256), 256, 0, st>>>(c->mg_cof_total, d.mg_cof, d.mg_cof32); MPH_COUNT_LAUNCH(); }
+    { k_convert<double, float><<<grid_for(c->mg_rows_total, 256), 256, 0, st>>>(c->mg_rows_total, d.mg_invd, d.mg_invd32); MPH_COUNT_LAUNCH(); }
+    { k_convert<double, float><<<grid_for(nv, 256), 256, 0, st>>>(nv, d.invDiag, d.v32 + 7 * nv); MPH_COUNT_LAUNCH(); }
+    return MPH_OK;
+}
+
+void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
+
+template <int D>
+static int mixed_solve_t(mph_case* c)
+{
+    MPH_TRY(mixed_prepare(c));
+    DeviceState& d = c->d;
+    const int Nf = c->dp.Nf;
+    const int n = Nf * D;
+    cudaStream_t st = c->stream;
+    double* scal = d.scal;
+    int* flags = d.flags;
+    unsigned* counter = (unsigned*)(flags + kFlagCounter);
+    double* part = d.partials;
+    const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
+    const unsigned gs = grid_for(Nf, 128);
+    float* r32 = d.v32;
+    float* z32 = d.v32 + (size_t)n;
+    float* s32 = d.v32 + 2 * (size_t)n;
+    float* y32 = d.v32 + 3 * (size_t)n;
+    float* p32 = d.v32 + 4 * (size_t)n;
+    float* q32 = d.v32 + 5 * (size_t)n;
+    float* u32 = d.v32 + 6 * (size_t)n;
+    MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
+    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
+    { k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+    const double tol_out2 = c->tol_outer * c->tol_outer;
+    const double tol_in2 = c->tol_inner * c->tol_inner;
+    const int cap = n;
+    int total_inner = 0, outer = 0;
+    int host_flags[kFlagCount];
+    double hs[32];
+    bool bad = false;
+    for (;;) {
+        MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        MPH_CUDA(cudaStreamSynchronize(st));
+        if (!(hs[kSRR] == hs[kSRR])) { bad = true; break; }
+        if (hs[kSRR] / hs[kSRR0] < tol_out2 || outer >= c->max_outer || hs[kSRR] == 0.0) break;
+        ++outer;
+        MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
+        { k_to32<<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, scal, part, counter); MPH_COUNT_LAUNCH(); }
+        // inner CR from z = 0: r_in = r32, s = M r_in
+        vcycle_mixed(c, r32, s32, scal + kSQU32);
+        int it = 0;
+        bool done = false;
+        const int chunk = 8;
+        std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
+        while (!done) {
+            const int m = std::min(chunk, cap + 1 - it);
+            for (int k = 0; k < m; ++k, ++it) {
+                cudaEvent_t e[2] = {nullptr, nullptr};
+                const bool pon = prof_begin(c, 0, &e[0]) != 0;
+                { k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, it, cap, tol_in2, part,
+                                                     counter, scal + rho32_slot(it)); MPH_COUNT_LAUNCH(); }
+                if (pon) { prof_begin(c, 0, &e[1]); timed.push_back({it, {e[0], e[1]}}); }
+                { k_pq32<<<rb, kReduceThreads, 0, st>>>(n, it, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+                vcycle_mixed(c, q32, u32, scal + kSQU32);
+                { k_xrs32<<<rb, kReduceThreads, 0, st>>>(n, it, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
+            }
+            MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
+            MPH_CUDA(cudaStreamSynchronize(st));
+            done = host_flags[kFlagDone] != 0 || it > cap;
+        }
+        const int inner = host_flags[kFlagDone] ? host_flags[kFlagIter] : cap;
+        for (auto& t : timed) {   // keep the SpMV launches of iterations that ran
+            if (t.first < inner) {
+                c->prof.pending.push_back({0, t.second});
+            } else {
+                c->prof.pool.push_back(t.second.first);
+                c->prof.pool.push_back(t.second.second);
+            }
+        }
+        if (host_flags[kFlagBad]) { bad = true; break; }
+        total_inner += inner;
+        { k_refine<<<rb, kReduceThreads, 0, st>>>(n, d.x, z32, scal); MPH_COUNT_LAUNCH(); }
+        { k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+    }
+    { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
+    MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    MPH_CUDA(cudaStreamSynchronize(st));
+    c->stats.iterations = total_inner;
+    c->stats.rr0 = hs[kSRR0];
+    c->stats.rr = hs[kSRR];
+    c->stats.rs0 = 0.0;
+    c->stats.rs = 0.0;
+    c->stats.outer_iterations = outer;
+    c->stats.status = bad ? MPH_ERR_NAN : (hs[kSRR] / hs[kSRR0] < tol_out2 || hs[kSRR] == 0.0 ? MPH_OK : MPH_ERR_NOT_CONVERGED);
+    return MPH_OK;
+}
+
+int run_mixed_solve(mph_case* c)
+{
+    return c->dim == 2 ? mixed_solve_t<2>(c) : mixed_solve_t<3>(c);
+}
+
+}  // namespace mph

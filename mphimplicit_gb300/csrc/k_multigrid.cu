@@ -4,21 +4,29 @@
 // times by 2 (calculateMultiGridDepth, main.cpp:2777-2859).  Restriction (sum
 // of the 2^D children), prolongation (injection) and the particle<->grid
 // transfers (P2G sum, G2P injection) are index maps computed on the fly; only
-// the level matrices are stored, as dense 3^D-cell block stencils with the
-// reference's periodic wrap on the grid index.
+// the level matrices are stored, as 3^D-cell block stencils with the
+// reference's periodic wrap on the grid index.  A level's stencil is stored
+// entry-major: value (entry e, row) at e*rows + row, so the threads of a
+// warp (consecutive rows) read consecutive words.
 //
 // Build:  level 0 = per-cell sums of the per-row partial stencils written by
 //         the assembly pass; level L = the reference's re-binning of level
 //         L-1's stencil rows onto the parent cells (same summation order);
 //         invD = 2 / sum |a_row| (calculateMultiGridInvDiagA, main.cpp:3510).
-// V-cycle: one fused Jacobi kernel per smoothing sweep
-//         (S_new = S + invD (Q - A S)); the fine residual is recomputed inside
-//         the restriction kernel; the last kernel adds G2P S_0 to D^-1 q and
-//         forms the (q, u) partial dot product.
+// V-cycle: levels with many rows run as grid-wide kernels: one fused Jacobi
+//         kernel per smoothing sweep (S_new = S + invD (Q - A S)), a residual
+//         kernel before each restriction, and the restriction (child sums).
+//         Every level from the first one with at most kCtaRows rows down to
+//         the coarsest and back runs inside one 1024-thread block, its sweeps
+//         separated by __syncthreads, so the small levels cost one launch.
+//         The last kernel adds G2P S_0 to D^-1 q and forms the (q, u) dot.
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
 namespace mph {
+
+constexpr int kCtaRows = 8192;
+constexpr int kCtaThreads = 1024;
 
 struct LevelK {
     int mn[3], mx[3], cnt[3], st[3];
@@ -53,15 +61,25 @@ __device__ __forceinline__ int stencil_col(const LevelK& L, const int* p, int ix
     return grid_index(L, (p[0] + ix - 1 + L.cnt[0]) % L.cnt[0], (p[1] + iy - 1 + L.cnt[1]) % L.cnt[1],
                       (p[2] + iz - 1 + L.cnt[2]) % L.cnt[2]);
 }
+// children range of coarse cell p of level L inside the finer level S_
+__device__ __forceinline__ void child_range(const LevelK& S_, const LevelK& L, const int* p, int* fm, int* fM)
+{
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int lc = p[d] + L.mn[d];
+        fm[d] = S_.mn[d] > 2 * lc ? 1 : 0;
+        fM[d] = S_.mx[d] < 2 * (lc + 1) ? 1 : 0;
+    }
+}
 
 // ---- build -------------------------------------------------------------------
 template <int D>
 __global__ void k_mg_level0(DevParams P, LevelK L, const int* __restrict__ bucket, const double* __restrict__ part,
-                            double* __restrict__ cof)
+                            double* __restrict__ cofT)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)L.rows * L.width) return;
-    const int row = (int)(t / L.width), e = (int)(t % L.width);
+    const int e = (int)(t / L.rows), row = (int)(t % L.rows);
     const int g = row / D, rD = row % D;
     const int slot = e / D, sD = e % D;
     const int S = L.st[0] * L.st[1] * L.st[2];
@@ -73,7 +91,7 @@ __global__ void k_mg_level0(DevParams P, LevelK L, const int* __restrict__ bucke
         const int ic = cell_id(P, cx, cy, cz);
         for (int i = bucket[ic]; i < bucket[ic + 1]; ++i) sum += part[((size_t)i * S + slot) * D * D + rD * D + sD];
     }
-    cof[t] = sum;
+    cofT[t] = sum;
 }
 
 template <int D>
@@ -81,30 +99,25 @@ __global__ void k_mg_coarse(LevelK S_, LevelK L, const double* __restrict__ cofS
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)L.rows * L.width) return;
-    const int rowL = (int)(t / L.width), e = (int)(t % L.width);
+    const int e = (int)(t / L.rows), rowL = (int)(t % L.rows);
     const int g = rowL / D, rD = rowL % D;
     const int oslot = e / D, sD = e % D;
-    int p[3];
+    int p[3], fm[3], fM[3];
     grid_coords(L, g, p);
-    int fm[3], fM[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int lc = p[d] + L.mn[d];
-        fm[d] = S_.mn[d] > 2 * lc ? 1 : 0;
-        fM[d] = S_.mx[d] < 2 * (lc + 1) ? 1 : 0;
-    }
+    child_range(S_, L, p, fm, fM);
     double sum = 0.0;
     for (int dx = fm[0]; dx < 2 - fM[0]; ++dx)
         for (int dy = fm[1]; dy < 2 - fM[1]; ++dy)
             for (int dz = fm[2]; dz < 2 - fM[2]; ++dz) {
                 const int sg = grid_index(S_, 2 * (p[0] + L.mn[0]) + dx - S_.mn[0], 2 * (p[1] + L.mn[1]) + dy - S_.mn[1],
                                           2 * (p[2] + L.mn[2]) + dz - S_.mn[2]);
+                const int rowS = sg * D + rD;
                 int sp[3];
                 grid_coords(S_, sg, sp);
-                const double* in = cofS + (size_t)(sg * D + rD) * S_.width;
+                int fe = 0;
                 for (int ix = 0; ix < S_.st[0]; ++ix)
                     for (int iy = 0; iy < S_.st[1]; ++iy)
-                        for (int iz = 0; iz < S_.st[2]; ++iz) {
+                        for (int iz = 0; iz < S_.st[2]; ++iz, ++fe) {
                             const int jf[3] = {(sp[0] + ix - 1 + S_.cnt[0]) % S_.cnt[0], (sp[1] + iy - 1 + S_.cnt[1]) % S_.cnt[1],
                                                (sp[2] + iz - 1 + S_.cnt[2]) % S_.cnt[2]};
                             int o[3];
@@ -114,18 +127,18 @@ __global__ void k_mg_coarse(LevelK S_, LevelK L, const double* __restrict__ cofS
                                 o[d] = (jl - p[d] + 1 + L.cnt[d]) % L.cnt[d];
                             }
                             if (L.st[2] * L.st[1] * o[0] + L.st[2] * o[1] + o[2] != oslot) continue;
-                            sum += in[D * (S_.st[2] * S_.st[1] * ix + S_.st[2] * iy + iz) + sD];
+                            sum += cofS[(size_t)(fe * D + sD) * S_.rows + rowS];
                         }
             }
     cofL[t] = sum;
 }
 
-__global__ void k_mg_invd(int rows, int width, const double* __restrict__ cof, double* __restrict__ invd)
+__global__ void k_mg_invd(int rows, int width, const double* __restrict__ cofT, double* __restrict__ invd)
 {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     double s = 0.0;
-    for (int k = 0; k < width; ++k) s += fabs(cof[(size_t)row * width + k]);
+    for (int k = 0; k < width; ++k) s += fabs(cofT[(size_t)k * rows + row]);
     invd[row] = s != 0.0 ? 2.0 / s : 0.0;
 }
 
@@ -157,15 +170,15 @@ void launch_mg_invd(mph_case* c)
     }
 }
 
-// ---- V-cycle kernels -----------------------------------------------------------
+// ---- V-cycle row operations ------------------------------------------------------
+// Q - A S for one row (the reference's csrmv with alpha = -1, beta = 1)
 template <int D, typename T>
-__device__ __forceinline__ T level_residual(const LevelK& L, const T* __restrict__ cof, const T* __restrict__ Q,
-                                            const T* __restrict__ S, int row)
+__device__ __forceinline__ T row_residual(const LevelK& L, const T* __restrict__ cofT, const T* __restrict__ Q,
+                                          const T* __restrict__ S, int row)
 {
     const int g = row / D;
     int p[3];
     grid_coords(L, g, p);
-    const T* a = cof + (size_t)row * L.width;
     T sum = 0;
     int e = 0;
     for (int ix = 0; ix < L.st[0]; ++ix)
@@ -173,66 +186,82 @@ __device__ __forceinline__ T level_residual(const LevelK& L, const T* __restrict
             for (int iz = 0; iz < L.st[2]; ++iz) {
                 const int jg = stencil_col(L, p, ix, iy, iz);
 #pragma unroll
-                for (int sD = 0; sD < D; ++sD, ++e) sum += (-a[e]) * S[jg * D + sD];
+                for (int sD = 0; sD < D; ++sD, ++e) sum += (-cofT[(size_t)e * L.rows + row]) * S[jg * D + sD];
             }
     return Q[row] + sum;
 }
 
-// S_out = S_in + invD (Q - A S_in)
+// sum of the children's residuals (the restriction R, main.cpp:3154-3174)
 template <int D, typename T>
-__global__ void k_mg_jacobi(LevelK L, const T* __restrict__ cof, const T* __restrict__ invd, const T* __restrict__ Q,
-                            const T* __restrict__ Sin, T* __restrict__ Sout, const int* __restrict__ flags)
+__device__ __forceinline__ T row_restrict(const LevelK& S_, const LevelK& L, const T* __restrict__ RS, int row)
 {
-    if (flags[kFlagDone]) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= L.rows) return;
-    const T r = level_residual<D, T>(L, cof, Q, Sin, row);
-    Sout[row] = Sin[row] + invd[row] * r;
-}
-
-// Q_L = R (Q_S - A_S S_S) over the children; S_L = invD_L Q_L
-template <int D, typename T>
-__global__ void k_mg_restrict(LevelK S_, LevelK L, const T* __restrict__ cofS, const T* __restrict__ QS,
-                              const T* __restrict__ SS, const T* __restrict__ invdL, T* __restrict__ QL,
-                              T* __restrict__ SL, const int* __restrict__ flags)
-{
-    if (flags[kFlagDone]) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= L.rows) return;
     const int g = row / D, rD = row % D;
-    int p[3];
+    int p[3], fm[3], fM[3];
     grid_coords(L, g, p);
-    int fm[3], fM[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int lc = p[d] + L.mn[d];
-        fm[d] = S_.mn[d] > 2 * lc ? 1 : 0;
-        fM[d] = S_.mx[d] < 2 * (lc + 1) ? 1 : 0;
-    }
+    child_range(S_, L, p, fm, fM);
     T sum = 0;
     for (int dx = fm[0]; dx < 2 - fM[0]; ++dx)
         for (int dy = fm[1]; dy < 2 - fM[1]; ++dy)
             for (int dz = fm[2]; dz < 2 - fM[2]; ++dz) {
                 const int sg = grid_index(S_, 2 * (p[0] + L.mn[0]) + dx - S_.mn[0], 2 * (p[1] + L.mn[1]) + dy - S_.mn[1],
                                           2 * (p[2] + L.mn[2]) + dz - S_.mn[2]);
-                sum += level_residual<D, T>(S_, cofS, QS, SS, sg * D + rD);
+                sum += RS[sg * D + rD];
             }
-    QL[row] = sum;
-    SL[row] = invdL[row] * sum;
+    return sum;
 }
 
-// S_S += P S_L (injection from the parent cell)
+// parent row of fine row `row` (the prolongation P, main.cpp:3216-3240)
+template <int D>
+__device__ __forceinline__ int row_parent(const LevelK& S_, const LevelK& L, int row)
+{
+    const int g = row / D, rD = row % D;
+    int p[3];
+    grid_coords(S_, g, p);
+    return grid_index(L, (p[0] + S_.mn[0]) / 2 - L.mn[0], (p[1] + S_.mn[1]) / 2 - L.mn[1], (p[2] + S_.mn[2]) / 2 - L.mn[2]) * D + rD;
+}
+
+// ---- grid-wide V-cycle kernels ------------------------------------------------------
+template <int D, typename T>
+__global__ void k_mg_jacobi(LevelK L, const T* __restrict__ cofT, const T* __restrict__ invd, const T* __restrict__ Q,
+                            const T* __restrict__ Sin, T* __restrict__ Sout, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= L.rows) return;
+    const T r = row_residual<D, T>(L, cofT, Q, Sin, row);
+    Sout[row] = Sin[row] + invd[row] * r;
+}
+
+template <int D, typename T>
+__global__ void k_mg_residual(LevelK L, const T* __restrict__ cofT, const T* __restrict__ Q, const T* __restrict__ S,
+                              T* __restrict__ R, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= L.rows) return;
+    R[row] = row_residual<D, T>(L, cofT, Q, S, row);
+}
+
+// Q_L = R r_{L-1};  S_L = invD_L Q_L (the first smoothing update from S = 0)
+template <int D, typename T>
+__global__ void k_mg_restrict(LevelK S_, LevelK L, const T* __restrict__ RS, const T* __restrict__ invdL, T* __restrict__ QL,
+                              T* __restrict__ SL, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= L.rows) return;
+    const T q = row_restrict<D, T>(S_, L, RS, row);
+    QL[row] = q;
+    SL[row] = invdL[row] * q;
+}
+
 template <int D, typename T>
 __global__ void k_mg_prolong(LevelK S_, LevelK L, const T* __restrict__ SL, T* __restrict__ SS, const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= S_.rows) return;
-    const int g = row / D, rD = row % D;
-    int p[3];
-    grid_coords(S_, g, p);
-    const int lg = grid_index(L, (p[0] + S_.mn[0]) / 2 - L.mn[0], (p[1] + S_.mn[1]) / 2 - L.mn[1], (p[2] + S_.mn[2]) / 2 - L.mn[2]);
-    SS[row] = SS[row] + SL[lg * D + rD];
+    SS[row] = SS[row] + SL[row_parent<D>(S_, L, row)];
 }
 
 // Q_0 = P2G q (sum over the fluid particles of each cell); S_0 = invD_0 Q_0
@@ -276,54 +305,162 @@ __global__ void k_mg_g2p_dot(DevParams P, LevelK L, const int* __restrict__ key,
     reduce_finalize(acc, partials, counter, out);
 }
 
+// ---- the small levels in one block ------------------------------------------------
+template <typename T>
+struct CoarseArgs {
+    int first, depth;                 // levels first..depth-1 run here; first >= 1
+    LevelK L[kMaxLevels];
+    const T* cof[kMaxLevels];
+    const T* invd[kMaxLevels];
+    T* Q[kMaxLevels];
+    T* Sa[kMaxLevels];
+    T* Sb[kMaxLevels];
+    T* R[kMaxLevels];                 // R[first-1] holds the finer level's residual
+    T* Sfine;                         // current S of level first-1 (receives the prolongation)
+};
+
+template <int D, typename T>
+__global__ void __launch_bounds__(kCtaThreads) k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    T* cur[kMaxLevels];
+    T* oth[kMaxLevels];
+    for (int l = A.first; l < A.depth; ++l) { cur[l] = A.Sa[l]; oth[l] = A.Sb[l]; }
+    auto jacobi = [&](int l) {
+        const LevelK& L = A.L[l];
+        for (int row = threadIdx.x; row < L.rows; row += blockDim.x) {
+            const T r = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
+            oth[l][row] = cur[l][row] + A.invd[l][row] * r;
+        }
+        __syncthreads();
+        T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
+    };
+    // down: restriction + pre-smoothing (3 updates, the coarsest 5)
+    for (int l = A.first; l < A.depth; ++l) {
+        const LevelK& L = A.L[l];
+        for (int row = threadIdx.x; row < L.rows; row += blockDim.x) {
+            const T q = row_restrict<D, T>(A.L[l - 1], L, A.R[l - 1], row);
+            A.Q[l][row] = q;
+            cur[l][row] = A.invd[l][row] * q;
+        }
+        __syncthreads();
+        const int sweeps = (l == A.depth - 1) ? 4 : 2;
+        for (int k = 0; k < sweeps; ++k) jacobi(l);
+        if (l < A.depth - 1) {
+            for (int row = threadIdx.x; row < L.rows; row += blockDim.x)
+                A.R[l][row] = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
+            __syncthreads();
+        }
+    }
+    // up: prolongation + post-smoothing (3 updates)
+    for (int l = A.depth - 1; l > A.first; --l) {
+        const LevelK& S_ = A.L[l - 1];
+        for (int row = threadIdx.x; row < S_.rows; row += blockDim.x)
+            cur[l - 1][row] = cur[l - 1][row] + cur[l][row_parent<D>(S_, A.L[l], row)];
+        __syncthreads();
+        for (int k = 0; k < 3; ++k) jacobi(l - 1);
+    }
+    // prolongation into the finer, grid-wide level
+    const LevelK& S_ = A.L[A.first - 1];
+    for (int row = threadIdx.x; row < S_.rows; row += blockDim.x)
+        A.Sfine[row] = A.Sfine[row] + cur[A.first][row_parent<D>(S_, A.L[A.first], row)];
+}
+
 // ---- host-side V-cycle -----------------------------------------------------------
 template <int D, typename T, typename TQ>
 static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T* cof, const T* invd, T* Qp, T* Sa, T* Sb,
-                     double* dot_out)
+                     T* Rp, double* dot_out)
 {
     const int depth = c->depth;
     cudaStream_t st = c->stream;
     const int* flags = c->d.flags;
-    std::vector<LevelK> L(depth);
+    LevelK L[kMaxLevels];
     for (int l = 0; l < depth; ++l) L[l] = level_k(c, l);
-    auto off_v = [&](int l) { return c->lv[l].off_vec; };
-    auto off_c = [&](int l) { return c->lv[l].off_cof; };
-    // current S buffer of each level (ping-pong between Sa and Sb)
-    std::vector<T*> cur(depth), oth(depth);
-    for (int l = 0; l < depth; ++l) { cur[l] = Sa + off_v(l); oth[l] = Sb + off_v(l); }
+    auto ov = [&](int l) { return c->lv[l].off_vec; };
+    auto oc = [&](int l) { return c->lv[l].off_cof; };
+    T* cur[kMaxLevels];
+    T* oth[kMaxLevels];
+    for (int l = 0; l < depth; ++l) { cur[l] = Sa + ov(l); oth[l] = Sb + ov(l); }
+    // first level handled by the single-block kernel (>= 1), or depth if none
+    int first = depth;
+    for (int l = 1; l < depth; ++l)
+        if (L[l].rows <= kCtaRows) { first = l; break; }
     auto jacobi = [&](int l) {
-        { k_mg_jacobi<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + off_c(l), invd + off_v(l), Qp + off_v(l),
-                                                                     cur[l], oth[l], flags); MPH_COUNT_LAUNCH(); }
-        std::swap(cur[l], oth[l]);
+        { k_mg_jacobi<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + oc(l), invd + ov(l), Qp + ov(l), cur[l], oth[l],
+                                                                       flags); MPH_COUNT_LAUNCH(); }
+        T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
     };
-    // pre-smoothing, going down
-    { k_mg_p2g<D, T, TQ><<<grid_for(L[0].rows, 128), 128, 0, st>>>(c->dp, L[0], c->d.bucket, q, invd + off_v(0), Qp + off_v(0),
-                                                                 cur[0], flags); MPH_COUNT_LAUNCH(); }
-    jacobi(0);                                   // 2 sweeps on level 0
-    for (int l = 1; l < depth; ++l) {
-        { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cof + off_c(l - 1), Qp + off_v(l - 1),
-                                                                       cur[l - 1], invd + off_v(l), Qp + off_v(l), cur[l], flags); MPH_COUNT_LAUNCH(); }
-        const int sweeps = (l == depth - 1) ? 5 : 3;   // coarsest: 4 sweeps + one more update
-        for (int k = 1; k < sweeps; ++k) jacobi(l);
+    auto residual = [&](int l) {
+        { k_mg_residual<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + oc(l), Qp + ov(l), cur[l], Rp + ov(l), flags); MPH_COUNT_LAUNCH(); }
+    };
+    // down, grid-wide levels
+    { k_mg_p2g<D, T, TQ><<<grid_for(L[0].rows, 128), 128, 0, st>>>(c->dp, L[0], c->d.bucket, q, invd + ov(0), Qp + ov(0),
+                                                                   cur[0], flags); MPH_COUNT_LAUNCH(); }
+    jacobi(0);                                            // level 0: 2 updates
+    for (int l = 1; l < first; ++l) {
+        residual(l - 1);
+        { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], Rp + ov(l - 1), invd + ov(l), Qp + ov(l),
+                                                                        cur[l], flags); MPH_COUNT_LAUNCH(); }
+        const int sweeps = (l == depth - 1) ? 4 : 2;     // coarsest: 4 sweeps + one more update
+        for (int k = 0; k < sweeps; ++k) jacobi(l);
     }
-    // post-smoothing, going up
-    for (int l = depth - 1; l >= 1; --l) {
+    if (first < depth) {
+        residual(first - 1);
+        CoarseArgs<T> A;
+        A.first = first;
+        A.depth = depth;
+        for (int l = 0; l < depth; ++l) {
+            A.L[l] = L[l];
+            A.cof[l] = cof + oc(l);
+            A.invd[l] = invd + ov(l);
+            A.Q[l] = Qp + ov(l);
+            A.Sa[l] = Sa + ov(l);
+            A.Sb[l] = Sb + ov(l);
+            A.R[l] = Rp + ov(l);
+        }
+        A.Sfine = cur[first - 1];
+        { k_mg_small_levels<D, T><<<1, kCtaThreads, 0, st>>>(A, flags); MPH_COUNT_LAUNCH(); }
+    }
+    // up, grid-wide levels: the block kernel already prolongated into level
+    // first-1; without it the coarsest level is prolongated here
+    auto prolong = [&](int l) {   // S_{l-1} += P S_l
         { k_mg_prolong<D, T><<<grid_for(L[l - 1].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cur[l], cur[l - 1], flags); MPH_COUNT_LAUNCH(); }
-        const int sweeps = (l - 1 == 0) ? 2 : 3;
-        for (int k = 0; k < sweeps; ++k) jacobi(l - 1);
+    };
+    int top = first - 1;
+    if (first == depth) {
+        prolong(depth - 1);
+        top = depth - 2;
     }
+    for (int l = top; l >= 1; --l) {
+        for (int k = 0; k < 3; ++k) jacobi(l);
+        prolong(l);
+    }
+    for (int k = 0; k < 2; ++k) jacobi(0);               // level 0 post-smoothing
     const int n = c->dp.Nf * D;
     const int blocks = std::min<int>(grid_for(n, 256), kReduceBlocks);
     { k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
-                                                   (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags); MPH_COUNT_LAUNCH(); }
+                                                     (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags); MPH_COUNT_LAUNCH(); }
+}
+
+// FP32 V-cycle of the mixed form: the FP32 copies of the level stencils and
+// of D^-1 (prepared after the FP64 build), FP32 level vectors, FP64 (q,u) dot
+void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
+{
+    DeviceState& d = c->d;
+    const float* invDiag32 = d.v32 + 7 * (size_t)c->dp.Nf * c->dim;
+    if (c->dim == 2)
+        vcycle_t<2, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
+    else
+        vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
 }
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)
 {
+    DeviceState& d = c->d;
     if (c->dim == 2)
-        vcycle_t<2, double, double>(c, q, u, c->d.invDiag, c->d.mg_cof, c->d.mg_invd, c->d.mg_q, c->d.mg_s, c->d.mg_r, dot_out);
+        vcycle_t<2, double, double>(c, q, u, d.invDiag, d.mg_cof, d.mg_invd, d.mg_q, d.mg_s, d.mg_r, d.mg_res, dot_out);
     else
-        vcycle_t<3, double, double>(c, q, u, c->d.invDiag, c->d.mg_cof, c->d.mg_invd, c->d.mg_q, c->d.mg_s, c->d.mg_r, dot_out);
+        vcycle_t<3, double, double>(c, q, u, d.invDiag, d.mg_cof, d.mg_invd, d.mg_q, d.mg_s, d.mg_r, d.mg_res, dot_out);
 }
 
 }  // namespace mph

@@ -236,13 +236,5 @@ int run_cr_solve(mph_case* c)
     return c->dim == 2 ? cr_solve_t<2>(c) : cr_solve_t<3>(c);
 }
 
-// Mixed precision (FP32 inner CR + V-cycle, FP64 outer refinement) is not
-// built yet: such cases are refused at creation.
-bool mixed_available() { return false; }
-int run_mixed_solve(mph_case* c)
-{
-    (void)c;
-    return fail(MPH_ERR_ARG, "mixed precision solve is not available in this build");
-}
 
 }  // namespace mph

@@ -2,6 +2,7 @@
 // point catches C++ exceptions and turns them into status codes.
 #include <exception>
 #include <new>
+#include <string>
 
 #include "mph_internal.h"
 
@@ -69,6 +70,30 @@ int mph_batch_step(mph_case** cases, int ncases, int nsteps)
     } catch (...) {
         return mph::fail(MPH_ERR_STATE, "exception in batch step");
     }
+}
+
+int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel_residual, int max_outer)
+{
+    NEED(c);
+    if (!(outer_rel_residual > 0.0) || !(inner_rel_residual > 0.0) || inner_rel_residual >= 1.0 || max_outer < 1)
+        return mph::fail(MPH_ERR_ARG, "solver tolerances must be positive (inner < 1) and max_outer >= 1");
+    if (c->precision == MPH_PRECISION_FP64 && outer_rel_residual != 1.0e-6)
+        return mph::fail(MPH_ERR_ARG, "the FP64 form keeps the reference's tolerance 1e-6");
+    c->tol_outer = outer_rel_residual;
+    c->tol_inner = inner_rel_residual;
+    c->max_outer = max_outer;
+    return MPH_OK;
+}
+
+int mph_case_set_option(mph_case* c, const char* name, double value)
+{
+    NEED(c);
+    if (!name) return mph::fail(MPH_ERR_ARG, "null option name");
+    if (std::string(name) == "cell_assembly") {
+        c->cell_assembly = value != 0.0;
+        return MPH_OK;
+    }
+    return mph::fail(MPH_ERR_ARG, std::string("unknown option: ") + name);
 }
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count)

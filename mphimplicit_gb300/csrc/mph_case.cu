@@ -159,6 +159,13 @@ static int derive(mph_case* c, const mph_particles* parts)
     }
     for (int d = 0; d < 3; ++d) P.gravity[d] = p.gravity[d];
     P.visc = two_d ? 8.0 : 10.0;
+    P.inv_rv = 1.0 / P.rV;
+    P.m2h_rv = -2.0 / P.rV;
+    P.inv_rp = 1.0 / P.rP;
+    P.m2h_rp = -2.0 / P.rP;
+    for (int t = 0; t < kTypeCount; ++t)
+        for (int u = 0; u < kTypeCount; ++u)
+            P.muij[t][u] = 2.0 * (P.mu[t] * P.mu[u]) / (P.mu[t] + P.mu[u]);
     // walls (initializeWall main.cpp:1023-1062; theta = |omega|^2 as written there)
     for (int t = 0; t < 4; ++t)
         for (int d = 0; d < 3; ++d) {
@@ -328,6 +335,7 @@ int case_alloc_particles(mph_case* c)
     MPH_TRY(dalloc(c, &d.flags, kFlagCount));
     MPH_TRY(dalloc(c, &d.bbox, 8));
     MPH_TRY(dalloc(c, &d.totals, 8));
+    MPH_TRY(dalloc(c, &d.dmax, 4));
     MPH_CUDA(cudaMemsetAsync(d.flags, 0, kFlagCount * sizeof(int), c->stream));
     return MPH_OK;
 }
@@ -411,6 +419,7 @@ static int grow(void** p, long long* cap, long long need, size_t elem)
 int stage_step_begin(mph_case* c)
 {
     launch_step_begin(c);
+    c->densa_valid = false;
     // WallCenter += WallVelocity*Dt after the particles moved (main.cpp:2123-2127)
     for (int t = 2; t < 4; ++t)
         for (int d = 0; d < 3; ++d) c->wallC[t][d] += c->wallV[t][d] * c->dp.dt;
@@ -498,12 +507,12 @@ int stage_mg_build(mph_case* c)
     MPH_TRY(grow(&p, &c->d.cap_mg_cof, c->mg_cof_total, sizeof(double)));
     c->d.mg_cof = (double*)p;
     if (c->mg_rows_total > c->d.cap_mg_vec) {
-        for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r}) {
+        for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r, &c->d.mg_res}) {
             if (*b) cudaFree(*b);
             *b = nullptr;
         }
         const long long n = c->mg_rows_total + c->mg_rows_total / 8 + 256;
-        for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r}) MPH_CUDA(cudaMalloc((void**)b, n * sizeof(double)));
+        for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r, &c->d.mg_res}) MPH_CUDA(cudaMalloc((void**)b, n * sizeof(double)));
         c->d.cap_mg_vec = n;
     }
     launch_mg_level0(c);
@@ -588,7 +597,9 @@ int case_destroy(mph_case* c)
     for (void* p : c->allocations) cudaFree(p);
     DeviceState& d = c->d;
     for (void* p : {(void*)d.nind, (void*)d.nindP, (void*)d.acol, (void*)d.aval, (void*)d.aval32, (void*)d.cval,
-                    (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_cof32,
+                    (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
+                    (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
+                    (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags,
                     (void*)d.mg_invd32, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {

@@ -51,6 +51,11 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
     auto i32 = [&](const int* p, size_t n) { o.kind = 0; return d2h(c, o.i32, p, n); };
     auto i64 = [&](const long long* p, size_t n) { o.kind = 1; return d2h(c, o.i64, p, n); };
     auto f64 = [&](const double* p, size_t n) { o.kind = 2; return d2h(c, o.f64, p, n); };
+    if (name == "DensityA" || name == "GravityCenter" || name == "PressureA") {
+        if (c->stage == 1 || c->stage == 2) return fail(MPH_ERR_STATE, name + " needs this step's neighbour lists");
+        ensure_density_a(c);
+        MPH_CUDA(cudaGetLastError());
+    }
     if (name == "Position") { o.kind = 2; return vec3(c, d.pos, o.f64, c->z_plane); }
     if (name == "Velocity") { o.kind = 2; return vec3(c, d.vel, o.f64, 0.0); }
     if (name == "Force") { o.kind = 2; return vec3(c, d.force, o.f64, 0.0); }
@@ -166,7 +171,17 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
         const int L = std::atoi(name.c_str() + colon + 1);
         if (L < 0 || L >= c->depth) return fail(MPH_ERR_ARG, "no such multigrid level");
         const LevelGeom& g = c->lv[L];
-        if (base == "MultiGridCsrCofA") return f64(d.mg_cof + g.off_cof, (size_t)g.rows * D * g.st[0] * g.st[1] * g.st[2]);
+        if (base == "MultiGridCsrCofA") {
+            // stored entry-major; returned row-major like the reference's CSR rows
+            const size_t width = (size_t)D * g.st[0] * g.st[1] * g.st[2];
+            std::vector<double> t;
+            MPH_TRY(d2h(c, t, d.mg_cof + g.off_cof, (size_t)g.rows * width));
+            o.kind = 2;
+            o.f64.resize(t.size());
+            for (size_t row = 0; row < (size_t)g.rows; ++row)
+                for (size_t e = 0; e < width; ++e) o.f64[row * width + e] = t[e * g.rows + row];
+            return MPH_OK;
+        }
         if (base == "MultiGridInvDiagA") return f64(d.mg_invd + g.off_vec, (size_t)g.rows);
         if (base == "MultiGridGeom") {
             o.kind = 0;
@@ -294,6 +309,7 @@ int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_c
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     if (wall_center) std::memcpy(&c->wallC[0][0], wall_center, sizeof(c->wallC));
     c->time = parts->time;
+    c->densa_valid = false;
     c->fB = 0;
     c->fE = nf;
     c->wB = nf;

@@ -16,8 +16,8 @@
 //   matrix C                        : per fluid particle, D values per P-neighbour,
 //                                      aligned with the P-list (row-contiguous)
 //   multigrid level L               : dense 3^D-cell block stencil per grid cell,
-//                                      value (cell, r, slot, s) at
-//                                      ((cell*D + r)*S + slot)*D + s, S = 3^D.
+//                                      entry-major: row = cell*D + r, entry
+//                                      e = slot*D + s, value at e*rows + row.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -50,6 +50,8 @@ struct DevParams {
     double ratio[kTypeCount][kTypeCount];
     double gravity[3];
     double visc;                               // 8 (2D) or 10 (3D)
+    double inv_rv, m2h_rv, inv_rp, m2h_rp;     // 1/h and -2/h of the V and P kernels (assembly)
+    double muij[kTypeCount][kTypeCount];       // harmonic mean 2 mu_i mu_j / (mu_i + mu_j)
     float maxR2_lo, maxR2_hi, rP2_lo, rP2_hi;  // FP32 pre-classification band
     float w32[3], hw32[3];
     int exact_only;                            // 1: skip the FP32 pre-classification
@@ -93,11 +95,22 @@ struct DeviceState {
     long long cap_cval = 0;
     // level-0 partial stencils per fluid row: [Nf][S][D*D]
     double* part = nullptr;
+    // transpose of the fluid P-lists (cell-block assembly) and per-cell
+    // fallback flags; capacities in bytes
+    int* ct_cnt = nullptr;
+    long long* ct_ptr = nullptr;
+    int* ct_j = nullptr;
+    double* ct_v = nullptr;
+    int* cell_flags = nullptr;
+    int* dmax = nullptr;
+    long long cap_ct_cnt = 0, cap_ct_ptr = 0, cap_ct_j = 0, cap_ct_v = 0, cap_cell_flags = 0;
     // multigrid
     double *mg_cof = nullptr, *mg_invd = nullptr;
-    double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr;
+    double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr, *mg_res = nullptr;   // Q, S ping-pong pair, residual
     float *mg_cof32 = nullptr, *mg_invd32 = nullptr;
-    long long cap_mg_cof = 0, cap_mg_vec = 0;
+    float *mg_q32 = nullptr, *mg_s32 = nullptr, *mg_r32 = nullptr, *mg_res32 = nullptr;
+    float* v32 = nullptr;           // mixed form: 7 FP32 CR vectors + FP32 D^-1, each D*Nf
+    long long cap_mg_cof = 0, cap_mg_vec = 0, cap_mg_cof32 = 0, cap_mg_vec32 = 0;
     // solver vectors [D*Nf]
     double *x = nullptr, *r = nullptr, *s = nullptr, *y = nullptr, *p = nullptr, *q = nullptr, *u = nullptr;
     double* partials = nullptr;     // block partial sums for reductions
@@ -151,8 +164,13 @@ struct mph_case {
     // stage bookkeeping
     int stage = 0;                      // last completed stage
     bool have_output = false;
+    bool densa_valid = false;           // DensityA / GravityCenter / PressureA hold this step's values
     mph_solve_stats stats{};
     int iter_cap = 0;
+    double tol_outer = 1.0e-6;          // ||b - A x|| / ||b|| stop (the reference's rr/rr0 < 1e-12)
+    double tol_inner = 1.0e-3;          // mixed form: inner relative reduction
+    int max_outer = 50;                 // mixed form: refinement steps
+    bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     mph::DeviceState d;
     std::vector<void*> allocations;
     mph::Profile prof;
@@ -217,8 +235,11 @@ int launch_scan_i32_to_i64(mph_case* c, const int* in, long long* out, int n);
 void launch_neighbor_fill(mph_case* c);
 void launch_explicit(mph_case* c);
 void launch_explicit_density_only(mph_case* c);
+void launch_density_full(mph_case* c);
+void ensure_density_a(mph_case* c);
 void launch_output_fields(mph_case* c);
 int launch_assemble(mph_case* c);
+int launch_assemble_cells(mph_case* c, int kmax_rows, bool* done);
 void launch_mg_level0(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);

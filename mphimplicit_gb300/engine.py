@@ -59,6 +59,8 @@ def load_library(path: str = LIB_PATH):
         "mph_scalars": ([vp, ctypes.POINTER(ctypes.c_double), ip], ip),
         "mph_scalar_names": ([], cp),
         "mph_case_profile": ([vp, ip], ip),
+        "mph_case_set_solver": ([vp, ctypes.c_double, ctypes.c_double, ip], ip),
+        "mph_case_set_option": ([vp, cp, ctypes.c_double], ip),
         "mph_case_profile_read": ([vp, ctypes.POINTER(ctypes.c_double), ip], ip),
         "mph_launch_count": ([], ctypes.c_longlong),
         "mph_last_error": ([], cp),
@@ -161,7 +163,14 @@ class Case:
     def solve_stats(self) -> Dict[str, float]:
         s = MphSolveStats()
         _check(self.lib.mph_get_solve_stats(self.h, ctypes.byref(s)))
-        return {"iter": s.iterations, "rr0": s.rr0, "rr": s.rr, "rs0": s.rs0, "rs": s.rs, "status": s.status}
+        return {"iter": s.iterations, "rr0": s.rr0, "rr": s.rr, "rs0": s.rs0, "rs": s.rs, "status": s.status,
+                "outer": s.outer_iterations}
+
+    def set_solver(self, outer_rel_residual: float = 1e-6, inner_rel_residual: float = 1e-3, max_outer: int = 50):
+        _check(self.lib.mph_case_set_solver(self.h, outer_rel_residual, inner_rel_residual, max_outer))
+
+    def set_option(self, name: str, value: float):
+        _check(self.lib.mph_case_set_option(self.h, name.encode(), float(value)))
 
     def time(self) -> float:
         t = ctypes.c_double()

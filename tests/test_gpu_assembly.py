@@ -1,0 +1,74 @@
+"""The two assembly kernels of A agree, and the cell-block kernel matches
+the oracle on cases large enough for it to apply (at least 3 neighbour cells
+of fluid along every axis).
+
+k_assemble_cells gathers C Lambda C^T column by column through the
+transposed P-lists; k_matrix_a merge-joins the P-lists pair by pair
+(multiplyMatrixC, main.cpp:2590-2641).  Both sum the same products in
+different orders, so they agree to rounding."""
+import numpy as np
+import pytest
+
+from mphimplicit_gb300 import casegen, engine
+from parity_util import csr_blocks_oracle, mg_proj, rel, vec_proj
+
+pytestmark = pytest.mark.gpu
+
+
+def medium_cases():
+    p2, parts2 = casegen.square_drop_2d(scale=0.25, seed=2)
+    parts3 = casegen.dam_case(3, (11, 10, 12), (16, 13, 14), 0.005, seed=4,
+                              fluid_types=(np.arange(11 * 10 * 12) % 4 == 0).astype(np.int32))
+    p3 = casegen.baseline_params(3, 0.005, 5.0e-5)
+    p3.density = (1000.0, 1100.0, 1000.0, 1000.0)
+    p3.shear_viscosity = (0.1, 0.5, 0.1, 0.1)
+    return [("dam2d_25", 2, p2, parts2), ("cube3d_11", 3, p3, parts3)]
+
+
+CASES = medium_cases()
+IDS = [c[0] for c in CASES]
+
+
+def _assembled(params, parts, dim, cell):
+    g = engine.Case(params, parts, dim)
+    g.set_option("cell_assembly", 1 if cell else 0)
+    for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
+        g.stage(st)
+    return g
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_cell_and_row_assembly_agree(engine_lib, case):
+    name, dim, params, parts = case
+    a = _assembled(params, parts, dim, True)
+    b = _assembled(params, parts, dim, False)
+    assert np.array_equal(a.export("CsrIndA"), b.export("CsrIndA"))
+    assert rel(a.export("CsrCofA"), b.export("CsrCofA")) <= 1e-12
+    assert rel(a.export("VectorB"), b.export("VectorB")) <= 1e-12
+    assert rel(a.export("InvDiagA"), b.export("InvDiagA")) <= 1e-12
+    depth = int(a.scalars()["MultiGridDepth"])
+    assert depth >= 2
+    for L in range(depth):
+        assert rel(a.export(f"MultiGridCsrCofA:{L}"), b.export(f"MultiGridCsrCofA:{L}")) <= 1e-12, L
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_cell_assembly_matches_oracle(engine_lib, oracle_built, case):
+    name, dim, params, parts = case
+    o = oracle_built.Oracle(params, parts, dim, threads=1)
+    o.init()
+    o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build()
+    g = _assembled(params, parts, dim, True)
+    nf = g.fluid_count
+    nfc = o.array("NeighborFluidCount")[:nf]
+    oa = csr_blocks_oracle(o.array("CsrPtrA"), o.array("CsrCofA"), nf, nfc, dim)
+    assert rel(g.export("CsrCofA"), oa) <= 1e-11
+    assert rel(g.export("VectorB"), vec_proj(o.array("VectorB"), dim).ravel()) <= 1e-11
+    for L, lv in enumerate(o.mg_levels()):
+        assert rel(g.export(f"MultiGridCsrCofA:{L}"), mg_proj(lv["cof"], dim)) <= 1e-11, L
+    # one full solve on top: same tolerance band as the other parity tests
+    o.solve()
+    g.stage("solve")
+    vo = vec_proj(o.array("Velocity"), dim)[:nf]
+    vg = vec_proj(g.export("Velocity"), dim)[:nf]
+    assert np.linalg.norm(vg - vo) / np.linalg.norm(vo) <= 2e-5

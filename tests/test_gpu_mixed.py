@@ -1,0 +1,67 @@
+"""The mixed-precision form (FP32 inner CR + FP32 V-cycle, FP64 outer
+refinement) against the FP64 oracle.
+
+Everything before the solve is the FP64 form's code, so only the solve is
+checked here: with the reference's tolerance the velocity must solve the
+oracle's FP64 system to ||b - A x|| / ||b|| < 1e-6 and stay within the same
+band of the oracle as the FP64 form; with a tightened tolerance (1e-10) the
+FP64 residual the engine reports must reach it."""
+import numpy as np
+import pytest
+
+from mphimplicit_gb300 import engine
+from mphimplicit_gb300.cabi import PRECISION_MIXED
+from parity_util import small_cases, vec_proj
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+IDS = [c[0] for c in CASES]
+
+
+def oracle_residual(ptr, ind, val, b, x):
+    rows = np.repeat(np.arange(len(ptr) - 1), np.diff(ptr))
+    ax = np.bincount(rows, weights=val * x[ind], minlength=len(ptr) - 1)
+    return float(np.linalg.norm(b - ax) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_mixed_solve_meets_reference_tolerance(engine_lib, oracle_built, case):
+    name, dim, params, parts = case
+    o = oracle_built.Oracle(params, parts, dim, threads=1)
+    o.init()
+    g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
+        g.stage(st)
+    o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build()
+    ptr, ind, val, bo = o.array("CsrPtrA"), o.array("CsrIndA"), o.array("CsrCofA"), o.array("VectorB")
+    o.solve()
+    g.stage("solve")
+    s = g.solve_stats()
+    assert s["status"] == 0 and s["outer"] >= 1
+    nf = g.fluid_count
+    x = np.zeros((nf, 3))
+    x[:, :dim] = vec_proj(g.export("Velocity"), dim)[:nf]
+    assert oracle_residual(ptr, ind, val, bo, x.ravel()) < 1.0e-6 * 1.05
+    vo = vec_proj(o.array("Velocity"), dim)[:nf]
+    err = np.linalg.norm(x[:, :dim] - vo) / np.linalg.norm(vo)
+    assert err <= 2e-5, err
+
+
+@pytest.mark.parametrize("case", CASES[:1] + CASES[2:3], ids=[IDS[0], IDS[2]])
+def test_mixed_tight_tolerance(engine_lib, oracle_built, case):
+    name, dim, params, parts = case
+    g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_solver(1e-10, 1e-3, 50)
+    g.step(2)
+    s = g.solve_stats()
+    assert s["status"] == 0
+    assert s["rr"] / s["rr0"] < 1e-20
+    # and the same state as the FP64 form after two steps, to the FP64 form's band
+    f = engine.Case(params, parts, dim)
+    f.step(2)
+    nf = g.fluid_count
+    vg = vec_proj(g.export("Velocity"), dim)[:nf]
+    vf = vec_proj(f.export("Velocity"), dim)[:nf]
+    assert np.array_equal(g.export("ParticleIndex"), f.export("ParticleIndex"))
+    assert np.linalg.norm(vg - vf) / np.linalg.norm(vf) <= 5e-5
