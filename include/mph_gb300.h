@@ -145,7 +145,12 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
 
 /* Engine options (no counterpart in the reference):
  *   "cell_assembly" 1 (default) / 0: assemble A with the cell-block kernel
- *   where it applies, or with the per-row kernel only (same matrix). */
+ *   where it applies, or with the per-row kernel only (same matrix).
+ *   "graphs" 1 (default) / 0: replay the solver's iteration chunks as CUDA
+ *   graphs, or launch every kernel directly (same arithmetic).  The chunks
+ *   are recorded on a private side stream of the case and launched on the
+ *   case stream.  A step waits on the host for its solver flags, so mph_step
+ *   must not be called while the case stream is being captured. */
 int mph_case_set_option(mph_case* c, const char* name, double value);
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);

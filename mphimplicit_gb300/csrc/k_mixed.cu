@@ -28,23 +28,23 @@ template <int D, int MODE>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                                 const int* __restrict__ acol, const float* __restrict__ aval,
                                                 const float* __restrict__ xin, float* __restrict__ yout,
-                                                double* __restrict__ scal, int* __restrict__ flags, int it, int cap,
-                                                double tol2, double* __restrict__ partials, unsigned* __restrict__ counter,
-                                                double* __restrict__ out)
+                                                double* __restrict__ scal, int* __restrict__ flags, int cap,
+                                                double tol2, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
     constexpr int DD = D * D;
     if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
     const double rr0 = scal[kSIn0];
     const double rr = it == 0 ? rr0 : scal[kSIn];   // the inner solve starts from z = 0: r_in = r32
     const bool bad = !(rr == rr);
     if (it >= cap || rr / rr0 < tol2 || bad) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             flags[kFlagDone] = 1;
-            flags[kFlagIter] = it;
             if (bad) flags[kFlagBad] = 1;
         }
         return;
     }
+    double* out = scal + rho32_slot(it);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (i < Nf) {
@@ -76,10 +76,11 @@ __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ 
     reduce_finalize(acc, partials, counter, out);
 }
 
-__global__ void k_pq32(int n, int it, const float* __restrict__ s, const float* __restrict__ y, float* __restrict__ p,
+__global__ void k_pq32(int n, const float* __restrict__ s, const float* __restrict__ y, float* __restrict__ p,
                        float* __restrict__ q, const double* __restrict__ scal, const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
     if (it == 0) {
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
             p[k] = s[k];
@@ -94,12 +95,15 @@ __global__ void k_pq32(int n, int it, const float* __restrict__ s, const float* 
     }
 }
 
-__global__ void k_xrs32(int n, int it, float* __restrict__ z, float* __restrict__ r, float* __restrict__ s,
+// z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
+// then advances the iteration counter flags[kFlagIter].
+__global__ void k_xrs32(int n, float* __restrict__ z, float* __restrict__ r, float* __restrict__ s,
                         const float* __restrict__ p, const float* __restrict__ q, const float* __restrict__ u,
-                        double* __restrict__ scal, const int* __restrict__ flags, double* __restrict__ partials,
+                        double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                         unsigned* __restrict__ counter)
 {
     if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
     const float alpha = (float)(scal[rho32_slot(it)] / scal[kSQU32]);
     double acc = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -109,7 +113,7 @@ __global__ void k_xrs32(int n, int it, float* __restrict__ z, float* __restrict_
         s[k] -= alpha * u[k];
         acc += (double)rk * (double)rk;
     }
-    reduce_finalize(acc, partials, counter, scal + kSIn);
+    reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
 }
 
 // r32 = r / sqrt(rr), z = 0, and the inner reference norm (r32, r32)
@@ -277,6 +281,26 @@ static int mixed_solve_t(mph_case* c)
     int host_flags[kFlagCount];
     double hs[32];
     bool bad = false;
+    // One inner CR iteration; its index lives in flags[kFlagIter] (reset per
+    // outer step), so one launch sequence serves every iteration and replays
+    // as a graph.  Iterations after convergence return at once.
+    auto iteration = [&, c](cudaEvent_t* e) {
+        cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
+        { k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
+                                             counter); MPH_COUNT_LAUNCH(); }
+        if (e) prof_begin(c, 0, &e[1]);
+        { k_pq32<<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+        vcycle_mixed(c, q32, u32, scal + kSQU32);
+        { k_xrs32<<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
+    };
+    const int chunk = 8;
+    const bool graphs = c->use_graphs && !c->prof.on;
+    long long chunk_launches = 0;
+    if (graphs) {
+        MPH_TRY(capture_graph(c, &c->mx_exec, [&] {
+            for (int k = 0; k < chunk; ++k) iteration(nullptr);
+        }, &chunk_launches));
+    }
     for (;;) {
         MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
         MPH_CUDA(cudaStreamSynchronize(st));
@@ -287,21 +311,22 @@ static int mixed_solve_t(mph_case* c)
         { k_to32<<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, scal, part, counter); MPH_COUNT_LAUNCH(); }
         // inner CR from z = 0: r_in = r32, s = M r_in
         vcycle_mixed(c, r32, s32, scal + kSQU32);
-        int it = 0;
+        int it = 0;   // iterations launched
         bool done = false;
-        const int chunk = 8;
         std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
         while (!done) {
-            const int m = std::min(chunk, cap + 1 - it);
-            for (int k = 0; k < m; ++k, ++it) {
-                cudaEvent_t e[2] = {nullptr, nullptr};
-                const bool pon = prof_begin(c, 0, &e[0]) != 0;
-                { k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, it, cap, tol_in2, part,
-                                                     counter, scal + rho32_slot(it)); MPH_COUNT_LAUNCH(); }
-                if (pon) { prof_begin(c, 0, &e[1]); timed.push_back({it, {e[0], e[1]}}); }
-                { k_pq32<<<rb, kReduceThreads, 0, st>>>(n, it, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
-                vcycle_mixed(c, q32, u32, scal + kSQU32);
-                { k_xrs32<<<rb, kReduceThreads, 0, st>>>(n, it, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
+            if (graphs) {
+                MPH_CUDA(cudaGraphLaunch(c->mx_exec, st));
+                g_launch_count += chunk_launches;
+                it += chunk;
+            } else {
+                const int m = std::min(chunk, cap + 1 - it);
+                for (int k = 0; k < m; ++k, ++it) {
+                    cudaEvent_t e[2] = {nullptr, nullptr};
+                    const bool pon = prof_begin(c, 0, &e[0]) != 0;
+                    iteration(pon ? e : nullptr);
+                    if (pon) timed.push_back({it, {e[0], e[1]}});
+                }
             }
             MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
             MPH_CUDA(cudaStreamSynchronize(st));

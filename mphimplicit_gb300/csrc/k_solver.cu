@@ -39,29 +39,31 @@ __global__ void k_cr_init(int Nf, const int* __restrict__ type, const double* __
     reduce_finalize(acc, partials, counter, out);
 }
 
-// MODE 0: r = b - A x with (r,r) -> out.   MODE 1: y = A s with (s,y) -> out,
-// after the convergence test of iteration `it`.
+// MODE 0: r = b - A x with (r,r) -> out.   MODE 1: y = A s with (s,y) ->
+// the rho slot of iteration it = flags[kFlagIter], after the convergence test
+// of that iteration (out is unused).
 template <int D, int MODE>
 __global__ void __launch_bounds__(128) k_spmv(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                               const int* __restrict__ acol, const double* __restrict__ aval,
                                               const double* __restrict__ xin, const double* __restrict__ b,
                                               double* __restrict__ yout, double* __restrict__ scal, int* __restrict__ flags,
-                                              int it, int cap, double* __restrict__ partials, unsigned* __restrict__ counter,
+                                              int cap, double* __restrict__ partials, unsigned* __restrict__ counter,
                                               double* __restrict__ out)
 {
     constexpr int DD = D * D;
     if (MODE == 1) {
         if (flags[kFlagDone]) return;
+        const int it = flags[kFlagIter];
         const double rr = scal[kSRR], rr0 = scal[kSRR0];
         const bool bad = !(rr == rr);   // NaN residual
         if (it >= cap || rr / rr0 < 1.0e-12 || bad) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 flags[kFlagDone] = 1;
-                flags[kFlagIter] = it;
                 if (bad) flags[kFlagBad] = 1;
             }
             return;
         }
+        out = scal + rho_slot(it);
     }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double acc = 0.0;
@@ -99,10 +101,11 @@ __global__ void __launch_bounds__(128) k_spmv(int Nf, const int* __restrict__ nf
     reduce_finalize(acc, partials, counter, out);
 }
 
-__global__ void k_update_pq(int n, int it, const double* __restrict__ s, const double* __restrict__ y, double* __restrict__ p,
+__global__ void k_update_pq(int n, const double* __restrict__ s, const double* __restrict__ y, double* __restrict__ p,
                             double* __restrict__ q, const double* __restrict__ scal, const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
     if (it == 0) {
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
             p[k] = s[k];
@@ -117,12 +120,15 @@ __global__ void k_update_pq(int n, int it, const double* __restrict__ s, const d
     }
 }
 
-__global__ void k_update_xrs(int n, int it, double* __restrict__ x, double* __restrict__ r, double* __restrict__ s,
+// x += alpha p, r -= alpha q, s -= alpha u, (r,r) -> rr; the last block then
+// advances the iteration counter flags[kFlagIter].
+__global__ void k_update_xrs(int n, double* __restrict__ x, double* __restrict__ r, double* __restrict__ s,
                              const double* __restrict__ p, const double* __restrict__ q, const double* __restrict__ u,
-                             double* __restrict__ scal, const int* __restrict__ flags, double* __restrict__ partials,
+                             double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                              unsigned* __restrict__ counter)
 {
     if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
     const double alpha = scal[rho_slot(it)] / scal[kSQU];
     double acc = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -132,7 +138,7 @@ __global__ void k_update_xrs(int n, int it, double* __restrict__ x, double* __re
         s[k] -= alpha * u[k];
         acc += rk * rk;
     }
-    reduce_finalize(acc, partials, counter, scal + kSRR);
+    reduce_finalize_step(acc, partials, counter, scal + kSRR, flags + kFlagIter);
 }
 
 __global__ void k_dot(int n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ partials,
@@ -171,35 +177,55 @@ static int cr_solve_t(mph_case* c)
                                                 c->dp.density[1], c->dp.vol, c->dp.dt, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.bvec, c->d.s, scal + kSRS0);
     { k_spmv<D, 0><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.x, c->d.bvec, c->d.r, scal, flags, 0,
-                                     0, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+                                     part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.r, c->d.s, scal + kSQU);
 
+    // One CR iteration; the iteration index lives in flags[kFlagIter], so the
+    // same launch sequence serves every iteration (and can be replayed as a
+    // graph).  Iterations after convergence return at once.
     const int cap = n;   // the reference iterates at most N = D*Nf times
+    auto iteration = [&, c](cudaEvent_t* e) {
+        cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
+        { k_spmv<D, 1><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.s, nullptr, c->d.y, scal, flags,
+                                         cap, part, counter, nullptr); MPH_COUNT_LAUNCH(); }
+        if (e) prof_begin(c, 0, &e[1]);
+        { k_update_pq<<<rb, kReduceThreads, 0, st>>>(n, c->d.s, c->d.y, c->d.p, c->d.q, scal, flags); MPH_COUNT_LAUNCH(); }
+        if (e) prof_begin(c, 1, &e[2]);
+        vcycle_fp64(c, c->d.q, c->d.u, scal + kSQU);
+        if (e) prof_begin(c, 1, &e[3]);
+        { k_update_xrs<<<rb, kReduceThreads, 0, st>>>(n, c->d.x, c->d.r, c->d.s, c->d.p, c->d.q, c->d.u, scal, flags, part,
+                                                    counter); MPH_COUNT_LAUNCH(); }
+    };
     const int chunk = 8;
     int host_flags[kFlagCount];
-    int it = 0;
+    int it = 0;   // iterations launched
     bool done = false;
     // (iteration | class bit, events) of timed SpMV / V-cycle launches; only
     // launches of iterations that ran are kept (later ones return at once)
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
+    const bool graphs = c->use_graphs && !c->prof.on;
+    long long chunk_launches = 0;
+    if (graphs) {
+        MPH_TRY(capture_graph(c, &c->cr_exec, [&] {
+            for (int k = 0; k < chunk; ++k) iteration(nullptr);
+        }, &chunk_launches));
+    }
     while (!done) {
-        const int m = std::min(chunk, cap + 1 - it);
-        for (int k = 0; k < m; ++k, ++it) {
-            cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
-            const bool pon = prof_begin(c, 0, &e[0]) != 0;
-            { k_spmv<D, 1><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.s, nullptr, c->d.y, scal, flags,
-                                             it, cap, part, counter, scal + rho_slot(it)); MPH_COUNT_LAUNCH(); }
-            if (pon) prof_begin(c, 0, &e[1]);
-            { k_update_pq<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.s, c->d.y, c->d.p, c->d.q, scal, flags); MPH_COUNT_LAUNCH(); }
-            if (pon) prof_begin(c, 1, &e[2]);
-            vcycle_fp64(c, c->d.q, c->d.u, scal + kSQU);
-            if (pon) {
-                prof_begin(c, 1, &e[3]);
-                timed.push_back({it, {e[0], e[1]}});
-                timed.push_back({it | (1 << 30), {e[2], e[3]}});
+        if (graphs) {
+            MPH_CUDA(cudaGraphLaunch(c->cr_exec, st));
+            g_launch_count += chunk_launches;
+            it += chunk;
+        } else {
+            const int m = std::min(chunk, cap + 1 - it);
+            for (int k = 0; k < m; ++k, ++it) {
+                cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+                const bool pon = prof_begin(c, 0, &e[0]) != 0;
+                iteration(pon ? e : nullptr);
+                if (pon) {
+                    timed.push_back({it, {e[0], e[1]}});
+                    timed.push_back({it | (1 << 30), {e[2], e[3]}});
+                }
             }
-            { k_update_xrs<<<rb, kReduceThreads, 0, st>>>(n, it, c->d.x, c->d.r, c->d.s, c->d.p, c->d.q, c->d.u, scal, flags, part,
-                                                        counter); MPH_COUNT_LAUNCH(); }
         }
         MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
         MPH_CUDA(cudaStreamSynchronize(st));

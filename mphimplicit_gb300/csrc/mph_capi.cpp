@@ -93,6 +93,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->cell_assembly = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "graphs") {
+        c->use_graphs = value != 0.0;
+        return MPH_OK;
+    }
     return mph::fail(MPH_ERR_ARG, std::string("unknown option: ") + name);
 }
 

@@ -17,7 +17,8 @@
 namespace mph {
 
 static thread_local std::string g_error;
-long long g_launch_count = 0;
+std::atomic<long long> g_launch_count{0};
+thread_local long long t_launch_count = 0;
 
 // ---- profiling (CUDA events on the case stream) ------------------------------
 static cudaEvent_t take_event(mph_case* c)
@@ -594,6 +595,9 @@ int case_destroy(mph_case* c)
     if (!c) return MPH_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
     else cudaDeviceSynchronize();
+    if (c->cr_exec) cudaGraphExecDestroy(c->cr_exec);
+    if (c->mx_exec) cudaGraphExecDestroy(c->mx_exec);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     for (void* p : c->allocations) cudaFree(p);
     DeviceState& d = c->d;
     for (void* p : {(void*)d.nind, (void*)d.nindP, (void*)d.acol, (void*)d.aval, (void*)d.aval32, (void*)d.cval,

@@ -21,6 +21,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -123,9 +124,11 @@ struct DeviceState {
     size_t scan_tmp_bytes = 0;
 };
 
-// Kernel launches issued by this library (host-side count).
-extern long long g_launch_count;
-#define MPH_COUNT_LAUNCH() (++::mph::g_launch_count)
+// Kernel launches issued by this library (host-side count, all threads), and
+// the calling thread's own count (used to count the launches of a capture).
+extern std::atomic<long long> g_launch_count;
+extern thread_local long long t_launch_count;
+#define MPH_COUNT_LAUNCH() (++::mph::g_launch_count, ++::mph::t_launch_count)
 
 // Optional CUDA-event timing on the case stream: per stage and per launch of
 // the hot kernels.
@@ -171,6 +174,10 @@ struct mph_case {
     double tol_inner = 1.0e-3;          // mixed form: inner relative reduction
     int max_outer = 50;                 // mixed form: refinement steps
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
+    bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
+    cudaGraphExec_t cr_exec = nullptr;  // FP64 CR chunk
+    cudaGraphExec_t mx_exec = nullptr;  // mixed form: FP32 inner CR chunk
+    cudaStream_t cap_stream = nullptr;  // side stream the chunks are captured on
     mph::DeviceState d;
     std::vector<void*> allocations;
     mph::Profile prof;

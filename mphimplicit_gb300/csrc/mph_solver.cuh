@@ -66,6 +66,75 @@ __device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ p
     }
 }
 
+// As reduce_finalize; the last block also advances the device iteration
+// counter *it (every block read it before taking its ticket).
+__device__ __forceinline__ void reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+                                                     double* __restrict__ out, int* __restrict__ it)
+{
+    __shared__ bool last;
+    const double bs = block_sum(v);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        const unsigned ticket = atomicAdd(counter, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        *out = s;
+        *counter = 0u;
+        *it = *it + 1;
+    }
+}
+
+// Capture `body` (a fixed launch sequence on c->stream) into a CUDA graph and
+// update or instantiate *exec with it; the graph is later launched on
+// c->stream.  The capture records on the case's own side stream (c->stream
+// may be the legacy stream, which cannot be captured): c->stream points
+// there while `body` runs.  Returns the number of kernel launches the
+// sequence contains in *launches.
+template <typename F>
+int capture_graph(mph_case* c, cudaGraphExec_t* exec, F&& body, long long* launches)
+{
+    if (!c->cap_stream) MPH_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    const long long l0 = t_launch_count;
+    cudaGraph_t graph = nullptr;
+    MPH_CUDA(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t saved = c->stream;
+    c->stream = c->cap_stream;
+    body();
+    c->stream = saved;
+    const cudaError_t ec = cudaStreamEndCapture(c->cap_stream, &graph);
+    *launches = t_launch_count - l0;
+    t_launch_count = l0;
+    g_launch_count -= *launches;
+    if (ec != cudaSuccess) return cuda_check(ec, "cudaStreamEndCapture");
+    bool ok = false;
+    if (*exec) {
+        cudaGraphExecUpdateResultInfo info;
+        ok = cudaGraphExecUpdate(*exec, graph, &info) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(*exec);
+            *exec = nullptr;
+        }
+    }
+    if (!ok) {
+        const cudaError_t ei = cudaGraphInstantiate(exec, graph, 0);
+        if (ei != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return cuda_check(ei, "cudaGraphInstantiate");
+        }
+    }
+    cudaGraphDestroy(graph);
+    return MPH_OK;
+}
+
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out);
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
 
