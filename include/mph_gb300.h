@@ -214,6 +214,18 @@ long long mph_launch_count(void);
 const char* mph_last_error(void);
 const char* mph_version(void);
 
+/* Residual norms of the solved system, with no device allocation by the call
+ * (no counterpart in the reference).  out[0] = ||b - A x||^2 and out[1] =
+ * ||b||^2 (host memory) for the system of the last mph_stage_solve; valid
+ * between that stage and mph_stage_step_end, else MPH_ERR_STATE.  Its scratch
+ * is one fixed per-device array of 262,400 bytes, so it serves cases of at
+ * most 2,097,152 fluid particles (larger: MPH_ERR_CAPACITY).  The first call
+ * for a device looks up that array's address: make it before any stream
+ * capture.  Calls that overlap on the GPU share the array and race: serialise
+ * them.  For servers whose device memory is fully committed to resident cases,
+ * where a per-call allocation could fail and a free would stall every stream. */
+int mph_residual_noalloc(mph_case* c, double* out);
+
 #ifdef __cplusplus
 }
 #endif
