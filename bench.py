@@ -54,6 +54,19 @@ def workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+def replica_throughput(units: float, seconds: float, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas: the units every rank
+    processed, summed, over the slowest rank's time (max over ranks)."""
+    if dist is None:
+        return units / seconds, seconds
+    import torch
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
 def measured_peaks():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -199,6 +212,184 @@ def run_reference(args, rank, world):
     return 0
 
 
+def _vel_error_vs_fp64(engine, cases, prec_mixed, prec_fp64, tol_outer):
+    """One step of each (params, parts, dim) in the mixed and the FP64 form
+    from the same state: relative velocity error of the mixed result over the
+    fluid particles (both forms keep the same particle order)."""
+    errs = []
+    for params, parts, dim in cases:
+        out = []
+        for prec in (prec_mixed, prec_fp64):
+            g = engine.Case(params, parts, dim, precision=prec)
+            if prec == prec_mixed:
+                g.set_solver(tol_outer, 1e-3, 50)
+            g.step(1)
+            f = g.fields(("id", "type", "vel"))
+            g.close()
+            out.append(f)
+        a, b = out
+        assert np.array_equal(a["id"], b["id"])
+        fl = b["type"] < 2
+        errs.append(float(np.linalg.norm(a["vel"][fl] - b["vel"][fl]) / max(np.linalg.norm(b["vel"][fl]), 1e-300)))
+    return errs
+
+
+def _fp64_sequential_ms(engine, cases, prec_fp64):
+    """Per-step time of each case run alone in the plain FP64 form (one warm-up
+    step, one timed step, CUDA events on the legacy stream)."""
+    import torch
+    out = []
+    for params, parts, dim in cases:
+        g = engine.Case(params, parts, dim, precision=prec_fp64)
+        g.step(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(torch.cuda.default_stream())
+        g.step(1)
+        e1.record(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+        g.close()
+    return out
+
+
+def run_ensemble(args, line_base):
+    """Batched 2D ensemble (512 cases by default): every timed step advances
+    every case once, all cases concurrently (mph_batch_step)."""
+    import torch
+    from mphimplicit_gb300 import engine, serving
+    from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    ens = casegen.ensemble_2d(args.cases, seed=1)
+    cases = []
+    for params, parts in ens:
+        g = engine.Case(params, parts, 2, precision=prec)
+        if prec == PRECISION_MIXED:
+            g.set_solver(args.outer_tol, args.inner_tol, 50)
+        cases.append(g)
+    N = sum(g.count for g in cases)
+    for _ in range(args.warmup):
+        serving.batch_step(cases, 1, args.workers)
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    l0 = engine.launch_count()
+    with Clocks(0) as clk:
+        evs[0].record(torch.cuda.default_stream())
+        for k in range(args.steps):
+            serving.batch_step(cases, 1, args.workers)
+            evs[k + 1].record(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+    launches = engine.launch_count() - l0
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_s = sum(step_ms) / 1000.0
+    value = N * args.steps / total_s
+    for g in cases:
+        g.close()
+    # plain FP64 form, one case after the other, on an evenly spaced sample
+    idx = list(range(0, len(ens), max(1, len(ens) // args.sample)))[:args.sample]
+    sample = [(ens[i][0], ens[i][1], 2) for i in idx]
+    seq_ms = _fp64_sequential_ms(engine, sample, PRECISION_FP64)
+    plain = sum(ens[i][1].count for i in idx) / (sum(seq_ms) / 1000.0)
+    errs = _vel_error_vs_fp64(engine, sample[:4], PRECISION_MIXED, PRECISION_FP64, args.outer_tol) \
+        if prec == PRECISION_MIXED else []
+    line = dict(line_base)
+    line.update({
+        "value": value, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
+        "dtype": "f64" if prec == PRECISION_FP64 else "f32-inner/f64-outer",
+        "config": {"workload": "ensemble2d", "description": f"{len(ens)} independent 2D cases, fluid n x m, n,m ~ U[40,250] "
+                   "(seed 1), mu log-uniform [0.01,1], gravity angle U[0,30], two fluid types in half (config 3); "
+                   "one step = every case advanced once, all concurrently", "cases": len(ens), "particles": N,
+                   "precision": args.precision, "workers": args.workers, "parallelism": "single",
+                   "l2": "inputs larger than L2 (the cases' matrices total ~GBs)",
+                   "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+                   "plain_fp64_sequential_value": plain,
+                   "plain_fp64_sample": f"{len(idx)} evenly spaced cases, one step each, alone, FP64 form",
+                   "speedup_vs_plain_fp64_sequential": value / plain,
+                   "vel_rel_err_vs_fp64_per_step": errs},
+        "gpu_launches": launches, "clocks": clk.summary(),
+        "e2e": {"value": None, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args, line_base):
+    """Serving loop: Poisson arrivals (20 cases/s, seed 2) of 2D and 3D cases
+    of 1e4..5e5 particles, admitted by device-memory footprint under a 150 GB
+    budget, stepped concurrently; steps per case scaled by --serve-step-scale."""
+    import threading
+    import torch
+    from mphimplicit_gb300 import engine, serving
+    from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    reqs = casegen.serving_requests(args.cases, seed=2, step_scale=args.serve_step_scale)
+    srv = serving.Server(int(150e9), workers=args.workers)
+    lock = threading.Lock()
+    tickets = {}
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k, r in enumerate(reqs):
+            dt = r["t"] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            t = srv.submit(r["params"], r["parts"], r["dim"], r["steps"], precision=prec, fields=("id",))
+            with lock:
+                tickets[t] = k
+
+    th = threading.Thread(target=submitter)
+    l0 = engine.launch_count()
+    with Clocks(0) as clk:
+        th.start()
+        results = []
+        while len(results) < len(reqs):
+            results += srv.poll(wait_ms=100)
+        th.join()
+        torch.cuda.synchronize()
+    launches = engine.launch_count() - l0
+    stats = srv.stats()
+    srv.close()
+    bad = [r for r in results if r["status"] not in (0, 7)]
+    if bad:
+        raise SystemExit(f"served case failed: {bad[0]['error']}")
+    first = min(r["submit_s"] for r in results)
+    last = min(max(r["done_s"] for r in results), stats["elapsed_s"])
+    span = max(r["done_s"] for r in results) - first
+    psteps = sum(r["particles"] * r["steps"] for r in results)
+    value = psteps / span
+    step_ms = np.concatenate([r["step_ms"] for r in results])
+    lat = np.array([r["done_s"] - r["submit_s"] for r in results])
+    # plain FP64 form, the same requests one after the other (per-step time of
+    # each request alone x its steps)
+    sample = [(r["params"], r["parts"], r["dim"]) for r in reqs]
+    seq_ms = _fp64_sequential_ms(engine, sample, PRECISION_FP64)
+    seq_s = sum(ms / 1000.0 * r["steps"] for ms, r in zip(seq_ms, reqs))
+    plain = psteps / seq_s
+    errs = _vel_error_vs_fp64(engine, sample[:4], PRECISION_MIXED, PRECISION_FP64, args.outer_tol) \
+        if prec == PRECISION_MIXED else []
+    line = dict(line_base)
+    line.update({
+        "value": value, "steps": int(sum(r["steps"] for r in results)), "warmup": 0,
+        "ms_per_step": float(np.mean(step_ms)), "dtype": "f64" if prec == PRECISION_FP64 else "f32-inner/f64-outer",
+        "config": {"workload": "serve", "description": f"{len(reqs)} requests, Poisson arrivals 20/s (seed 2), 2D and 3D, "
+                   "1e4..5e5 particles log-uniform, steps U[50,400] x step scale, 150 GB admission budget (config 4)",
+                   "requests": len(reqs), "step_scale": args.serve_step_scale, "precision": args.precision,
+                   "workers": args.workers, "parallelism": "single", "particle_steps": psteps, "span_s": span,
+                   "l2": "inputs larger than L2",
+                   "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+                   "p50_completion_s": float(np.percentile(lat, 50)), "p99_completion_s": float(np.percentile(lat, 99)),
+                   "plain_fp64_sequential_value": plain,
+                   "plain_fp64_sample": "every request alone in the FP64 form: one timed step x its step count",
+                   "speedup_vs_plain_fp64_sequential": value / plain,
+                   "vel_rel_err_vs_fp64_per_step": errs},
+        "gpu_launches": launches, "clocks": clk.summary(),
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": "requests are submitted from host memory and their fields returned to host buffers"},
+    })
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -210,10 +401,20 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=1e-3,
                     help="mixed form: relative residual reduction of each FP32 inner solve")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-factored", action="store_true",
+                    help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
     ap.add_argument("--ref-fluid", type=int, default=50)
+    ap.add_argument("--outer-tol", type=float, default=1e-6,
+                    help="mixed form: FP64 outer relative residual (the reference's tolerance is 1e-6)")
+    ap.add_argument("--cases", type=int, default=0, help="ensemble / serve: number of cases (0: 512 / 24)")
+    ap.add_argument("--workers", type=int, default=32, help="ensemble / serve: host worker threads")
+    ap.add_argument("--sample", type=int, default=16, help="ensemble: cases timed alone in the FP64 form")
+    ap.add_argument("--serve-step-scale", type=float, default=0.1, help="serve: factor on each request's step count")
     args = ap.parse_args()
+    if args.workload in ("ensemble2d", "serve") and args.cases <= 0:
+        args.cases = 512 if args.workload == "ensemble2d" else 24
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -233,12 +434,17 @@ def main():
         build.build()
     if dist:
         dist.barrier()
+    if args.workload in ("ensemble2d", "serve"):
+        base = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "data": "synthetic", "roofline": None, "cpu_baseline": None}
+        return run_ensemble(args, base) if args.workload == "ensemble2d" else run_serve(args, base)
     dim, params, parts, desc = workload(args.workload)
     stream = torch.cuda.Stream()
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
     case = engine.Case(params, parts, dim, precision=prec, stream=stream.cuda_stream)
     if prec == PRECISION_MIXED:
-        case.set_solver(1e-6, args.inner_tol, 50)
+        case.set_solver(args.outer_tol, args.inner_tol, 50)
+        case.set_option("factored", 0 if args.no_factored else 1)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)
@@ -265,11 +471,7 @@ def main():
     prof = case.profile_read()
     case.profile(False)
     scal = case.scalars()
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = N * args.steps * world / total_s
+    value, total_s = replica_throughput(N * args.steps, total_s, dist, "cuda")
 
     # end to end through the public API with host buffers
     fields = case.fields(("id", "type", "pos", "vel"))

@@ -132,8 +132,55 @@ int mph_case_set_stream(mph_case* c, void* stream);
 /* One or more full time steps (the body of main.cpp:386-474, without the
  * file output).  Returns MPH_ERR_NOT_CONVERGED if a solve hit its cap. */
 int mph_step(mph_case* c, int nsteps);
-/* Steps of several independent cases, interleaved on their streams. */
+/* ---- batching and serving (no counterpart in the reference, which runs one
+ * case per process) ----
+ * mph_batch_step advances independent cases concurrently: host worker
+ * threads (one case at a time each) drive the cases' steps, every case on its
+ * own stream (a case on the legacy stream gets a private non-blocking stream
+ * for the call), so the kernels of different cases overlap on the device.
+ * Returns when every case has taken nsteps steps; a case computes the same
+ * bits alone or in a batch.  A case must not appear twice.  workers <= 0:
+ * min(ncases, 2 x host threads, 64). */
 int mph_batch_step(mph_case** cases, int ncases, int nsteps);
+int mph_batch_step_workers(mph_case** cases, int ncases, int nsteps, int workers);
+
+/* Upper bound of the device memory of one case (bytes): the admission unit
+ * of the serving loop. */
+int mph_case_footprint(const mph_params* prm, const mph_particles* parts, int dim, int precision,
+                       long long* bytes);
+
+/* Serving loop on the current device: submitted cases wait in arrival order
+ * until their footprint fits the budget, are then created on their own
+ * stream, kept resident and stepped round-robin by `workers` host threads
+ * together with every other admitted case (continuous batching); a finished
+ * case copies its fields to the caller's buffers (given at submit, kept valid
+ * until the result is polled), frees its memory and admits the next. */
+typedef struct mph_server mph_server;
+typedef struct mph_server_result {
+    long long ticket;
+    int status;              /* MPH_OK, MPH_ERR_NOT_CONVERGED (a solve hit its cap), or the error */
+    int steps;               /* steps completed */
+    int particles;
+    int pad;
+    double submit_s, admit_s, done_s;   /* seconds since mph_server_create */
+    long long footprint_bytes;
+    char error[128];
+} mph_server_result;
+typedef struct mph_server_stats {
+    long long budget_bytes, used_bytes;
+    int pending, active, finished, pad;
+    long long steps;
+    double particle_steps, elapsed_s;
+} mph_server_stats;
+int mph_server_create(long long budget_bytes, int workers, mph_server** out);
+/* out: fields to fill at completion (NULL: none); step_ms: `steps` floats
+ * receiving each step's host-measured latency (NULL: none). */
+int mph_server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision,
+                      int steps, const mph_fields* out, float* step_ms, long long* ticket);
+/* Completed requests (up to max), waiting up to wait_ms for the first. */
+int mph_server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count);
+int mph_server_stats_get(mph_server* s, mph_server_stats* out);
+int mph_server_destroy(mph_server* s);
 
 /* Solver tolerances.  outer_rel_residual: stop when ||b - A x|| / ||b|| is
  * below it (the reference stops at 1e-6: rr/rr0 < 1e-12, main.cpp:4346; this
@@ -150,7 +197,15 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
  *   graphs, or launch every kernel directly (same arithmetic).  The chunks
  *   are recorded on a private side stream of the case and launched on the
  *   case stream.  A step waits on the host for its solver flags, so mph_step
- *   must not be called while the case stream is being captured. */
+ *   must not be called while the case stream is being captured.
+ *   "factored" 1 (default) / 0: mixed form only.  1: where 2 RadiusP <
+ *   MaxRadius, the FP64 operator of the outer residual is applied in factored
+ *   form (viscous pair terms + C Lambda C^T through the transposed P-lists)
+ *   and only FP32 blocks are assembled; CsrCofA then exports the FP32 blocks.
+ *   0: FP64 blocks are assembled and copied to FP32.
+ *   "inner_blocks" 1 (default) / 0: factored mixed form only.  0: the inner
+ *   FP32 SpMV runs on the FP32 pair terms and no blocks are written
+ *   (CsrIndA / CsrCofA exports then fail with MPH_ERR_STATE). */
 int mph_case_set_option(mph_case* c, const char* name, double value);
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);
@@ -217,7 +272,8 @@ const char* mph_version(void);
 /* Residual norms of the solved system, with no device allocation by the call
  * (no counterpart in the reference).  out[0] = ||b - A x||^2 and out[1] =
  * ||b||^2 (host memory) for the system of the last mph_stage_solve; valid
- * between that stage and mph_stage_step_end, else MPH_ERR_STATE.  Its scratch
+ * between that stage and mph_stage_step_end, else MPH_ERR_STATE (also when
+ * the step assembled no FP64 blocks: mixed form, option "factored").  Its scratch
  * is one fixed per-device array of 262,400 bytes, so it serves cases of at
  * most 2,097,152 fluid particles (larger: MPH_ERR_CAPACITY).  The first call
  * for a device looks up that array's address: make it before any stream

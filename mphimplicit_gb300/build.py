@@ -27,8 +27,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off"]
 
 LIB_SOURCES = ["k_particles.cu", "k_neighbor.cu", "k_explicit.cu", "k_assemble.cu", "k_multigrid.cu",
-               "k_solver.cu", "k_mixed.cu", "k_assemble_cells.cu", "k_resid_noalloc.cu", "mph_case.cu", "mph_export.cu",
-               "mph_io.cpp", "mph_capi.cpp"]
+               "k_solver.cu", "k_mixed.cu", "k_assemble_cells.cu", "k_factored.cu", "k_resid_noalloc.cu", "mph_case.cu", "mph_export.cu",
+               "mph_io.cpp", "mph_batch.cpp", "mph_capi.cpp"]
 HEADERS = ["mph_internal.h", "mph_device.cuh", "mph_solver.cuh", os.path.join("..", "..", "include", "mph_gb300.h")]
 
 

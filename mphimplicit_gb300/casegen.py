@@ -233,3 +233,70 @@ def cube_collapse_3d(n: int = 100, seed: int = 0) -> Tuple[Params, Particles]:
     ni = (int(round(1.6 * n)), int(round(1.1 * n)), int(round(1.1 * n)))
     parts = dam_case(3, (n, n, n), ni, 0.005, seed=seed)
     return baseline_params(3, 0.005, 5.0e-5), parts
+
+
+# Batched and served workloads ----------------------------------------------------
+def ensemble_case_2d(n: int, m: int, mu: float, gravity_deg: float, two_fluids: bool,
+                     seed: int) -> Tuple[Params, Particles]:
+    """One 2D case of the batched ensemble: an n x m fluid block (l0 = 0.01)
+    in a 3-layer wall box around a 2n x 1.5m interior (the proportions of the
+    2D dam case), shear viscosity mu, gravity 9.8 m/s^2 tilted by
+    gravity_deg from -y, and with two_fluids the upper half of the block of
+    type 1 with density 1.2x type 0; dt = 1e-4."""
+    types = None
+    if two_fluids:
+        iy = np.tile(np.arange(m), n)           # lattice order: ix major, iy minor
+        types = (iy >= m // 2).astype(np.int32)
+    parts = dam_case(2, (n, m), (2 * n, int(round(1.5 * m)) + 2), 0.01, seed=seed, fluid_types=types)
+    p = baseline_params(2, 0.01, 1.0e-4, mu=mu)
+    a = np.deg2rad(gravity_deg)
+    p = dataclasses.replace(p, gravity=(9.8 * float(np.sin(a)), -9.8 * float(np.cos(a)), 0.0))
+    if two_fluids:
+        p = dataclasses.replace(p, density=(1000.0, 1200.0, 1000.0, 1000.0))
+    return p, parts
+
+
+def ensemble_2d(count: int = 512, seed: int = 1, nmin: int = 40, nmax: int = 250):
+    """The batched 2D ensemble: `count` cases with n, m ~ U[nmin, nmax], shear
+    viscosity log-uniform in [0.01, 1] Pa s, gravity angle ~ U[0, 30] deg, two
+    fluid types in every other case (seeded)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n, m = (int(v) for v in rng.integers(nmin, nmax + 1, size=2))
+        mu = float(10.0 ** rng.uniform(-2.0, 0.0))
+        ang = float(rng.uniform(0.0, 30.0))
+        out.append(ensemble_case_2d(n, m, mu, ang, k % 2 == 1, seed=seed * 1000003 + k))
+    return out
+
+
+def serving_requests(count: int, seed: int = 2, rate: float = 20.0, nmin: float = 1.0e4, nmax: float = 5.0e5,
+                     smin: int = 50, smax: int = 400, step_scale: float = 1.0):
+    """Poisson arrivals (mean `rate` per second) of 2D and 3D cases whose
+    total particle count is log-uniform in [nmin, nmax], each running a
+    number of steps ~ U[smin, smax] (times step_scale, at least 1).  2D cases
+    are ensemble cases; 3D cases are the cube-collapse geometry and constants
+    with the fluid cube sized to the count.  Returns dicts with the arrival
+    time t, dim, params, parts and steps (seeded)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        total = float(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        steps = max(1, int(round(int(rng.integers(smin, smax + 1)) * step_scale)))
+        if rng.random() < 0.5:
+            aspect = float(rng.uniform(0.5, 2.0))
+            nm = 0.85 * total
+            n = max(8, int(round(np.sqrt(nm * aspect))))
+            m = max(8, int(round(nm / n)))
+            mu = float(10.0 ** rng.uniform(-2.0, 0.0))
+            ang = float(rng.uniform(0.0, 30.0))
+            p, parts = ensemble_case_2d(n, m, mu, ang, bool(rng.random() < 0.5), seed=seed * 1000003 + k)
+            dim = 2
+        else:
+            n = max(6, int(round((0.77 * total) ** (1.0 / 3.0))))
+            p, parts = cube_collapse_3d(n, seed=seed * 1000003 + k)
+            dim = 3
+        out.append({"t": t, "dim": dim, "params": p, "parts": parts, "steps": steps})
+    return out

@@ -474,7 +474,15 @@ int launch_assemble(mph_case* c)
     cudaEvent_t pe = nullptr;
     const int pon = prof_begin(c, 2, &pe);
     bool cells = false;
-    if (c->cell_assembly) MPH_TRY(launch_assemble_cells(c, kmax_rows, &cells));
+    c->ct_ready = false;
+    c->step_factored = factored_applies(c);
+    if (c->step_factored) {
+        // mixed form: FP64 pair terms and b, transposed P-lists (the factored
+        // FP64 operator), then FP32 blocks only
+        MPH_TRY(build_ct(c));
+        MPH_TRY(launch_pair_terms(c));
+    }
+    if (c->cell_assembly) MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
     const int* only = cells ? c->d.cell_flags : nullptr;
     float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;
     if (D == 2) {

@@ -20,6 +20,8 @@
 // Cells whose candidate set or rows exceed the shared-memory budget, and
 // grids with fewer than 3 cells along an axis (where the cell walk visits a
 // cell twice), are assembled by k_matrix_a instead.
+#include <type_traits>
+
 #include "mph_device.cuh"
 
 namespace mph {
@@ -76,6 +78,12 @@ __global__ void k_ct_sort(int N, const long long* __restrict__ ctptr, int* __res
     }
 }
 
+__global__ void k_to_f32(long long n, const double* __restrict__ a, float* __restrict__ b)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) b[k] = (float)a[k];
+}
+
 // ---- the cell-block assembly ------------------------------------------------------
 struct CellMap {
     int mn[3], cnt[3], st[3];
@@ -84,7 +92,12 @@ struct CellMap {
 
 constexpr int kAsmWarps = 4;
 
-template <int D>
+// MIX = false: the FP64 blocks (and their FP32 copy when aval32 is given), b
+// and D^-1.  MIX = true (mixed form with the factored FP64 operator): FP32
+// arithmetic throughout, the viscous blocks from the FP32 pair terms pe32
+// (e, f), only the FP32 blocks, D^-1 and the level-0 stencils are written
+// (b comes from k_pair_terms).
+template <int D, bool MIX>
 __global__ void __launch_bounds__(kAsmWarps * 32)
 k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int kmax, const int* __restrict__ type,
                  const int* __restrict__ bucket, const double* __restrict__ pos, const double* __restrict__ vel,
@@ -94,8 +107,10 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
                  const long long* __restrict__ ctptr, const int* __restrict__ ct_j, const double* __restrict__ ct_v,
                  const long long* __restrict__ sptr, int* __restrict__ acol, double* __restrict__ aval,
                  float* __restrict__ aval32, double* __restrict__ bvec, double* __restrict__ invDiag,
-                 int* __restrict__ selfk_out, double* __restrict__ part, int* __restrict__ overflow)
+                 int* __restrict__ selfk_out, double* __restrict__ part, int* __restrict__ overflow,
+                 const float4* __restrict__ pe32, const float* __restrict__ ct_v32, const float* __restrict__ cval32)
 {
+    using T = typename std::conditional<MIX, float, double>::type;
     constexpr int DD = D * D;
     const int c = blockIdx.x;
     const int r0 = bucket[c], r1 = bucket[c + 1];
@@ -104,7 +119,8 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
     __shared__ int nwalk;
     extern __shared__ double smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* acc = smem + (size_t)warp * ((size_t)kmax * DD + mwords);
+    T* acc = reinterpret_cast<T*>(reinterpret_cast<char*>(smem) +
+                                  (size_t)warp * ((size_t)kmax * DD * sizeof(T) + (size_t)mwords * 8));
     unsigned* mask = reinterpret_cast<unsigned*>(acc + (size_t)kmax * DD);
     int* wpre = reinterpret_cast<int*>(mask + mwords);
 
@@ -190,20 +206,37 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
                 run += __popc(mask[w]);
             }
         }
-        for (int t = lane; t < nf * DD; t += 32) acc[t] = 0.0;
+        for (int t = lane; t < nf * DD; t += 32) acc[t] = T(0);
         __syncwarp();
         // 2. viscous blocks (main.cpp:2261-2304)
         const int ti = type[i];
         double xi[3], vi[3];
-        load_vec<D>(pos, i, xi);
-        load_vec<D>(vel, i, vi);
-        double selfc[DD], sumv[3] = {0, 0, 0};
+        if (!MIX) {
+            load_vec<D>(pos, i, xi);
+            load_vec<D>(vel, i, vi);
+        }
+        T selfc[DD];
+        double sumv[3] = {0, 0, 0};
 #pragma unroll
-        for (int t = 0; t < DD; ++t) selfc[t] = 0.0;
+        for (int t = 0; t < DD; ++t) selfc[t] = T(0);
         int myself = -1;
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
             if (j == i) { myself = k; continue; }
+            if (MIX) {
+                const float4 pt = pe32[nb + k];
+                const float e[3] = {pt.x, pt.y, pt.z};
+                const bool fluid = k < nf;
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int s = 0; s < D; ++s) {
+                        const float coef = pt.w * e[s] * e[r];
+                        selfc[r * D + s] += coef;
+                        if (fluid) acc[k * DD + r * D + s] = -coef;
+                    }
+                continue;
+            }
             double xj[3], q[3];
             load_vec<D>(pos, j, xj);
             sep_vec<D>(P, xj, xi, q);
@@ -223,8 +256,8 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
 #pragma unroll
                 for (int s = 0; s < D; ++s) {
                     const double coef = f * e[s] * e[r];
-                    selfc[r * D + s] += coef;
-                    if (fluid) acc[k * DD + r * D + s] = -coef;
+                    selfc[r * D + s] += (T)coef;
+                    if (fluid) acc[k * DD + r * D + s] = (T)-coef;
                     else sumv[r] += coef * vj[s];
                 }
         }
@@ -237,14 +270,15 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
         const int self = __reduce_max_sync(0xffffffffu, myself);
-        const double m = P.density[ti] * P.vol;
-        const double inert = m / P.vol / P.dt;
+        // inertia density/dt as the reference forms it, (rho*vol)/vol/dt; the
+        // FP32 form takes its host-rounded FP32 value (no FP64 on the device)
+        const T inert = MIX ? (T)P.inert32[ti] : (T)(P.density[ti] * P.vol / P.vol / P.dt);
         __syncwarp();
         if (lane == 0) {
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int s = 0; s < D; ++s) acc[self * DD + r * D + s] = selfc[r * D + s] + (r == s ? inert : 0.0);
+                for (int s = 0; s < D; ++s) acc[self * DD + r * D + s] = selfc[r * D + s] + (r == s ? (T)inert : T(0));
         }
         __syncwarp();
         // 3. C Lambda C^T, one P-neighbour column at a time (main.cpp:2590-2641)
@@ -252,18 +286,29 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
         const int np = ncp[i];
         for (int a = 0; a < np; ++a) {
             const int k = nindP[pb + a];
-            const double lam = P.lambda[type[k]];
-            double ga[3];
+            T ga[3];
+            if (MIX) {
+                const float lam = P.lambda32[type[k]];
 #pragma unroll
-            for (int r = 0; r < D; ++r) ga[r] = cval[(pb + a) * D + r] * lam;
+                for (int r = 0; r < D; ++r) ga[r] = cval32[(pb + a) * D + r] * lam;
+            } else {
+                const double lam = P.lambda[type[k]];
+#pragma unroll
+                for (int r = 0; r < D; ++r) ga[r] = (T)(cval[(pb + a) * D + r] * lam);
+            }
             const long long e0 = ctptr[k], e1 = ctptr[k + 1];
             for (long long e = e0 + lane; e < e1; e += 32) {
                 const int l = local_of(ct_j[e]);
                 if (l < 0 || !((mask[l >> 5] >> (l & 31)) & 1u)) continue;
                 const int slot = rank_of(l);
-                double cj[3];
+                T cj[3];
+                if (MIX) {
 #pragma unroll
-                for (int s = 0; s < D; ++s) cj[s] = ct_v[e * D + s];
+                    for (int s = 0; s < D; ++s) cj[s] = (T)ct_v32[e * D + s];
+                } else {
+#pragma unroll
+                    for (int s = 0; s < D; ++s) cj[s] = (T)ct_v[e * D + s];
+                }
 #pragma unroll
                 for (int r = 0; r < D; ++r)
 #pragma unroll
@@ -273,7 +318,7 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
         }
         // 4. b: wall terms + inertia - C p (main.cpp:2318-2333, 2574-2584)
         double cp[3] = {0, 0, 0};
-        for (int a = lane; a < np; a += 32) {
+        for (int a = lane; a < (MIX ? 0 : np); a += 32) {
             const double pk = pvec[nindP[pb + a]];
 #pragma unroll
             for (int r = 0; r < D; ++r) cp[r] += cval[(pb + a) * D + r] * pk;
@@ -285,9 +330,9 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
         if (lane == 0) {
 #pragma unroll
             for (int r = 0; r < D; ++r) {
-                bvec[(size_t)i * D + r] = (sumv[r] + inert * vi[r]) - cp[r];
-                const double dg = acc[self * DD + r * D + r];
-                invDiag[(size_t)i * D + r] = dg != 0.0 ? 1.0 / dg : 0.0;
+                if (!MIX) bvec[(size_t)i * D + r] = (sumv[r] + (double)inert * vi[r]) - cp[r];
+                const T dg = acc[self * DD + r * D + r];
+                invDiag[(size_t)i * D + r] = (double)(dg != T(0) ? T(1) / dg : T(0));
             }
             selfk_out[i] = self;
         }
@@ -296,18 +341,27 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
             const int s = t / DD, rs = t % DD;
             const int k0 = rank_of(woff[s]);
             const int k1 = woff[s + 1] >= mc ? nf : rank_of(woff[s + 1]);
-            double sum = 0.0;
+            T sum = T(0);
             for (int k = k0; k < k1; ++k) sum += acc[k * DD + rs];
-            part[((size_t)i * M.S + wslot[s]) * DD + rs] = sum;
+            part[((size_t)i * M.S + wslot[s]) * DD + rs] = (double)sum;
         }
-        // 6. sliced-ELL write-out
+        // 6. sliced-ELL write-out (the FP32 form writes blocks only when its
+        // inner SpMV uses them)
+        if (MIX && !aval32) {
+            __syncwarp();
+            continue;
+        }
         const long long sb = sptr[i >> 5];
         const int ln = i & 31;
         for (int t = lane; t < nf * DD; t += 32) {
             const int k = t / DD, rs = t - k * DD;
             const long long at = sb * DD + ((long long)k * DD + rs) * 32 + ln;
-            aval[at] = acc[t];
-            if (aval32) aval32[at] = (float)acc[t];
+            if (MIX) {
+                aval32[at] = (float)acc[t];
+            } else {
+                aval[at] = (double)acc[t];
+                if (aval32) aval32[at] = (float)acc[t];
+            }
         }
         for (int k = lane; k < nf; k += 32) acol[sb + (long long)k * 32 + ln] = nind[nb + k];
         __syncwarp();
@@ -327,31 +381,20 @@ static int grow_bytes(void** p, long long* cap, long long need)
     return MPH_OK;
 }
 
-// Builds the transpose of the fluid P-lists and runs the cell-block kernel;
-// returns MPH_OK with *done = false when the case needs k_matrix_a for all
-// rows, and leaves per-cell overflow flags in c->d.cell_flags otherwise.
-int launch_assemble_cells(mph_case* c, int kmax_rows, bool* done)
+// Transpose of the fluid rows' P-lists: for every particle k, the fluid rows
+// j whose P-list holds k, in ascending j, with C_jk.  Built once per step.
+int build_ct(mph_case* c)
 {
-    *done = false;
+    if (c->ct_ready) return MPH_OK;
     const DevParams& P = c->dp;
     const int D = c->dim;
-    const LevelGeom& g0 = c->lv[0];
-    for (int d = 0; d < D; ++d)
-        if (P.cc[d] < 3 || g0.cnt[d] < 3) return MPH_OK;   // walk visits a cell twice: per-row kernel
-    const int kmax = (kmax_rows + 7) & ~7;
-    const int mwords = 64;                                 // up to 2048 candidates per cell
-    const size_t smem = (size_t)kAsmWarps * ((size_t)kmax * D * D * 8 + (size_t)mwords * 8);
-    if (smem > 200 * 1024) return MPH_OK;
     DeviceState& dv = c->d;
     const int N = P.N, Nf = P.Nf;
-    // transpose of the P-lists
     MPH_TRY(grow_bytes((void**)&dv.ct_cnt, &dv.cap_ct_cnt, (long long)2 * (N + 1) * sizeof(int)));
     MPH_TRY(grow_bytes((void**)&dv.ct_ptr, &dv.cap_ct_ptr, (long long)(N + 1) * sizeof(long long)));
-    MPH_TRY(grow_bytes((void**)&dv.cell_flags, &dv.cap_cell_flags, (long long)(P.T + 1) * sizeof(int)));
     long long tot = 0;
     MPH_CUDA(cudaMemcpyAsync(&tot, dv.nptrP + Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     MPH_CUDA(cudaMemsetAsync(dv.ct_cnt, 0, (size_t)2 * (N + 1) * sizeof(int), c->stream));
-    MPH_CUDA(cudaMemsetAsync(dv.cell_flags, 0, (size_t)(P.T + 1) * sizeof(int), c->stream));
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     MPH_TRY(grow_bytes((void**)&dv.ct_j, &dv.cap_ct_j, tot * (long long)sizeof(int)));
     MPH_TRY(grow_bytes((void**)&dv.ct_v, &dv.cap_ct_v, tot * D * (long long)sizeof(double)));
@@ -367,6 +410,33 @@ int launch_assemble_cells(mph_case* c, int kmax_rows, bool* done)
         { k_ct_fill<3><<<gf, 256, 0, c->stream>>>(Nf, dv.ncp, dv.nptrP, dv.nindP, dv.cval, dv.ct_ptr, cur, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
         { k_ct_sort<3><<<grid_for(N, 256), 256, 0, c->stream>>>(N, dv.ct_ptr, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
     }
+    if (c->step_factored) {   // FP32 copy for the FP32 cell-block kernel
+        MPH_TRY(grow_bytes((void**)&dv.ct_v32, &dv.cap_ct_v32, tot * D * (long long)sizeof(float)));
+        { k_to_f32<<<grid_for(tot * D, 256), 256, 0, c->stream>>>(tot * D, dv.ct_v, dv.ct_v32); MPH_COUNT_LAUNCH(); }
+    }
+    c->ct_ready = true;
+    return MPH_OK;
+}
+
+// Runs the cell-block kernel (FP32 form when `mix`); returns MPH_OK with
+// *done = false when the case needs k_matrix_a for all rows, and leaves
+// per-cell overflow flags in c->d.cell_flags otherwise.
+int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done)
+{
+    *done = false;
+    const DevParams& P = c->dp;
+    const int D = c->dim;
+    const LevelGeom& g0 = c->lv[0];
+    for (int d = 0; d < D; ++d)
+        if (P.cc[d] < 3 || g0.cnt[d] < 3) return MPH_OK;   // walk visits a cell twice: per-row kernel
+    const int kmax = (kmax_rows + 7) & ~7;
+    const int mwords = 64;                                 // up to 2048 candidates per cell
+    const size_t smem = (size_t)kAsmWarps * ((size_t)kmax * D * D * (mix ? 4 : 8) + (size_t)mwords * 8);
+    if (smem > 200 * 1024) return MPH_OK;
+    DeviceState& dv = c->d;
+    MPH_TRY(grow_bytes((void**)&dv.cell_flags, &dv.cap_cell_flags, (long long)(P.T + 1) * sizeof(int)));
+    MPH_CUDA(cudaMemsetAsync(dv.cell_flags, 0, (size_t)(P.T + 1) * sizeof(int), c->stream));
+    MPH_TRY(build_ct(c));
     CellMap M{};
     M.S = 1;
     for (int d = 0; d < 3; ++d) {
@@ -377,19 +447,21 @@ int launch_assemble_cells(mph_case* c, int kmax_rows, bool* done)
     }
     int r[3] = {0, 0, 0};
     for (int d = 0; d < D; ++d) r[d] = (int)std::ceil(P.maxR / P.cw[d]);
-    float* a32 = c->precision == MPH_PRECISION_MIXED ? dv.aval32 : nullptr;
+    // FP32 blocks: the mixed form's copy, except when its inner SpMV runs on the
+    // pair terms (factored form without inner_blocks)
+    float* a32 = c->precision == MPH_PRECISION_MIXED && !(mix && !c->inner_blocks) ? dv.aval32 : nullptr;
+    auto go = [&](auto kern) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<P.T, kAsmWarps * 32, smem, c->stream>>>(
+            P, M, r[0], r[1], r[2], mwords, kmax, dv.type, dv.bucket, dv.pos, dv.vel, dv.nc, dv.nfc, dv.nptr, dv.nind, dv.ncp,
+            dv.nptrP, dv.nindP, dv.cval, dv.pvec, dv.ct_ptr, dv.ct_j, dv.ct_v, dv.sptr, dv.acol, dv.aval, a32, dv.bvec,
+            dv.invDiag, dv.selfk, dv.part, dv.cell_flags, dv.pe32, dv.ct_v32, dv.cval32);
+        MPH_COUNT_LAUNCH();
+    };
     if (D == 2) {
-        cudaFuncSetAttribute(k_assemble_cells<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        { k_assemble_cells<2><<<P.T, kAsmWarps * 32, smem, c->stream>>>(
-              P, M, r[0], r[1], r[2], mwords, kmax, dv.type, dv.bucket, dv.pos, dv.vel, dv.nc, dv.nfc, dv.nptr, dv.nind, dv.ncp,
-              dv.nptrP, dv.nindP, dv.cval, dv.pvec, dv.ct_ptr, dv.ct_j, dv.ct_v, dv.sptr, dv.acol, dv.aval, a32, dv.bvec,
-              dv.invDiag, dv.selfk, dv.part, dv.cell_flags); MPH_COUNT_LAUNCH(); }
+        if (mix) go(k_assemble_cells<2, true>); else go(k_assemble_cells<2, false>);
     } else {
-        cudaFuncSetAttribute(k_assemble_cells<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        { k_assemble_cells<3><<<P.T, kAsmWarps * 32, smem, c->stream>>>(
-              P, M, r[0], r[1], r[2], mwords, kmax, dv.type, dv.bucket, dv.pos, dv.vel, dv.nc, dv.nfc, dv.nptr, dv.nind, dv.ncp,
-              dv.nptrP, dv.nindP, dv.cval, dv.pvec, dv.ct_ptr, dv.ct_j, dv.ct_v, dv.sptr, dv.acol, dv.aval, a32, dv.bvec,
-              dv.invDiag, dv.selfk, dv.part, dv.cell_flags); MPH_COUNT_LAUNCH(); }
+        if (mix) go(k_assemble_cells<3, true>); else go(k_assemble_cells<3, false>);
     }
     *done = true;
     return MPH_OK;

@@ -1,0 +1,378 @@
+// k_factored.cu - the FP64 operator of the mixed form, applied in factored
+// form instead of from assembled FP64 blocks.
+//
+// A = inertia + V + C Lambda C^T (calculateMatrixA main.cpp:2251-2335,
+// multiplyMatrixC main.cpp:2574-2642).  Its viscous blocks are rank one:
+// block (i,j) = -f_ij e_ij (x) e_ij for a fluid neighbour j, and the diagonal
+// block adds f_ij e_ij (x) e_ij over every neighbour (fluid and wall), so
+//
+//   (V x)_i = sum_{j fluid} f e (e . (x_i - x_j)) + sum_{j wall} f e (e . x_i).
+//
+// The C Lambda C^T part is C (Lambda (C^T x)): t_k = sum over the fluid rows j
+// whose P-list holds k of C_jk . x_j (the transposed P-lists), then
+// sum_k C_ik lambda_k t_k.  In exact arithmetic this equals the assembled A
+// whenever 2 RadiusP < MaxRadius (every pair with a common P-neighbour is then
+// in the neighbour list, where the reference adds the product); the engine
+// uses this form only then.
+//
+// k_pair_terms stores (e, f) per neighbour slot of every fluid row in FP64
+// (the outer residual b - A x) and in FP32 (the inner FP32 blocks), and b in
+// FP64.  FP64 work per slot: the separation, its norm, one rsqrt and a few
+// products, against the nine-entry block and its accumulation of the
+// assembled form.
+#include "mph_device.cuh"
+#include "mph_solver.cuh"
+
+namespace mph {
+
+constexpr int kPairWarps = 8;
+
+// (e, f) of every neighbour slot of the fluid rows, and b
+// (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).
+template <int D>
+__global__ void __launch_bounds__(kPairWarps * 32)
+k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const double* __restrict__ vel,
+             const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
+             const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
+             const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
+             double4* __restrict__ pe, float4* __restrict__ pe32, double* __restrict__ bvec)
+{
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const double rV2 = P.rV * P.rV;
+    for (int i = wid; i < P.Nf; i += nwarps) {
+        const int ti = type[i];
+        const long long nb = nptr[i];
+        const int n = nc[i], nf = nfc[i];
+        double xi[3], vi[3];
+        load_vec<D>(pos, i, xi);
+        load_vec<D>(vel, i, vi);
+        double sumv[3] = {0.0, 0.0, 0.0};
+        for (int k = lane; k < n; k += 32) {
+            const int j = nind[nb + k];
+            double e[3] = {0.0, 0.0, 0.0};
+            double f = 0.0;
+            if (j != i) {
+                double xj[3], q[3];
+                load_vec<D>(pos, j, xj);
+                sep_vec<D>(P, xj, xi, q);
+                const double r2 = norm2_exact<D>(q);
+                if (r2 != 0.0 && rV2 - r2 > 0) {
+                    const double inv = rsqrt(r2);
+                    const double wd = -P.kfv * (P.m2h_rv * (1.0 - (r2 * inv) * P.inv_rv));
+                    f = P.visc * P.muij[ti][type[j]] * wd * inv;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) e[d] = q[d] * inv;
+                    if (k >= nf) {   // wall neighbour: its velocity enters b
+                        double vj[3];
+                        load_vec<D>(vel, j, vj);
+                        double ev = 0.0;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) ev += e[d] * vj[d];
+#pragma unroll
+                        for (int r = 0; r < D; ++r) sumv[r] += f * e[r] * ev;
+                    }
+                }
+            }
+            pe[nb + k] = make_double4(e[0], e[1], e[2], f);
+            pe32[nb + k] = make_float4((float)e[0], (float)e[1], (float)e[2], (float)f);
+        }
+        // - C p over the row's P-neighbours
+        const long long pb = nptrP[i];
+        const int np = ncp[i];
+        for (int a = lane; a < np; a += 32) {
+            const double pk = pvec[nindP[pb + a]];
+#pragma unroll
+            for (int r = 0; r < D; ++r) sumv[r] -= cval[(pb + a) * D + r] * pk;
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
+        if (lane == 0) {
+            const double inert = P.density[ti] * P.vol / P.vol / P.dt;   // as the assembly
+#pragma unroll
+            for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
+        }
+    }
+}
+
+__global__ void k_cval_f32(long long n, const double* __restrict__ a, float* __restrict__ b)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) b[k] = (float)a[k];
+}
+
+// t_k = sum over the transposed P-list of k of C_jk . x_j (every particle k)
+template <int D>
+__global__ void k_ct_apply(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
+                           const double* __restrict__ ct_v, const double* __restrict__ x, double* __restrict__ t)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double s = 0.0;
+    const long long e1 = ctptr[k + 1];
+    for (long long e = ctptr[k]; e < e1; ++e) {
+        const int j = ct_j[e];
+#pragma unroll
+        for (int d = 0; d < D; ++d) s += ct_v[e * D + d] * x[(size_t)j * D + d];
+    }
+    t[k] = s;
+}
+
+// r = b - A x in factored form, (r, r) -> *out (deterministic reduction).
+template <int D>
+__global__ void __launch_bounds__(kPairWarps * 32)
+k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restrict__ nc, const int* __restrict__ nfc,
+                 const long long* __restrict__ nptr, const int* __restrict__ nind, const double4* __restrict__ pe,
+                 const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
+                 const double* __restrict__ cval, const double* __restrict__ t, const double* __restrict__ x,
+                 const double* __restrict__ b, double* __restrict__ r, double* __restrict__ partials,
+                 unsigned* __restrict__ counter, double* __restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double acc_rr = 0.0;
+    for (int i = wid; i < P.Nf; i += nwarps) {
+        double xi[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
+        double y[3] = {0.0, 0.0, 0.0};
+        const long long nb = nptr[i];
+        const int n = nc[i], nf = nfc[i];
+        for (int k = lane; k < n; k += 32) {
+            const double4 p = pe[nb + k];
+            const double e[3] = {p.x, p.y, p.z};
+            double dx[3] = {xi[0], xi[1], xi[2]};
+            if (k < nf) {
+                const int j = nind[nb + k];
+#pragma unroll
+                for (int d = 0; d < D; ++d) dx[d] -= x[(size_t)j * D + d];
+            }
+            double ed = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) ed += e[d] * dx[d];
+            const double s = p.w * ed;
+#pragma unroll
+            for (int d = 0; d < D; ++d) y[d] += s * e[d];
+        }
+        const long long pb = nptrP[i];
+        const int np = ncp[i];
+        for (int a = lane; a < np; a += 32) {
+            const int k = nindP[pb + a];
+            const double lt = P.lambda[type[k]] * t[k];
+#pragma unroll
+            for (int d = 0; d < D; ++d) y[d] += cval[(pb + a) * D + d] * lt;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) y[d] += __shfl_xor_sync(0xffffffffu, y[d], o);
+        if (lane == 0) {
+            const double inert = P.density[type[i]] * P.vol / P.vol / P.dt;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const double rv = b[(size_t)i * D + d] - (inert * xi[d] + y[d]);
+                r[(size_t)i * D + d] = rv;
+                acc_rr += rv * rv;
+            }
+        }
+    }
+    reduce_finalize(acc_rr, partials, counter, out);
+}
+
+// ---- FP32 inner operator of the mixed form, without assembled blocks --------------
+// The inner CR's y = A32 s from the FP32 pair terms: t = C^T s per particle
+// (k_ct_apply32, which also runs the iteration's convergence test), then per
+// fluid row inertia + viscous pair terms + C Lambda t, and (s, y) into the
+// iteration's rho slot (k_apply32).  Same recurrences and flags as k_spmv32.
+constexpr int kSIn0 = 16, kSIn = 17;
+__device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
+
+template <int D>
+__global__ void k_ct_apply32(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
+                             const float* __restrict__ ct_v32, const float* __restrict__ x, float* __restrict__ t,
+                             const double* __restrict__ scal, int* __restrict__ flags, int cap, double tol2)
+{
+    if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
+    const double rr0 = scal[kSIn0];
+    const double rr = it == 0 ? rr0 : scal[kSIn];
+    const bool bad = !(rr == rr);
+    if (it >= cap || rr / rr0 < tol2 || bad) {
+        __syncthreads();
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            flags[kFlagDone] = 1;
+            if (bad) flags[kFlagBad] = 1;
+        }
+        return;
+    }
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    float s = 0.f;
+    const long long e1 = ctptr[k + 1];
+    for (long long e = ctptr[k]; e < e1; ++e) {
+        const int j = ct_j[e];
+#pragma unroll
+        for (int d = 0; d < D; ++d) s += ct_v32[e * D + d] * x[(size_t)j * D + d];
+    }
+    t[k] = s;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kPairWarps * 32)
+k_apply32(DevParams P, const int* __restrict__ type, const int* __restrict__ nc, const int* __restrict__ nfc,
+          const long long* __restrict__ nptr, const int* __restrict__ nind, const float4* __restrict__ pe32,
+          const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
+          const float* __restrict__ cval32, const float* __restrict__ t, const float* __restrict__ x,
+          float* __restrict__ y, double* __restrict__ scal, const int* __restrict__ flags,
+          double* __restrict__ partials, unsigned* __restrict__ counter)
+{
+    if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double acc = 0.0;
+    for (int i = wid; i < P.Nf; i += nwarps) {
+        float xi[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
+        float yv[3] = {0.f, 0.f, 0.f};
+        const long long nb = nptr[i];
+        const int n = nc[i], nf = nfc[i];
+        for (int k = lane; k < n; k += 32) {
+            const float4 p = pe32[nb + k];
+            const float e[3] = {p.x, p.y, p.z};
+            float dx[3] = {xi[0], xi[1], xi[2]};
+            if (k < nf) {
+                const int j = nind[nb + k];
+#pragma unroll
+                for (int d = 0; d < D; ++d) dx[d] -= x[(size_t)j * D + d];
+            }
+            float ed = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) ed += e[d] * dx[d];
+            const float sc = p.w * ed;
+#pragma unroll
+            for (int d = 0; d < D; ++d) yv[d] += sc * e[d];
+        }
+        const long long pb = nptrP[i];
+        const int np = ncp[i];
+        for (int a = lane; a < np; a += 32) {
+            const int k = nindP[pb + a];
+            const float lt = (float)P.lambda[type[k]] * t[k];
+#pragma unroll
+            for (int d = 0; d < D; ++d) yv[d] += cval32[(pb + a) * D + d] * lt;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) yv[d] += __shfl_xor_sync(0xffffffffu, yv[d], o);
+        if (lane == 0) {
+            const float inert = (float)(P.density[type[i]] * P.vol / P.vol / P.dt);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const float v = inert * xi[d] + yv[d];
+                y[(size_t)i * D + d] = v;
+                acc += (double)xi[d] * (double)v;
+            }
+        }
+    }
+    reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
+}
+
+void launch_apply32(mph_case* c, const float* x, float* y, int cap, double tol2)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
+    const unsigned gt = grid_for(P.N, 256);
+    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
+    if (c->dim == 2) {
+        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap, tol2); MPH_COUNT_LAUNCH(); }
+        { k_apply32<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
+                                                            d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap, tol2); MPH_COUNT_LAUNCH(); }
+        { k_apply32<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
+                                                            d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+    }
+}
+
+// ---- host side ---------------------------------------------------------------------
+static int grow_pairs(mph_case* c, long long slots)
+{
+    DeviceState& d = c->d;
+    if (slots <= d.cap_pairs) return MPH_OK;
+    if (d.pe) cudaFree(d.pe);
+    if (d.pe32) cudaFree(d.pe32);
+    d.pe = nullptr;
+    d.pe32 = nullptr;
+    d.cap_pairs = 0;
+    const long long n = slots + slots / 8 + 1024;
+    MPH_CUDA(cudaMalloc((void**)&d.pe, (size_t)n * sizeof(double4)));
+    MPH_CUDA(cudaMalloc((void**)&d.pe32, (size_t)n * sizeof(float4)));
+    d.cap_pairs = n;
+    return MPH_OK;
+}
+
+bool factored_applies(const mph_case* c)
+{
+    return c->precision == MPH_PRECISION_MIXED && c->factored && 2.0 * c->dp.rP < c->dp.maxR;
+}
+
+int launch_pair_terms(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    long long slots = 0;
+    MPH_CUDA(cudaMemcpyAsync(&slots, d.nptr + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    MPH_TRY(grow_pairs(c, slots));
+    if (!d.tct) MPH_CUDA(cudaMalloc((void**)&d.tct, (size_t)(P.N + 1) * sizeof(double)));
+    if (!d.tct32) MPH_CUDA(cudaMalloc((void**)&d.tct32, (size_t)(P.N + 1) * sizeof(float)));
+    long long ncv = 0;   // C values of the fluid rows, FP32 copy for the inner operator
+    MPH_CUDA(cudaMemcpyAsync(&ncv, d.nptrP + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    ncv *= c->dim;
+    if (ncv > d.cap_cval32) {
+        if (d.cval32) cudaFree(d.cval32);
+        d.cval32 = nullptr;
+        d.cap_cval32 = 0;
+        MPH_CUDA(cudaMalloc((void**)&d.cval32, (size_t)(ncv + ncv / 8 + 1024) * sizeof(float)));
+        d.cap_cval32 = ncv + ncv / 8 + 1024;
+    }
+    { k_cval_f32<<<grid_for(ncv, 256), 256, 0, c->stream>>>(ncv, d.cval, d.cval32); MPH_COUNT_LAUNCH(); }
+    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
+    if (c->dim == 2) {
+        { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval, d.pvec, d.pe, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval, d.pvec, d.pe, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+    }
+    return MPH_OK;
+}
+
+void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
+    const unsigned gt = grid_for(P.N, 256);
+    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
+    if (c->dim == 2) {
+        { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+        { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe, d.ncp, d.nptrP, d.nindP,
+                                                                   d.cval, d.tct, x, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+        { k_resid_factored<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe, d.ncp, d.nptrP, d.nindP,
+                                                                   d.cval, d.tct, x, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+    }
+}
+
+}  // namespace mph

@@ -273,7 +273,16 @@ static int mixed_solve_t(mph_case* c)
     float* u32 = d.v32 + 6 * (size_t)n;
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
     { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
-    { k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+    // FP64 residual: from the assembled FP64 blocks, or in factored form
+    auto residual = [&]() {
+        if (c->step_factored) {
+            launch_resid_factored(c, d.x, d.r, scal + kSRR);
+        } else {
+            k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR);
+            MPH_COUNT_LAUNCH();
+        }
+    };
+    residual();
     const double tol_out2 = c->tol_outer * c->tol_outer;
     const double tol_in2 = c->tol_inner * c->tol_inner;
     const int cap = n;
@@ -286,8 +295,13 @@ static int mixed_solve_t(mph_case* c)
     // as a graph.  Iterations after convergence return at once.
     auto iteration = [&, c](cudaEvent_t* e) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
-        { k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
-                                             counter); MPH_COUNT_LAUNCH(); }
+        if (c->step_factored && !c->inner_blocks) {
+            launch_apply32(c, s32, y32, cap, tol_in2);   // FP32 pair terms, no assembled blocks
+        } else {
+            k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
+                                               counter);
+            MPH_COUNT_LAUNCH();
+        }
         if (e) prof_begin(c, 0, &e[1]);
         { k_pq32<<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
         vcycle_mixed(c, q32, u32, scal + kSQU32);
@@ -344,7 +358,7 @@ static int mixed_solve_t(mph_case* c)
         if (host_flags[kFlagBad]) { bad = true; break; }
         total_inner += inner;
         { k_refine<<<rb, kReduceThreads, 0, st>>>(n, d.x, z32, scal); MPH_COUNT_LAUNCH(); }
-        { k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+        residual();
     }
     { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
     MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));

@@ -137,6 +137,9 @@ int residual_noalloc(mph_case* c, double* out)
         return fail(MPH_ERR_CAPACITY, "allocation-free residual: " + std::to_string(Nf) + " fluid particles exceed its limit of " +
                                           std::to_string((long long)kNoAllocMaxBlocks * kNoAllocRows));
     if (c->stage != 7) return fail(MPH_ERR_STATE, "allocation-free residual: call it after mph_stage_solve, before the step ends");
+    if (c->step_factored)
+        return fail(MPH_ERR_STATE, "allocation-free residual: this step has no FP64 blocks (mixed form with the factored "
+                                   "operator; set option \"factored\" to 0)");
     int prev = 0;
     MPH_CUDA(cudaGetDevice(&prev));
     if (prev != c->device) MPH_CUDA(cudaSetDevice(c->device));

@@ -54,23 +54,27 @@ int mph_step(mph_case* c, int nsteps)
     GUARD(mph::case_step(c, nsteps))
 }
 
-int mph_batch_step(mph_case** cases, int ncases, int nsteps)
+int mph_batch_step(mph_case** cases, int ncases, int nsteps) { GUARD(mph::batch_step(cases, ncases, nsteps, 0)) }
+int mph_batch_step_workers(mph_case** cases, int ncases, int nsteps, int workers)
 {
-    if (!cases || ncases < 0) return mph::fail(MPH_ERR_ARG, "bad case list");
-    try {
-        int last = MPH_OK;
-        for (int s = 0; s < nsteps; ++s)
-            for (int k = 0; k < ncases; ++k) {
-                NEED(cases[k]);
-                const int st = mph::case_step(cases[k], 1);
-                if (st != MPH_OK && st != MPH_ERR_NOT_CONVERGED) return st;
-                if (st != MPH_OK) last = st;
-            }
-        return last;
-    } catch (...) {
-        return mph::fail(MPH_ERR_STATE, "exception in batch step");
-    }
+    GUARD(mph::batch_step(cases, ncases, nsteps, workers))
 }
+int mph_case_footprint(const mph_params* prm, const mph_particles* parts, int dim, int precision, long long* bytes)
+{
+    GUARD(mph::case_footprint(prm, parts, dim, precision, bytes))
+}
+int mph_server_create(long long budget_bytes, int workers, mph_server** out) { GUARD(mph::server_create(budget_bytes, workers, out)) }
+int mph_server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision, int steps,
+                      const mph_fields* out, float* step_ms, long long* ticket)
+{
+    GUARD(mph::server_submit(s, prm, parts, dim, precision, steps, out, step_ms, ticket))
+}
+int mph_server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count)
+{
+    GUARD(mph::server_poll(s, out, max, wait_ms, count))
+}
+int mph_server_stats_get(mph_server* s, mph_server_stats* out) { GUARD(mph::server_stats(s, out)) }
+int mph_server_destroy(mph_server* s) { GUARD(mph::server_destroy(s)) }
 
 int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel_residual, int max_outer)
 {
@@ -95,6 +99,14 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
     }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
+        return MPH_OK;
+    }
+    if (std::string(name) == "factored") {
+        c->factored = value != 0.0;
+        return MPH_OK;
+    }
+    if (std::string(name) == "inner_blocks") {
+        c->inner_blocks = value != 0.0;
         return MPH_OK;
     }
     return mph::fail(MPH_ERR_ARG, std::string("unknown option: ") + name);

@@ -167,6 +167,10 @@ static int derive(mph_case* c, const mph_particles* parts)
     for (int t = 0; t < kTypeCount; ++t)
         for (int u = 0; u < kTypeCount; ++u)
             P.muij[t][u] = 2.0 * (P.mu[t] * P.mu[u]) / (P.mu[t] + P.mu[u]);
+    for (int t = 0; t < kTypeCount; ++t) {
+        P.inert32[t] = (float)(P.density[t] * P.vol / P.vol / P.dt);
+        P.lambda32[t] = (float)P.lambda[t];
+    }
     // walls (initializeWall main.cpp:1023-1062; theta = |omega|^2 as written there)
     for (int t = 0; t < 4; ++t)
         for (int d = 0; d < 3; ++d) {
@@ -598,13 +602,14 @@ int case_destroy(mph_case* c)
     if (c->cr_exec) cudaGraphExecDestroy(c->cr_exec);
     if (c->mx_exec) cudaGraphExecDestroy(c->mx_exec);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
     for (void* p : c->allocations) cudaFree(p);
     DeviceState& d = c->d;
     for (void* p : {(void*)d.nind, (void*)d.nindP, (void*)d.acol, (void*)d.aval, (void*)d.aval32, (void*)d.cval,
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags,
-                    (void*)d.mg_invd32, d.scan_tmp})
+                    (void*)d.mg_invd32, (void*)d.pe, (void*)d.pe32, (void*)d.tct, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

@@ -108,6 +108,9 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
         }
         return MPH_OK;
     }
+    if ((name == "CsrIndA" || name == "CsrCofA") && c->step_factored && !c->inner_blocks)
+        return fail(MPH_ERR_STATE, name + ": this step assembled no blocks (mixed form, factored operator; "
+                                          "set option \"inner_blocks\" to 1 to keep FP32 blocks)");
     if (name == "CsrPtrA" || name == "CsrIndA" || name == "CsrCofA") {
         // sliced ELL -> CSR with rows D*i+r and entries (k, s), as the reference
         std::vector<int> nfc, acol;
@@ -116,7 +119,14 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
         MPH_TRY(d2h(c, nfc, d.nfc, Nf));
         MPH_TRY(d2h(c, sptr, d.sptr, (size_t)c->nslices + 1));
         MPH_TRY(d2h(c, acol, d.acol, (size_t)c->nslots));
-        if (name == "CsrCofA") MPH_TRY(d2h(c, aval, d.aval, (size_t)c->nslots * D * D));
+        if (name == "CsrCofA" && c->step_factored) {
+            // mixed form with the factored FP64 operator: only FP32 blocks exist
+            std::vector<float> a32;
+            MPH_TRY(d2h(c, a32, d.aval32, (size_t)c->nslots * D * D));
+            aval.assign(a32.begin(), a32.end());
+        } else if (name == "CsrCofA") {
+            MPH_TRY(d2h(c, aval, d.aval, (size_t)c->nslots * D * D));
+        }
         long long nnz = 0;
         for (int i = 0; i < Nf; ++i) nnz += (long long)D * D * nfc[i];
         if (name == "CsrPtrA") {

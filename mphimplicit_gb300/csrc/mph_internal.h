@@ -55,6 +55,8 @@ struct DevParams {
     double muij[kTypeCount][kTypeCount];       // harmonic mean 2 mu_i mu_j / (mu_i + mu_j)
     float maxR2_lo, maxR2_hi, rP2_lo, rP2_hi;  // FP32 pre-classification band
     float w32[3], hw32[3];
+    float inert32[kTypeCount];                 // FP32 density/dt and bulk viscosity (mixed-form kernels)
+    float lambda32[kTypeCount];
     int exact_only;                            // 1: skip the FP32 pre-classification
     int surface;                               // 1 if any CofA != 0
 };
@@ -105,6 +107,17 @@ struct DeviceState {
     int* cell_flags = nullptr;
     int* dmax = nullptr;
     long long cap_ct_cnt = 0, cap_ct_ptr = 0, cap_ct_j = 0, cap_ct_v = 0, cap_cell_flags = 0;
+    // mixed form, factored FP64 operator: (e, f) per neighbour slot of the
+    // fluid rows in FP64 and FP32, and t = C^T x per particle
+    double4* pe = nullptr;
+    float4* pe32 = nullptr;
+    long long cap_pairs = 0;
+    double* tct = nullptr;
+    float* ct_v32 = nullptr;        // FP32 copy of ct_v
+    long long cap_ct_v32 = 0;
+    float* cval32 = nullptr;        // FP32 copy of the fluid rows' C values
+    long long cap_cval32 = 0;
+    float* tct32 = nullptr;         // t = C^T x of the FP32 inner operator
     // multigrid
     double *mg_cof = nullptr, *mg_invd = nullptr;
     double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr, *mg_res = nullptr;   // Q, S ping-pong pair, residual
@@ -174,10 +187,15 @@ struct mph_case {
     double tol_inner = 1.0e-3;          // mixed form: inner relative reduction
     int max_outer = 50;                 // mixed form: refinement steps
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
+    bool factored = true;               // mixed form: FP64 operator in factored form where it applies
+    bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
+    bool step_factored = false;         // this step's system uses the factored form
+    bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
     cudaGraphExec_t cr_exec = nullptr;  // FP64 CR chunk
     cudaGraphExec_t mx_exec = nullptr;  // mixed form: FP32 inner CR chunk
     cudaStream_t cap_stream = nullptr;  // side stream the chunks are captured on
+    cudaStream_t own_stream = nullptr;  // private stream for batched steps of a legacy-stream case
     mph::DeviceState d;
     std::vector<void*> allocations;
     mph::Profile prof;
@@ -212,6 +230,15 @@ const char* scalar_names();
 int case_get_fields(mph_case* c, mph_fields* out);
 int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_center);
 int case_profile(mph_case* c, int enable);
+// batching and serving (mph_batch.cpp)
+int batch_step(mph_case** cases, int ncases, int nsteps, int workers);
+int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, int precision, long long* bytes);
+int server_create(long long budget, int workers, mph_server** out);
+int server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision, int steps,
+                  const mph_fields* out, float* step_ms, long long* ticket);
+int server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count);
+int server_stats(mph_server* s, mph_server_stats* out);
+int server_destroy(mph_server* s);
 int case_profile_read(mph_case* c, double* out, int n);
 
 // profiling helpers (mph_case.cu): bracket a launch sequence of kernel class k
@@ -246,7 +273,12 @@ void launch_density_full(mph_case* c);
 void ensure_density_a(mph_case* c);
 void launch_output_fields(mph_case* c);
 int launch_assemble(mph_case* c);
-int launch_assemble_cells(mph_case* c, int kmax_rows, bool* done);
+int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done);
+int build_ct(mph_case* c);
+bool factored_applies(const mph_case* c);
+int launch_pair_terms(mph_case* c);
+void launch_resid_factored(mph_case* c, const double* x, double* r, double* out);
+void launch_apply32(mph_case* c, const float* x, float* y, int cap, double tol2);
 void launch_mg_level0(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);

@@ -124,3 +124,34 @@ def test_case_validation_without_gpu(lib):
     with pytest.raises(engine.MphError) as e:
         engine.Case(p, parts, 4)
     assert e.value.status == 1
+
+
+def test_footprint_bound_scales_with_case(lib):
+    from mphimplicit_gb300 import serving
+    from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
+    p1, s1 = casegen.square_drop_2d(scale=0.1, seed=0)
+    p2, s2 = casegen.square_drop_2d(scale=0.3, seed=0)
+    a = serving.footprint(p1, s1, 2, PRECISION_FP64)
+    b = serving.footprint(p2, s2, 2, PRECISION_FP64)
+    m = serving.footprint(p2, s2, 2, PRECISION_MIXED)
+    assert 0 < a < b < m
+    s3 = casegen.dam_case(3, (12, 12, 12), (16, 16, 16), 0.005, seed=0)
+    p3 = casegen.baseline_params(3, 0.005, 5.0e-5)
+    c = serving.footprint(p3, s3, 3, PRECISION_FP64)
+    # beyond the fixed 64 MiB, a 3D fluid particle (its matrix row) costs
+    # several times a 2D one
+    fixed = 64 << 20
+    assert (c - fixed) / (s3.types < 2).sum() > 3 * (b - fixed) / (s2.types < 2).sum()
+
+
+def test_server_rejects_requests_beyond_budget(lib):
+    from mphimplicit_gb300 import serving
+    p, s = casegen.square_drop_2d(scale=0.1, seed=0)
+    srv = serving.Server(budget_bytes=1 << 20, workers=1)
+    with pytest.raises(engine.MphError) as e:
+        srv.submit(p, s, 2, steps=1)
+    assert e.value.status == 6
+    with pytest.raises(engine.MphError):
+        srv.submit(p, s, 2, steps=0)
+    assert srv.stats()["pending"] == 0
+    srv.close()

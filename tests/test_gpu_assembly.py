@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from mphimplicit_gb300 import casegen, engine
+from mphimplicit_gb300.cabi import PRECISION_MIXED
 from parity_util import csr_blocks_oracle, mg_proj, rel, vec_proj
 
 pytestmark = pytest.mark.gpu
@@ -72,3 +73,46 @@ def test_cell_assembly_matches_oracle(engine_lib, oracle_built, case):
     vo = vec_proj(o.array("Velocity"), dim)[:nf]
     vg = vec_proj(g.export("Velocity"), dim)[:nf]
     assert np.linalg.norm(vg - vo) / np.linalg.norm(vo) <= 2e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_fp32_cell_assembly_of_the_factored_form(engine_lib, case):
+    """Mixed form with the factored FP64 operator: the FP32 cell-block kernel
+    (blocks from the FP32 pair terms) against the FP64 cell-block kernel, and
+    one full mixed solve against the FP64 form's velocity."""
+    name, dim, params, parts = case
+    a = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    a.set_option("inner_blocks", 1)   # keep the FP32 blocks to compare them
+    b = _assembled(params, parts, dim, True)
+    for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
+        a.stage(st)
+    assert np.array_equal(a.export("CsrIndA"), b.export("CsrIndA"))
+    assert rel(a.export("CsrCofA"), b.export("CsrCofA")) <= 1e-6
+    assert rel(a.export("VectorB"), b.export("VectorB")) <= 1e-12
+    assert rel(a.export("InvDiagA"), b.export("InvDiagA")) <= 1e-6
+    for L in range(int(a.scalars()["MultiGridDepth"])):
+        assert rel(a.export(f"MultiGridCsrCofA:{L}"), b.export(f"MultiGridCsrCofA:{L}")) <= 1e-6, L
+    a.stage("solve")
+    b.stage("solve")
+    assert a.solve_stats()["status"] == 0
+    nf = a.fluid_count
+    va = vec_proj(a.export("Velocity"), dim)[:nf]
+    vb = vec_proj(b.export("Velocity"), dim)[:nf]
+    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 2e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_pair_term_inner_operator_solves(engine_lib, case):
+    """The mixed form with its inner SpMV on the FP32 pair terms (no blocks)
+    reaches the FP64 form's velocity."""
+    name, dim, params, parts = case
+    a = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    a.set_option("inner_blocks", 0)
+    b = engine.Case(params, parts, dim)
+    a.step(1)
+    b.step(1)
+    assert a.solve_stats()["status"] == 0
+    nf = a.fluid_count
+    va = vec_proj(a.export("Velocity"), dim)[:nf]
+    vb = vec_proj(b.export("Velocity"), dim)[:nf]
+    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 2e-5

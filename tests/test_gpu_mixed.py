@@ -5,7 +5,9 @@ Everything before the solve is the FP64 form's code, so only the solve is
 checked here: with the reference's tolerance the velocity must solve the
 oracle's FP64 system to ||b - A x|| / ||b|| < 1e-6 and stay within the same
 band of the oracle as the FP64 form; with a tightened tolerance (1e-10) the
-FP64 residual the engine reports must reach it."""
+FP64 residual the engine reports must reach it.  Both FP64 operators of the
+mixed form are covered: the factored one (pair terms + transposed P-lists,
+the default where 2 RadiusP < MaxRadius) and the assembled FP64 blocks."""
 import numpy as np
 import pytest
 
@@ -25,12 +27,20 @@ def oracle_residual(ptr, ind, val, b, x):
     return float(np.linalg.norm(b - ax) / np.linalg.norm(b))
 
 
+# (factored FP64 operator, inner SpMV on assembled FP32 blocks)
+MODES = [(1, 0), (1, 1), (0, 0)]
+MODE_IDS = ["factored", "factored-blocks", "assembled"]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("case", CASES, ids=IDS)
-def test_mixed_solve_meets_reference_tolerance(engine_lib, oracle_built, case):
+def test_mixed_solve_meets_reference_tolerance(engine_lib, oracle_built, case, mode):
     name, dim, params, parts = case
     o = oracle_built.Oracle(params, parts, dim, threads=1)
     o.init()
     g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_option("factored", mode[0])
+    g.set_option("inner_blocks", mode[1])
     for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
         g.stage(st)
     o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build()
@@ -48,10 +58,13 @@ def test_mixed_solve_meets_reference_tolerance(engine_lib, oracle_built, case):
     assert err <= 2e-5, err
 
 
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("case", CASES[:1] + CASES[2:3], ids=[IDS[0], IDS[2]])
-def test_mixed_tight_tolerance(engine_lib, oracle_built, case):
+def test_mixed_tight_tolerance(engine_lib, oracle_built, case, mode):
     name, dim, params, parts = case
     g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_option("factored", mode[0])
+    g.set_option("inner_blocks", mode[1])
     g.set_solver(1e-10, 1e-3, 50)
     g.step(2)
     s = g.solve_stats()
@@ -65,3 +78,36 @@ def test_mixed_tight_tolerance(engine_lib, oracle_built, case):
     vf = vec_proj(f.export("Velocity"), dim)[:nf]
     assert np.array_equal(g.export("ParticleIndex"), f.export("ParticleIndex"))
     assert np.linalg.norm(vg - vf) / np.linalg.norm(vf) <= 5e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_factored_terms_match_assembled(engine_lib, case):
+    """b from the pair-term kernel equals the assembled b to rounding, and the
+    FP32 blocks built from the FP32 pair terms equal the FP64 blocks to FP32
+    rounding."""
+    name, dim, params, parts = case
+    out = {}
+    for fac in (1, 0):
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_option("factored", fac)
+        g.set_option("inner_blocks", 1)
+        for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble"):
+            g.stage(st)
+        out[fac] = (g.export("VectorB"), g.export("CsrCofA"), g.export("InvDiagA"))
+    b1, a1, d1 = out[1]
+    b0, a0, d0 = out[0]
+    assert np.linalg.norm(b1 - b0) <= 1e-12 * np.linalg.norm(b0)
+    assert np.linalg.norm(a1 - a0) <= 1e-6 * np.linalg.norm(a0)
+    assert np.linalg.norm(d1 - d0) <= 1e-6 * np.linalg.norm(d0)
+
+
+def test_factored_form_without_blocks_refuses_block_export(engine_lib):
+    name, dim, params, parts = CASES[0]
+    g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_option("inner_blocks", 0)
+    for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble"):
+        g.stage(st)
+    with pytest.raises(engine.MphError) as e:
+        g.export("CsrCofA")
+    assert e.value.status == 9
+    assert len(g.export("VectorB")) == g.fluid_count * dim

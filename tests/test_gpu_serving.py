@@ -1,0 +1,100 @@
+"""Batched stepping and the serving loop.
+
+Each case's arithmetic is independent of the others (own buffers, own
+stream, deterministic reductions), so a case stepped in a batch or served in
+a mix of cases must give the same bits as the same case stepped alone: the
+stated tolerance of these tests is exact equality."""
+import numpy as np
+import pytest
+
+from mphimplicit_gb300 import casegen, engine, serving
+from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
+from parity_util import small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+
+
+def _alone(params, parts, dim, precision, steps):
+    g = engine.Case(params, parts, dim, precision=precision)
+    g.step(steps)
+    f = g.fields(("id", "pos", "vel"))
+    g.close()
+    return f
+
+
+def _mix():
+    """Small cases of both dimensions and precisions, uneven sizes."""
+    out = []
+    for k, (name, dim, params, parts) in enumerate(CASES):
+        out.append((f"{name}-fp64", dim, params, parts, PRECISION_FP64, 2 + k % 2))
+        out.append((f"{name}-mixed", dim, params, parts, PRECISION_MIXED, 3 - k % 2))
+    p, parts = casegen.square_drop_2d(scale=0.2, seed=5)
+    out.append(("dam2d_20-mixed", 2, p, parts, PRECISION_MIXED, 2))
+    return out
+
+
+def test_batch_step_matches_alone(engine_lib):
+    mix = _mix()
+    cases = [engine.Case(params, parts, dim, precision=prec) for _, dim, params, parts, prec, _ in mix]
+    assert serving.batch_step(cases, 2) in (0, 7)
+    for (name, dim, params, parts, prec, _), g in zip(mix, cases):
+        ref = _alone(params, parts, dim, prec, 2)
+        got = g.fields(("id", "pos", "vel"))
+        for k in ("id", "pos", "vel"):
+            assert np.array_equal(got[k], ref[k]), (name, k)
+        g.close()
+
+
+def test_batch_rejects_duplicates(engine_lib):
+    name, dim, params, parts = CASES[0]
+    g = engine.Case(params, parts, dim)
+    with pytest.raises(engine.MphError):
+        serving.batch_step([g, g], 1)
+    g.close()
+
+
+def test_server_results_equal_alone_and_admission_by_footprint(engine_lib):
+    mix = _mix()
+    fps = [serving.footprint(params, parts, dim, prec) for _, dim, params, parts, prec, _ in mix]
+    budget = sorted(fps)[-1] + sorted(fps)[-2]          # at most about two cases resident at once
+    srv = serving.Server(budget, workers=4)
+    tickets = {}
+    for (name, dim, params, parts, prec, steps) in mix:
+        tickets[srv.submit(params, parts, dim, steps, precision=prec)] = (name, dim, params, parts, prec, steps)
+    results = []
+    for _ in range(600):
+        results += srv.poll(wait_ms=200)
+        if len(results) == len(mix):
+            break
+    st = srv.stats()
+    srv.close()
+    assert len(results) == len(mix)
+    assert st["used_bytes"] == 0 and st["pending"] == 0
+    assert st["steps"] == sum(m[5] for m in mix)
+    by_ticket = sorted(results, key=lambda r: r["ticket"])
+    admits = [r["admit_s"] for r in by_ticket]
+    assert admits == sorted(admits)                     # admitted in arrival order
+    for r in results:
+        name, dim, params, parts, prec, steps = tickets[r["ticket"]]
+        assert r["status"] in (0, 7), (name, r["error"])
+        assert r["steps"] == steps and len(r["step_ms"]) == steps and (r["step_ms"] > 0).all()
+        assert r["submit_s"] <= r["admit_s"] <= r["done_s"]
+        ref = _alone(params, parts, dim, prec, steps)
+        for k in ("id", "pos", "vel"):
+            assert np.array_equal(r["fields"][k], ref[k]), (name, k)
+
+
+def test_footprint_bounds_device_memory(engine_lib):
+    torch = pytest.importorskip("torch")
+    torch.cuda.init()
+    p, parts = casegen.square_drop_2d(scale=0.5, seed=3)
+    for prec in (PRECISION_FP64, PRECISION_MIXED):
+        fp = serving.footprint(p, parts, 2, prec)
+        free0, _ = torch.cuda.mem_get_info()
+        g = engine.Case(p, parts, 2, precision=prec)
+        g.step(2)
+        free1, _ = torch.cuda.mem_get_info()
+        g.close()
+        assert free0 - free1 <= fp, (prec, free0 - free1, fp)

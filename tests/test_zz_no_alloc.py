@@ -37,8 +37,9 @@ def _noalloc(case):
     return st, (out[0], out[1])
 
 
-def _solved(params, parts, dim, precision):
+def _solved(params, parts, dim, precision, factored=0):
     g = engine.Case(params, parts, dim, precision=precision)
+    g.set_option("factored", factored)   # the factored mixed form has no FP64 blocks
     for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"):
         g.stage(st)
     return g
@@ -79,6 +80,7 @@ def test_noalloc_fp64_case(engine_lib):
 def test_noalloc_rejects_calls_out_of_order(engine_lib):
     name, dim, params, parts = CASES[0]
     g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_option("factored", 0)
     assert _noalloc(g)[0] == ERR_STATE          # nothing solved yet
     for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
         g.stage(st)
@@ -89,6 +91,9 @@ def test_noalloc_rejects_calls_out_of_order(engine_lib):
     assert _noalloc(g)[0] == ERR_STATE          # the step has ended
     assert _entry()(g.h, None) != 0             # null output
     g.close()
+    f = _solved(params, parts, dim, PRECISION_MIXED, factored=1)
+    assert _noalloc(f)[0] == ERR_STATE          # no FP64 blocks in this form
+    f.close()
 
 
 def test_noalloc_rejects_cases_beyond_its_limit(engine_lib):
