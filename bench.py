@@ -403,6 +403,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-factored", action="store_true",
                     help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
+    ap.add_argument("--vectors64", action="store_true", help="mixed form: FP64 CR vectors around the FP32 operators")
+    ap.add_argument("--vcycle64", action="store_true", help="with --vectors64: FP64 V-cycle, FP32 SpMV only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
     ap.add_argument("--ref-fluid", type=int, default=50)
@@ -445,6 +447,8 @@ def main():
     if prec == PRECISION_MIXED:
         case.set_solver(args.outer_tol, args.inner_tol, 50)
         case.set_option("factored", 0 if args.no_factored else 1)
+        case.set_option("vectors64", 1 if args.vectors64 else 0)
+        case.set_option("vcycle64", 1 if args.vcycle64 else 0)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)

@@ -1,19 +1,23 @@
-// k_mixed.cu - mixed-precision solve of the step's system: FP32 inner
-// conjugate residual + FP32 V-cycle, FP64 outer iterative refinement.
+// k_mixed.cu - mixed-precision solve of the step's system: FP32 conjugate
+// residual + FP32 V-cycle, with the FP64 residual replacing the recursive one
+// at every refinement step.
 //
-//   x = v* - F/m dt ; r = b - A x                       (FP64, as the reference)
-//   while rr/rr0 >= tol_outer^2:                          (rr0 = (b,b), FP64)
-//       r32 = r / ||r||                                   (scaled to unit norm)
-//       z = CR_32(A32, r32; M32) to ||r_in|| < tol_inner  (FP32 vectors and
-//                                                          matrices, FP64 dots)
-//       x += ||r|| z ; r = b - A x ; rr = (r,r)           (FP64)
+//   x = v* - F/m dt ; r = b - A x                 (FP64, as the reference)
+//   r32 = r / ||r_0|| ; s = M r32                  (one scale for the whole solve)
+//   CR iterations in FP32 (FP64 dot products) until (r32, r32) has dropped by
+//   tol_inner^2 since the last replacement; then
+//       x += ||r_0|| z ; r = b - A x ; rr = (r,r)  (FP64)
+//       stop if rr/rr0 < tol_outer^2 (rr0 = (b,b)), else replace r32, s = M r32
+//       and go on with the same search directions and iteration count
 //   v = x
 //
 // FP64 on the device is confined to the outer residual b - A x, the solution
 // update and the dot products / norms, which also carry both convergence
-// tests.  The inner CR runs the reference's recurrences (main.cpp:4344-4377)
-// from z = 0.  The default outer tolerance is the reference's
-// ||r||/||b|| < 1e-6; mph_case_set_solver tightens it (e.g. 1e-10).
+// tests.  The CR recurrences are the reference's (main.cpp:4344-4377).  The
+// default outer tolerance is the reference's ||r||/||b|| < 1e-6;
+// mph_case_set_solver tightens it (e.g. 1e-10).
+#include <type_traits>
+
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -24,10 +28,11 @@ bool mixed_available() { return true; }
 __host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
 enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSScale = 19 };
 
-template <int D, int MODE>
+// V: the type of the CR vectors (float, or double with FP32 operators)
+template <int D, int MODE, typename V>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                                 const int* __restrict__ acol, const float* __restrict__ aval,
-                                                const float* __restrict__ xin, float* __restrict__ yout,
+                                                const V* __restrict__ xin, V* __restrict__ yout,
                                                 double* __restrict__ scal, int* __restrict__ flags, int cap,
                                                 double tol2, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
@@ -52,23 +57,23 @@ __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ 
         const long long base = sptr[i >> 5];
         const int* cp = acol + base + lane;
         const float* vp = aval + base * DD + lane;
-        float y[3] = {0.f, 0.f, 0.f};
+        V y[3] = {V(0), V(0), V(0)};   // FP64 vectors: FP64 accumulation over the FP32 blocks
         const int n = nfc[i];
 #pragma unroll 4
         for (int k = 0; k < n; ++k) {
             const int col = cp[(long long)k * 32];
-            float xv[3];
+            V xv[3];
 #pragma unroll
             for (int s = 0; s < D; ++s) xv[s] = xin[(size_t)col * D + s];
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int s = 0; s < D; ++s) y[r] += vp[((long long)k * DD + r * D + s) * 32] * xv[s];
+                for (int s = 0; s < D; ++s) y[r] += (V)vp[((long long)k * DD + r * D + s) * 32] * xv[s];
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
             const size_t k = (size_t)i * D + r;
-            yout[k] = y[r];
+            yout[k] = (V)y[r];
             acc += (double)xin[k] * (double)y[r];
         }
     }
@@ -76,8 +81,9 @@ __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ 
     reduce_finalize(acc, partials, counter, out);
 }
 
-__global__ void k_pq32(int n, const float* __restrict__ s, const float* __restrict__ y, float* __restrict__ p,
-                       float* __restrict__ q, const double* __restrict__ scal, const int* __restrict__ flags)
+template <typename V>
+__global__ void k_pq32(int n, const V* __restrict__ s, const V* __restrict__ y, V* __restrict__ p,
+                       V* __restrict__ q, const double* __restrict__ scal, const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
@@ -88,7 +94,7 @@ __global__ void k_pq32(int n, const float* __restrict__ s, const float* __restri
         }
         return;
     }
-    const float beta = (float)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
+    const V beta = (V)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         p[k] = beta * p[k] + s[k];
         q[k] = beta * q[k] + y[k];
@@ -97,18 +103,19 @@ __global__ void k_pq32(int n, const float* __restrict__ s, const float* __restri
 
 // z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
 // then advances the iteration counter flags[kFlagIter].
-__global__ void k_xrs32(int n, float* __restrict__ z, float* __restrict__ r, float* __restrict__ s,
-                        const float* __restrict__ p, const float* __restrict__ q, const float* __restrict__ u,
+template <typename V>
+__global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
+                        const V* __restrict__ p, const V* __restrict__ q, const V* __restrict__ u,
                         double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                         unsigned* __restrict__ counter)
 {
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
-    const float alpha = (float)(scal[rho32_slot(it)] / scal[kSQU32]);
+    const V alpha = (V)(scal[rho32_slot(it)] / scal[kSQU32]);
     double acc = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         z[k] += alpha * p[k];
-        const float rk = r[k] - alpha * q[k];
+        const V rk = r[k] - alpha * q[k];
         r[k] = rk;
         s[k] -= alpha * u[k];
         acc += (double)rk * (double)rk;
@@ -116,26 +123,28 @@ __global__ void k_xrs32(int n, float* __restrict__ z, float* __restrict__ r, flo
     reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
 }
 
-// r32 = r / sqrt(rr), z = 0, and the inner reference norm (r32, r32)
-__global__ void k_to32(int n, const double* __restrict__ r, float* __restrict__ r32, float* __restrict__ z,
-                       double* __restrict__ scal, double* __restrict__ partials, unsigned* __restrict__ counter)
+// r32 = r * inv_scale, z = 0, and the inner reference norm (r32, r32) -> kSIn0
+template <typename V>
+__global__ void k_to32(int n, const double* __restrict__ r, V* __restrict__ r32, V* __restrict__ z,
+                       double inv_scale, double* __restrict__ scal, double* __restrict__ partials,
+                       unsigned* __restrict__ counter)
 {
-    const double sc = 1.0 / sqrt(scal[kSRR]);
+    const double sc = inv_scale;
     double acc = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const float v = (float)(r[k] * sc);
+        const V v = (V)(r[k] * sc);
         r32[k] = v;
-        z[k] = 0.f;
+        z[k] = V(0);
         acc += (double)v * (double)v;
     }
     reduce_finalize(acc, partials, counter, scal + kSIn0);
 }
 
-// x += ||r|| z  (FP64 update)
-__global__ void k_refine(int n, double* __restrict__ x, const float* __restrict__ z, const double* __restrict__ scal)
+// x += scale z  (FP64 update)
+template <typename V>
+__global__ void k_refine(int n, double* __restrict__ x, const V* __restrict__ z, double scale)
 {
-    const double sc = sqrt(scal[kSRR]);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += sc * (double)z[k];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += scale * (double)z[k];
 }
 
 // r = b - A x in FP64 (the outer residual), (r,r) -> scal[kSRR]
@@ -250,7 +259,7 @@ int mixed_prepare(mph_case* c)
 
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
 
-template <int D>
+template <int D, typename V>
 static int mixed_solve_t(mph_case* c)
 {
     MPH_TRY(mixed_prepare(c));
@@ -264,14 +273,18 @@ static int mixed_solve_t(mph_case* c)
     double* part = d.partials;
     const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
     const unsigned gs = grid_for(Nf, 128);
-    float* r32 = d.v32;
-    float* z32 = d.v32 + (size_t)n;
-    float* s32 = d.v32 + 2 * (size_t)n;
-    float* y32 = d.v32 + 3 * (size_t)n;
-    float* p32 = d.v32 + 4 * (size_t)n;
-    float* q32 = d.v32 + 5 * (size_t)n;
-    float* u32 = d.v32 + 6 * (size_t)n;
+    constexpr bool kF32 = std::is_same<V, float>::value;
+    if (!kF32 && !d.v64) MPH_CUDA(cudaMalloc((void**)&d.v64, (size_t)n * 7 * sizeof(double)));
+    V* vec = kF32 ? reinterpret_cast<V*>(d.v32) : reinterpret_cast<V*>(d.v64);
+    V* r32 = vec;
+    V* z32 = vec + (size_t)n;
+    V* s32 = vec + 2 * (size_t)n;
+    V* y32 = vec + 3 * (size_t)n;
+    V* p32 = vec + 4 * (size_t)n;
+    V* q32 = vec + 5 * (size_t)n;
+    V* u32 = vec + 6 * (size_t)n;
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
+    MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
     { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
     // FP64 residual: from the assembled FP64 blocks, or in factored form
     auto residual = [&]() {
@@ -290,75 +303,90 @@ static int mixed_solve_t(mph_case* c)
     int host_flags[kFlagCount];
     double hs[32];
     bool bad = false;
-    // One inner CR iteration; its index lives in flags[kFlagIter] (reset per
-    // outer step), so one launch sequence serves every iteration and replays
-    // as a graph.  Iterations after convergence return at once.
+    // One FP32 CR iteration; its index lives in flags[kFlagIter] (it runs on
+    // across refinement steps), so one launch sequence serves every iteration
+    // and replays as a graph.  Iterations after a stop return at once.
     auto iteration = [&, c](cudaEvent_t* e) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
-        if (c->step_factored && !c->inner_blocks) {
-            launch_apply32(c, s32, y32, cap, tol_in2);   // FP32 pair terms, no assembled blocks
-        } else {
-            k_spmv32<D, 1><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
-                                               counter);
+        bool blocks = true;
+        if constexpr (kF32) {
+            if (c->step_factored && !c->inner_blocks) {
+                launch_apply32(c, s32, y32, cap, tol_in2);   // FP32 pair terms, no assembled blocks
+                blocks = false;
+            }
+        }
+        if (blocks) {
+            k_spmv32<D, 1, V><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
+                                                  counter);
             MPH_COUNT_LAUNCH();
         }
         if (e) prof_begin(c, 0, &e[1]);
-        { k_pq32<<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
-        vcycle_mixed(c, q32, u32, scal + kSQU32);
-        { k_xrs32<<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
+        { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+        if constexpr (kF32) vcycle_mixed(c, q32, u32, scal + kSQU32);
+        else if (c->vcycle64) vcycle_fp64(c, q32, u32, scal + kSQU32);
+        else vcycle_mixed(c, q32, u32, scal + kSQU32);
+        { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
     const int chunk = 8;
     const bool graphs = c->use_graphs && !c->prof.on;
-    long long chunk_launches = 0;
     if (graphs) {
-        MPH_TRY(capture_graph(c, &c->mx_exec, [&] {
+        MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, tol_in2, cap), [&] {
             for (int k = 0; k < chunk; ++k) iteration(nullptr);
-        }, &chunk_launches));
+        }, &c->mx_launches));
     }
+    const long long chunk_launches = c->mx_launches;
+    // One FP32 CR run; at every refinement step the FP64 residual replaces the
+    // recursive FP32 one (and s = M r is recomputed), while the search
+    // directions p, q and the iteration count carry on, so the Krylov space is
+    // not thrown away.  All FP32 vectors share one scale, fixed at the start.
+    double scale = 1.0;
+    int launched = 0;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
     for (;;) {
         MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
         MPH_CUDA(cudaStreamSynchronize(st));
         if (!(hs[kSRR] == hs[kSRR])) { bad = true; break; }
         if (hs[kSRR] / hs[kSRR0] < tol_out2 || outer >= c->max_outer || hs[kSRR] == 0.0) break;
+        if (outer > 0 && host_flags[kFlagIter] >= cap) break;
+        if (outer == 0) scale = std::sqrt(hs[kSRR]);
+        else MPH_CUDA(cudaMemsetAsync(flags + kFlagDone, 0, sizeof(int), st));
         ++outer;
-        MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
-        { k_to32<<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, scal, part, counter); MPH_COUNT_LAUNCH(); }
-        // inner CR from z = 0: r_in = r32, s = M r_in
-        vcycle_mixed(c, r32, s32, scal + kSQU32);
-        int it = 0;   // iterations launched
+        { k_to32<V><<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, 1.0 / scale, scal, part, counter); MPH_COUNT_LAUNCH(); }
+        MPH_CUDA(cudaMemcpyAsync(scal + kSIn, scal + kSIn0, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        if constexpr (kF32) vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
+        else if (c->vcycle64) vcycle_fp64(c, r32, s32, scal + kSQU32);
+        else vcycle_mixed(c, r32, s32, scal + kSQU32);
         bool done = false;
-        std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
         while (!done) {
             if (graphs) {
                 MPH_CUDA(cudaGraphLaunch(c->mx_exec, st));
                 g_launch_count += chunk_launches;
-                it += chunk;
+                launched += chunk;
             } else {
-                const int m = std::min(chunk, cap + 1 - it);
-                for (int k = 0; k < m; ++k, ++it) {
+                for (int k = 0; k < chunk; ++k, ++launched) {
                     cudaEvent_t e[2] = {nullptr, nullptr};
                     const bool pon = prof_begin(c, 0, &e[0]) != 0;
                     iteration(pon ? e : nullptr);
-                    if (pon) timed.push_back({it, {e[0], e[1]}});
+                    if (pon) timed.push_back({launched, {e[0], e[1]}});
                 }
             }
             MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
             MPH_CUDA(cudaStreamSynchronize(st));
-            done = host_flags[kFlagDone] != 0 || it > cap;
-        }
-        const int inner = host_flags[kFlagDone] ? host_flags[kFlagIter] : cap;
-        for (auto& t : timed) {   // keep the SpMV launches of iterations that ran
-            if (t.first < inner) {
-                c->prof.pending.push_back({0, t.second});
-            } else {
-                c->prof.pool.push_back(t.second.first);
-                c->prof.pool.push_back(t.second.second);
-            }
+            done = host_flags[kFlagDone] != 0 || launched > cap + chunk;
         }
         if (host_flags[kFlagBad]) { bad = true; break; }
-        total_inner += inner;
-        { k_refine<<<rb, kReduceThreads, 0, st>>>(n, d.x, z32, scal); MPH_COUNT_LAUNCH(); }
+        { k_refine<V><<<rb, kReduceThreads, 0, st>>>(n, d.x, z32, scale); MPH_COUNT_LAUNCH(); }
         residual();
+    }
+    total_inner = host_flags[kFlagIter];
+    for (auto& t : timed) {   // keep the SpMV launches of iterations that ran
+        if (t.first < total_inner) {
+            c->prof.pending.push_back({0, t.second});
+        } else {
+            c->prof.pool.push_back(t.second.first);
+            c->prof.pool.push_back(t.second.second);
+        }
     }
     { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
     MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
@@ -375,7 +403,10 @@ static int mixed_solve_t(mph_case* c)
 
 int run_mixed_solve(mph_case* c)
 {
-    return c->dim == 2 ? mixed_solve_t<2>(c) : mixed_solve_t<3>(c);
+    // FP64 CR vectors around the FP32 operators (blocks SpMV and V-cycle)
+    const bool v64 = c->vectors64 && (!c->step_factored || c->inner_blocks);
+    if (v64) return c->dim == 2 ? mixed_solve_t<2, double>(c) : mixed_solve_t<3, double>(c);
+    return c->dim == 2 ? mixed_solve_t<2, float>(c) : mixed_solve_t<3, float>(c);
 }
 
 }  // namespace mph

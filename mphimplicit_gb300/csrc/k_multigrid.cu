@@ -17,16 +17,23 @@
 //         kernel per smoothing sweep (S_new = S + invD (Q - A S)), a residual
 //         kernel before each restriction, and the restriction (child sums).
 //         Every level from the first one with at most kCtaRows rows down to
-//         the coarsest and back runs inside one 1024-thread block, its sweeps
-//         separated by __syncthreads, so the small levels cost one launch.
+//         the coarsest and back runs inside one cluster of kClusterCtas
+//         1024-thread blocks (one per SM), its sweeps separated by cluster
+//         barriers, so the small levels cost one launch and read their
+//         stencils through the L2 ports of eight SMs.
 //         The last kernel adds G2P S_0 to D^-1 q and forms the (q, u) dot.
+#include <cooperative_groups.h>
+
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace mph {
 
 constexpr int kCtaRows = 8192;
 constexpr int kCtaThreads = 1024;
+constexpr int kClusterCtas = 8;
 
 struct LevelK {
     int mn[3], mx[3], cnt[3], st[3];
@@ -320,49 +327,53 @@ struct CoarseArgs {
 };
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kCtaThreads) k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCtaThreads)
+k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
 {
-    if (flags[kFlagDone]) return;
+    if (flags[kFlagDone]) return;   // the same for every block of the cluster
+    cg::cluster_group cluster = cg::this_cluster();
+    const int tid = (int)cluster.block_rank() * blockDim.x + threadIdx.x;
+    const int nth = (int)(blockDim.x * cluster.num_blocks());
     T* cur[kMaxLevels];
     T* oth[kMaxLevels];
     for (int l = A.first; l < A.depth; ++l) { cur[l] = A.Sa[l]; oth[l] = A.Sb[l]; }
     auto jacobi = [&](int l) {
         const LevelK& L = A.L[l];
-        for (int row = threadIdx.x; row < L.rows; row += blockDim.x) {
+        for (int row = tid; row < L.rows; row += nth) {
             const T r = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
             oth[l][row] = cur[l][row] + A.invd[l][row] * r;
         }
-        __syncthreads();
+        cluster.sync();
         T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
     };
     // down: restriction + pre-smoothing (3 updates, the coarsest 5)
     for (int l = A.first; l < A.depth; ++l) {
         const LevelK& L = A.L[l];
-        for (int row = threadIdx.x; row < L.rows; row += blockDim.x) {
+        for (int row = tid; row < L.rows; row += nth) {
             const T q = row_restrict<D, T>(A.L[l - 1], L, A.R[l - 1], row);
             A.Q[l][row] = q;
             cur[l][row] = A.invd[l][row] * q;
         }
-        __syncthreads();
+        cluster.sync();
         const int sweeps = (l == A.depth - 1) ? 4 : 2;
         for (int k = 0; k < sweeps; ++k) jacobi(l);
         if (l < A.depth - 1) {
-            for (int row = threadIdx.x; row < L.rows; row += blockDim.x)
+            for (int row = tid; row < L.rows; row += nth)
                 A.R[l][row] = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
-            __syncthreads();
+            cluster.sync();
         }
     }
     // up: prolongation + post-smoothing (3 updates)
     for (int l = A.depth - 1; l > A.first; --l) {
         const LevelK& S_ = A.L[l - 1];
-        for (int row = threadIdx.x; row < S_.rows; row += blockDim.x)
+        for (int row = tid; row < S_.rows; row += nth)
             cur[l - 1][row] = cur[l - 1][row] + cur[l][row_parent<D>(S_, A.L[l], row)];
-        __syncthreads();
+        cluster.sync();
         for (int k = 0; k < 3; ++k) jacobi(l - 1);
     }
     // prolongation into the finer, grid-wide level
     const LevelK& S_ = A.L[A.first - 1];
-    for (int row = threadIdx.x; row < S_.rows; row += blockDim.x)
+    for (int row = tid; row < S_.rows; row += nth)
         A.Sfine[row] = A.Sfine[row] + cur[A.first][row_parent<D>(S_, A.L[A.first], row)];
 }
 
@@ -419,7 +430,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
             A.R[l] = Rp + ov(l);
         }
         A.Sfine = cur[first - 1];
-        { k_mg_small_levels<D, T><<<1, kCtaThreads, 0, st>>>(A, flags); MPH_COUNT_LAUNCH(); }
+        { k_mg_small_levels<D, T><<<kClusterCtas, kCtaThreads, 0, st>>>(A, flags); MPH_COUNT_LAUNCH(); }
     }
     // up, grid-wide levels: the block kernel already prolongated into level
     // first-1; without it the coarsest level is prolongated here
@@ -452,6 +463,16 @@ void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
         vcycle_t<2, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
     else
         vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
+}
+
+// FP32 V-cycle with FP64 vectors in and out (the mixed form's FP64-vector CR)
+void vcycle_mixed(mph_case* c, const double* q, double* u, double* dot_out)
+{
+    DeviceState& d = c->d;
+    if (c->dim == 2)
+        vcycle_t<2, float, double>(c, q, u, d.invDiag, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
+    else
+        vcycle_t<3, float, double>(c, q, u, d.invDiag, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
 }
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)

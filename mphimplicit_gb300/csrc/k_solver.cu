@@ -204,12 +204,12 @@ static int cr_solve_t(mph_case* c)
     // launches of iterations that ran are kept (later ones return at once)
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
     const bool graphs = c->use_graphs && !c->prof.on;
-    long long chunk_launches = 0;
     if (graphs) {
-        MPH_TRY(capture_graph(c, &c->cr_exec, [&] {
+        MPH_TRY(capture_graph(c, &c->cr_exec, &c->cr_sig, graph_signature(c, 1.0e-12, cap), [&] {
             for (int k = 0; k < chunk; ++k) iteration(nullptr);
-        }, &chunk_launches));
+        }, &c->cr_launches));
     }
+    const long long chunk_launches = c->cr_launches;
     while (!done) {
         if (graphs) {
             MPH_CUDA(cudaGraphLaunch(c->cr_exec, st));

@@ -609,7 +609,7 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags,
-                    (void*)d.mg_invd32, (void*)d.pe, (void*)d.pe32, (void*)d.tct, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
+                    (void*)d.mg_invd32, (void*)d.pe, (void*)d.pe32, (void*)d.tct, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, (void*)d.v64, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

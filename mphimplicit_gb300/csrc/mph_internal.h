@@ -124,6 +124,7 @@ struct DeviceState {
     float *mg_cof32 = nullptr, *mg_invd32 = nullptr;
     float *mg_q32 = nullptr, *mg_s32 = nullptr, *mg_r32 = nullptr, *mg_res32 = nullptr;
     float* v32 = nullptr;           // mixed form: 7 FP32 CR vectors + FP32 D^-1, each D*Nf
+    double* v64 = nullptr;          // mixed form with FP64 CR vectors: 7 vectors, each D*Nf
     long long cap_mg_cof = 0, cap_mg_vec = 0, cap_mg_cof32 = 0, cap_mg_vec32 = 0;
     // solver vectors [D*Nf]
     double *x = nullptr, *r = nullptr, *s = nullptr, *y = nullptr, *p = nullptr, *q = nullptr, *u = nullptr;
@@ -189,12 +190,16 @@ struct mph_case {
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
+    bool vectors64 = false;             // mixed form: FP64 CR vectors around the FP32 operators
+    bool vcycle64 = false;              // with vectors64: FP64 V-cycle (only the SpMV in FP32)
     bool step_factored = false;         // this step's system uses the factored form
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
     cudaGraphExec_t cr_exec = nullptr;  // FP64 CR chunk
     cudaGraphExec_t mx_exec = nullptr;  // mixed form: FP32 inner CR chunk
     cudaStream_t cap_stream = nullptr;  // side stream the chunks are captured on
+    unsigned long long cr_sig = 0, mx_sig = 0;   // signatures the two graphs were captured from
+    long long cr_launches = 0, mx_launches = 0;  // kernel launches in one replay of each
     cudaStream_t own_stream = nullptr;  // private stream for batched steps of a legacy-stream case
     mph::DeviceState d;
     std::vector<void*> allocations;

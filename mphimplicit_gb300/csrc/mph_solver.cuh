@@ -98,9 +98,43 @@ __device__ __forceinline__ void reduce_finalize_step(double v, double* __restric
 // may be the legacy stream, which cannot be captured): c->stream points
 // there while `body` runs.  Returns the number of kernel launches the
 // sequence contains in *launches.
-template <typename F>
-int capture_graph(mph_case* c, cudaGraphExec_t* exec, F&& body, long long* launches)
+//
+// Every argument of the captured launches derives from the case's device
+// buffers, parameters, level geometry and the given scalars, so a hash of
+// those identifies the graph: when it matches the one *exec was made from,
+// the capture is skipped (*launches is kept from that capture).
+inline unsigned long long fnv1a(unsigned long long h, const void* p, size_t n)
 {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t k = 0; k < n; ++k) h = (h ^ b[k]) * 1099511628211ull;
+    return h;
+}
+
+inline unsigned long long graph_signature(const mph_case* c, double tol, int cap)
+{
+    unsigned long long h = 1469598103934665603ull;
+    // the particle arrays swap with their alternates every step and no
+    // captured kernel reads them (the type array only on the pair-term path)
+    DeviceState d = c->d;
+    d.pos = d.vel = d.force = d.pos_alt = d.vel_alt = nullptr;
+    d.pos32 = nullptr;
+    d.id = d.id_alt = d.type_alt = nullptr;
+    if (!(c->step_factored && !c->inner_blocks)) d.type = nullptr;
+    h = fnv1a(h, &d, sizeof(d));
+    h = fnv1a(h, &c->dp, sizeof(c->dp));
+    if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));
+    const long long misc[] = {c->depth, c->nslices, c->nslots, c->precision, c->step_factored, c->inner_blocks, c->vectors64, c->vcycle64,
+                              cap, c->mg_rows_total, c->mg_cof_total};
+    h = fnv1a(h, misc, sizeof(misc));
+    h = fnv1a(h, &tol, sizeof(tol));
+    return h;
+}
+
+template <typename F>
+int capture_graph(mph_case* c, cudaGraphExec_t* exec, unsigned long long* sig_slot, unsigned long long sig, F&& body,
+                  long long* launches)
+{
+    if (*exec && *sig_slot == sig) return MPH_OK;   // same graph as the last capture
     if (!c->cap_stream) MPH_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
     const long long l0 = t_launch_count;
     cudaGraph_t graph = nullptr;
@@ -132,10 +166,12 @@ int capture_graph(mph_case* c, cudaGraphExec_t* exec, F&& body, long long* launc
         }
     }
     cudaGraphDestroy(graph);
+    *sig_slot = sig;
     return MPH_OK;
 }
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out);
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
+void vcycle_mixed(mph_case* c, const double* q, double* u, double* dot_out);
 
 }  // namespace mph
