@@ -403,8 +403,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-factored", action="store_true",
                     help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
-    ap.add_argument("--vectors64", action="store_true", help="mixed form: FP64 CR vectors around the FP32 operators")
-    ap.add_argument("--vcycle64", action="store_true", help="with --vectors64: FP64 V-cycle, FP32 SpMV only")
+    ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
     ap.add_argument("--ref-fluid", type=int, default=50)
@@ -447,8 +446,6 @@ def main():
     if prec == PRECISION_MIXED:
         case.set_solver(args.outer_tol, args.inner_tol, 50)
         case.set_option("factored", 0 if args.no_factored else 1)
-        case.set_option("vectors64", 1 if args.vectors64 else 0)
-        case.set_option("vcycle64", 1 if args.vcycle64 else 0)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)
@@ -519,6 +516,26 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample(os.cpu_count() or 1, 1, args.cpu_fluid, check_gpu=True)
 
+    # the plain FP64 form on the same workload (for the mixed form's speed-up),
+    # and one step of each form from the same state (velocity error)
+    plain = None
+    errs = []
+    if prec == PRECISION_MIXED and not args.no_fp64_leg:
+        case.close()
+        f = engine.Case(params, parts, dim, precision=PRECISION_FP64, stream=stream.cuda_stream)
+        for _ in range(args.warmup):
+            f.step(1)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            f.step(1)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        plain = N * args.steps / (ev[0].elapsed_time(ev[1]) / 1000.0)
+        f.close()
+        errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol)
+
     stage_total = sum(prof[f"stage_ms_{s}"] for s in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -534,7 +551,11 @@ def main():
                    "stage_sum_ms_per_step": stage_total / args.steps,
                    "kernel_avg_ms": {k: (prof[f"kern_ms_{k}"] / prof[f"kern_n_{k}"] if prof[f"kern_n_{k}"] else None)
                                      for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
-                   "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "vcycle", "assemble_a", "neighbors")}},
+                   "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
+                   "outer_tol": args.outer_tol if prec == PRECISION_MIXED else 1e-6,
+                   "plain_fp64_value": plain,
+                   "speedup_vs_plain_fp64": (value / plain) if plain else None,
+                   "vel_rel_err_vs_fp64_per_step": errs},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": args.e2e_steps},
         "gpu_launches": launches,
@@ -544,7 +565,8 @@ def main():
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    case.close()
+    if prec != PRECISION_MIXED or args.no_fp64_leg:
+        case.close()
     if dist:
         dist.destroy_process_group()
     return 0

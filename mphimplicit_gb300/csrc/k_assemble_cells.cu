@@ -281,6 +281,24 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
                 for (int s = 0; s < D; ++s) acc[self * DD + r * D + s] = selfc[r * D + s] + (r == s ? (T)inert : T(0));
         }
         __syncwarp();
+        // sliced-ELL write-out of the row's blocks (the FP32 form writes them
+        // only when its inner SpMV uses them)
+        auto write_blocks = [&]() {
+            const long long sb = sptr[i >> 5];
+            const int ln = i & 31;
+            for (int t = lane; t < nf * DD; t += 32) {
+                const int k = t / DD, rs = t - k * DD;
+                const long long at = sb * DD + ((long long)k * DD + rs) * 32 + ln;
+                if (MIX) {
+                    aval32[at] = (float)acc[t];
+                } else {
+                    aval[at] = (double)acc[t];
+                    if (aval32) aval32[at] = (float)acc[t];
+                }
+            }
+            for (int k = lane; k < nf; k += 32) acol[sb + (long long)k * 32 + ln] = nind[nb + k];
+            __syncwarp();
+        };
         // 3. C Lambda C^T, one P-neighbour column at a time (main.cpp:2590-2641)
         const long long pb = nptrP[i];
         const int np = ncp[i];
@@ -345,25 +363,8 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
             for (int k = k0; k < k1; ++k) sum += acc[k * DD + rs];
             part[((size_t)i * M.S + wslot[s]) * DD + rs] = (double)sum;
         }
-        // 6. sliced-ELL write-out (the FP32 form writes blocks only when its
-        // inner SpMV uses them)
-        if (MIX && !aval32) {
-            __syncwarp();
-            continue;
-        }
-        const long long sb = sptr[i >> 5];
-        const int ln = i & 31;
-        for (int t = lane; t < nf * DD; t += 32) {
-            const int k = t / DD, rs = t - k * DD;
-            const long long at = sb * DD + ((long long)k * DD + rs) * 32 + ln;
-            if (MIX) {
-                aval32[at] = (float)acc[t];
-            } else {
-                aval[at] = (double)acc[t];
-                if (aval32) aval32[at] = (float)acc[t];
-            }
-        }
-        for (int k = lane; k < nf; k += 32) acol[sb + (long long)k * 32 + ln] = nind[nb + k];
+        // 6. sliced-ELL write-out of the full blocks
+        if (!(MIX && !aval32)) write_blocks();
         __syncwarp();
     }
 }

@@ -15,11 +15,12 @@
 // in the neighbour list, where the reference adds the product); the engine
 // uses this form only then.
 //
-// k_pair_terms stores (e, f) per neighbour slot of every fluid row in FP64
-// (the outer residual b - A x) and in FP32 (the inner FP32 blocks), and b in
-// FP64.  FP64 work per slot: the separation, its norm, one rsqrt and a few
-// products, against the nine-entry block and its accumulation of the
-// assembled form.
+// k_pair_terms stores (e, f) per neighbour slot of every fluid row in FP32
+// (used by the FP32 blocks and by the viscous part of the FP64 residual) and b
+// in FP64.  The only FP64 work per slot is the exact minimum-image separation,
+// against the nine-entry block and its accumulation of the assembled form; in
+// the residual only inertia and C Lambda C^T (about 20 P-slots a row) are
+// FP64.
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -27,20 +28,24 @@ namespace mph {
 
 constexpr int kPairWarps = 8;
 
-// (e, f) of every neighbour slot of the fluid rows, and b
-// (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).
+// (e, f) of every neighbour slot of the fluid rows in FP32, and b
+// (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).  The
+// separation is the exact FP64 minimum image of the neighbour search; the rest
+// of the viscous term is FP32: it is about nu dt / l0^2 (~1e-3) of the
+// inertia term, so its FP32 rounding moves A x by ~1e-10 of |b| (the host
+// keeps the factored form off when that bound would reach 1e-2 of the outer
+// tolerance).  Inertia and C p stay FP64.
 template <int D>
 __global__ void __launch_bounds__(kPairWarps * 32)
 k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const double* __restrict__ vel,
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
-             double4* __restrict__ pe, float4* __restrict__ pe32, double* __restrict__ bvec)
+             float4* __restrict__ pe32, double* __restrict__ bvec)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const double rV2 = P.rV * P.rV;
     for (int i = wid; i < P.Nf; i += nwarps) {
         const int ti = type[i];
         const long long nb = nptr[i];
@@ -48,37 +53,40 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         double xi[3], vi[3];
         load_vec<D>(pos, i, xi);
         load_vec<D>(vel, i, vi);
-        double sumv[3] = {0.0, 0.0, 0.0};
+        float sumw[3] = {0.f, 0.f, 0.f};
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
-            double e[3] = {0.0, 0.0, 0.0};
-            double f = 0.0;
+            float e[3] = {0.f, 0.f, 0.f};
+            float f = 0.f;
             if (j != i) {
                 double xj[3], q[3];
                 load_vec<D>(pos, j, xj);
                 sep_vec<D>(P, xj, xi, q);
-                const double r2 = norm2_exact<D>(q);
-                if (r2 != 0.0 && rV2 - r2 > 0) {
-                    const double inv = rsqrt(r2);
-                    const double wd = -P.kfv * (P.m2h_rv * (1.0 - (r2 * inv) * P.inv_rv));
-                    f = P.visc * P.muij[ti][type[j]] * wd * inv;
+                float q32[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-                    for (int d = 0; d < D; ++d) e[d] = q[d] * inv;
+                for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
+                const float r2 = q32[0] * q32[0] + q32[1] * q32[1] + q32[2] * q32[2];
+                if (r2 != 0.f && P.rV2_32 - r2 > 0.f) {
+                    const float inv = rsqrtf(r2);
+                    const float wd = P.wdA32 * (1.f - (r2 * inv) * P.inv_rv32);
+                    f = P.vm32[ti][type[j]] * wd * inv;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) e[d] = q32[d] * inv;
                     if (k >= nf) {   // wall neighbour: its velocity enters b
                         double vj[3];
                         load_vec<D>(vel, j, vj);
-                        double ev = 0.0;
+                        float ev = 0.f;
 #pragma unroll
-                        for (int d = 0; d < D; ++d) ev += e[d] * vj[d];
+                        for (int d = 0; d < D; ++d) ev += e[d] * (float)vj[d];
 #pragma unroll
-                        for (int r = 0; r < D; ++r) sumv[r] += f * e[r] * ev;
+                        for (int r = 0; r < D; ++r) sumw[r] += f * e[r] * ev;
                     }
                 }
             }
-            pe[nb + k] = make_double4(e[0], e[1], e[2], f);
-            pe32[nb + k] = make_float4((float)e[0], (float)e[1], (float)e[2], (float)f);
+            pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
         }
-        // - C p over the row's P-neighbours
+        // - C p over the row's P-neighbours (FP64)
+        double sumv[3] = {(double)sumw[0], (double)sumw[1], (double)sumw[2]};
         const long long pb = nptrP[i];
         const int np = ncp[i];
         for (int a = lane; a < np; a += 32) {
@@ -121,43 +129,44 @@ __global__ void k_ct_apply(int N, const long long* __restrict__ ctptr, const int
     t[k] = s;
 }
 
-// r = b - A x in factored form, (r, r) -> *out (deterministic reduction).
+// r = b - A x in factored form, (r, r) -> *out (deterministic reduction):
+// inertia and C Lambda t (t = C^T x) in FP64, the viscous pair terms in FP32
+// on the FP32 copy x32 of x.
 template <int D>
 __global__ void __launch_bounds__(kPairWarps * 32)
 k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restrict__ nc, const int* __restrict__ nfc,
-                 const long long* __restrict__ nptr, const int* __restrict__ nind, const double4* __restrict__ pe,
+                 const long long* __restrict__ nptr, const int* __restrict__ nind, const float4* __restrict__ pe32,
                  const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
                  const double* __restrict__ cval, const double* __restrict__ t, const double* __restrict__ x,
-                 const double* __restrict__ b, double* __restrict__ r, double* __restrict__ partials,
-                 unsigned* __restrict__ counter, double* __restrict__ out)
+                 const float* __restrict__ x32, const double* __restrict__ b, double* __restrict__ r,
+                 double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     double acc_rr = 0.0;
     for (int i = wid; i < P.Nf; i += nwarps) {
-        double xi[3] = {0.0, 0.0, 0.0};
+        float xi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
-        double y[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < D; ++d) xi[d] = x32[(size_t)i * D + d];
+        float yv[3] = {0.f, 0.f, 0.f};
         const long long nb = nptr[i];
         const int n = nc[i], nf = nfc[i];
         for (int k = lane; k < n; k += 32) {
-            const double4 p = pe[nb + k];
-            const double e[3] = {p.x, p.y, p.z};
-            double dx[3] = {xi[0], xi[1], xi[2]};
+            const float4 p = pe32[nb + k];
+            float dx[3] = {xi[0], xi[1], xi[2]};
             if (k < nf) {
                 const int j = nind[nb + k];
 #pragma unroll
-                for (int d = 0; d < D; ++d) dx[d] -= x[(size_t)j * D + d];
+                for (int d = 0; d < D; ++d) dx[d] -= x32[(size_t)j * D + d];
             }
-            double ed = 0.0;
-#pragma unroll
-            for (int d = 0; d < D; ++d) ed += e[d] * dx[d];
-            const double s = p.w * ed;
-#pragma unroll
-            for (int d = 0; d < D; ++d) y[d] += s * e[d];
+            const float ed = p.x * dx[0] + p.y * dx[1] + (D == 3 ? p.z * dx[2] : 0.f);
+            const float sc = p.w * ed;
+            yv[0] += sc * p.x;
+            yv[1] += sc * p.y;
+            if (D == 3) yv[2] += sc * p.z;
         }
+        double y[3] = {(double)yv[0], (double)yv[1], (double)yv[2]};
         const long long pb = nptrP[i];
         const int np = ncp[i];
         for (int a = lane; a < np; a += 32) {
@@ -174,8 +183,9 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
             const double inert = P.density[type[i]] * P.vol / P.vol / P.dt;
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                const double rv = b[(size_t)i * D + d] - (inert * xi[d] + y[d]);
-                r[(size_t)i * D + d] = rv;
+                const size_t k = (size_t)i * D + d;
+                const double rv = b[k] - (inert * x[k] + y[d]);
+                r[k] = rv;
                 acc_rr += rv * rv;
             }
         }
@@ -188,16 +198,17 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 // (k_ct_apply32, which also runs the iteration's convergence test), then per
 // fluid row inertia + viscous pair terms + C Lambda t, and (s, y) into the
 // iteration's rho slot (k_apply32).  Same recurrences and flags as k_spmv32.
-constexpr int kSIn0 = 16, kSIn = 17;
+constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 
 template <int D>
 __global__ void k_ct_apply32(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
                              const float* __restrict__ ct_v32, const float* __restrict__ x, float* __restrict__ t,
-                             const double* __restrict__ scal, int* __restrict__ flags, int cap, double tol2)
+                             const double* __restrict__ scal, int* __restrict__ flags, int cap)
 {
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
+    const double tol2 = scal[kSTol2];
     const double rr0 = scal[kSIn0];
     const double rr = it == 0 ? rr0 : scal[kSIn];
     const bool bad = !(rr == rr);
@@ -284,7 +295,7 @@ k_apply32(DevParams P, const int* __restrict__ type, const int* __restrict__ nc,
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }
 
-void launch_apply32(mph_case* c, const float* x, float* y, int cap, double tol2)
+void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 {
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
@@ -292,11 +303,11 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap, double tol2)
     const unsigned gt = grid_for(P.N, 256);
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
     if (c->dim == 2) {
-        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap, tol2); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
         { k_apply32<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
                                                             d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap, tol2); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
         { k_apply32<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
                                                             d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     }
@@ -307,21 +318,23 @@ static int grow_pairs(mph_case* c, long long slots)
 {
     DeviceState& d = c->d;
     if (slots <= d.cap_pairs) return MPH_OK;
-    if (d.pe) cudaFree(d.pe);
     if (d.pe32) cudaFree(d.pe32);
-    d.pe = nullptr;
     d.pe32 = nullptr;
     d.cap_pairs = 0;
     const long long n = slots + slots / 8 + 1024;
-    MPH_CUDA(cudaMalloc((void**)&d.pe, (size_t)n * sizeof(double4)));
     MPH_CUDA(cudaMalloc((void**)&d.pe32, (size_t)n * sizeof(float4)));
     d.cap_pairs = n;
     return MPH_OK;
 }
 
+// The factored operator equals the assembled one when 2 RadiusP < MaxRadius;
+// its FP32 viscous part is accurate enough while FP32 rounding of that part
+// (about 1e-7 of it, the part being visc_ratio of the inertia) stays below
+// 1e-2 of the outer tolerance.
 bool factored_applies(const mph_case* c)
 {
-    return c->precision == MPH_PRECISION_MIXED && c->factored && 2.0 * c->dp.rP < c->dp.maxR;
+    return c->precision == MPH_PRECISION_MIXED && c->factored && 2.0 * c->dp.rP < c->dp.maxR &&
+           1.0e-7 * c->visc_ratio < 1.0e-2 * c->tol_outer;
 }
 
 int launch_pair_terms(mph_case* c)
@@ -333,6 +346,7 @@ int launch_pair_terms(mph_case* c)
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     MPH_TRY(grow_pairs(c, slots));
     if (!d.tct) MPH_CUDA(cudaMalloc((void**)&d.tct, (size_t)(P.N + 1) * sizeof(double)));
+    if (!d.x32) MPH_CUDA(cudaMalloc((void**)&d.x32, (size_t)P.Nf * c->dim * sizeof(float)));
     if (!d.tct32) MPH_CUDA(cudaMalloc((void**)&d.tct32, (size_t)(P.N + 1) * sizeof(float)));
     long long ncv = 0;   // C values of the fluid rows, FP32 copy for the inner operator
     MPH_CUDA(cudaMemcpyAsync(&ncv, d.nptrP + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
@@ -349,10 +363,10 @@ int launch_pair_terms(mph_case* c)
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }
@@ -364,14 +378,18 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
     const unsigned gt = grid_for(P.N, 256);
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
+    const long long nv = (long long)P.Nf * c->dim;
+    { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
     if (c->dim == 2) {
         { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-        { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe, d.ncp, d.nptrP, d.nindP,
-                                                                   d.cval, d.tct, x, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+        { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                                   d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter,
+                                                                   out); MPH_COUNT_LAUNCH(); }
     } else {
         { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-        { k_resid_factored<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe, d.ncp, d.nptrP, d.nindP,
-                                                                   d.cval, d.tct, x, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+        { k_resid_factored<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                                   d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter,
+                                                                   out); MPH_COUNT_LAUNCH(); }
     }
 }
 

@@ -16,8 +16,6 @@
 // tests.  The CR recurrences are the reference's (main.cpp:4344-4377).  The
 // default outer tolerance is the reference's ||r||/||b|| < 1e-6;
 // mph_case_set_solver tightens it (e.g. 1e-10).
-#include <type_traits>
-
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -26,19 +24,19 @@ namespace mph {
 bool mixed_available() { return true; }
 
 __host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
-enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSScale = 19 };
+enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSTol2 = 23 };   // kSTol2: this phase's inner target
 
-// V: the type of the CR vectors (float, or double with FP32 operators)
 template <int D, int MODE, typename V>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                                 const int* __restrict__ acol, const float* __restrict__ aval,
                                                 const V* __restrict__ xin, V* __restrict__ yout,
                                                 double* __restrict__ scal, int* __restrict__ flags, int cap,
-                                                double tol2, double* __restrict__ partials, unsigned* __restrict__ counter)
+                                                double* __restrict__ partials, unsigned* __restrict__ counter)
 {
     constexpr int DD = D * D;
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
+    const double tol2 = scal[kSTol2];
     const double rr0 = scal[kSIn0];
     const double rr = it == 0 ? rr0 : scal[kSIn];   // the inner solve starts from z = 0: r_in = r32
     const bool bad = !(rr == rr);
@@ -57,18 +55,18 @@ __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ 
         const long long base = sptr[i >> 5];
         const int* cp = acol + base + lane;
         const float* vp = aval + base * DD + lane;
-        V y[3] = {V(0), V(0), V(0)};   // FP64 vectors: FP64 accumulation over the FP32 blocks
+        float y[3] = {0.f, 0.f, 0.f};
         const int n = nfc[i];
 #pragma unroll 4
         for (int k = 0; k < n; ++k) {
             const int col = cp[(long long)k * 32];
-            V xv[3];
+            float xv[3];
 #pragma unroll
-            for (int s = 0; s < D; ++s) xv[s] = xin[(size_t)col * D + s];
+            for (int s = 0; s < D; ++s) xv[s] = (float)xin[(size_t)col * D + s];
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int s = 0; s < D; ++s) y[r] += (V)vp[((long long)k * DD + r * D + s) * 32] * xv[s];
+                for (int s = 0; s < D; ++s) y[r] += vp[((long long)k * DD + r * D + s) * 32] * xv[s];
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
@@ -138,6 +136,18 @@ __global__ void k_to32(int n, const double* __restrict__ r, V* __restrict__ r32,
         acc += (double)v * (double)v;
     }
     reduce_finalize(acc, partials, counter, scal + kSIn0);
+}
+
+// Inner target of the next phase: reduce the recursive residual by tol_in,
+// but no further than half of what the outer test still asks for
+// (rr / rr0 -> tol_out^2), so the last phase does not overshoot.
+__global__ void k_phase_tol(double* __restrict__ scal, double tol_in2, double tol_out2)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double need = 0.25 * tol_out2 * scal[kSRR0] / scal[kSRR];
+        scal[kSTol2] = need > tol_in2 ? need : tol_in2;
+        scal[kSIn] = scal[kSIn0];
+    }
 }
 
 // x += scale z  (FP64 update)
@@ -259,9 +269,10 @@ int mixed_prepare(mph_case* c)
 
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
 
-template <int D, typename V>
+template <int D>
 static int mixed_solve_t(mph_case* c)
 {
+    using V = float;
     MPH_TRY(mixed_prepare(c));
     DeviceState& d = c->d;
     const int Nf = c->dp.Nf;
@@ -273,9 +284,7 @@ static int mixed_solve_t(mph_case* c)
     double* part = d.partials;
     const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
     const unsigned gs = grid_for(Nf, 128);
-    constexpr bool kF32 = std::is_same<V, float>::value;
-    if (!kF32 && !d.v64) MPH_CUDA(cudaMalloc((void**)&d.v64, (size_t)n * 7 * sizeof(double)));
-    V* vec = kF32 ? reinterpret_cast<V*>(d.v32) : reinterpret_cast<V*>(d.v64);
+    V* vec = d.v32;
     V* r32 = vec;
     V* z32 = vec + (size_t)n;
     V* s32 = vec + 2 * (size_t)n;
@@ -308,23 +317,16 @@ static int mixed_solve_t(mph_case* c)
     // and replays as a graph.  Iterations after a stop return at once.
     auto iteration = [&, c](cudaEvent_t* e) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
-        bool blocks = true;
-        if constexpr (kF32) {
-            if (c->step_factored && !c->inner_blocks) {
-                launch_apply32(c, s32, y32, cap, tol_in2);   // FP32 pair terms, no assembled blocks
-                blocks = false;
-            }
-        }
-        if (blocks) {
-            k_spmv32<D, 1, V><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, tol_in2, part,
+        if (c->step_factored && !c->inner_blocks) {
+            launch_apply32(c, s32, y32, cap);   // FP32 pair terms, no assembled blocks
+        } else {
+            k_spmv32<D, 1, V><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, part,
                                                   counter);
             MPH_COUNT_LAUNCH();
         }
         if (e) prof_begin(c, 0, &e[1]);
         { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
-        if constexpr (kF32) vcycle_mixed(c, q32, u32, scal + kSQU32);
-        else if (c->vcycle64) vcycle_fp64(c, q32, u32, scal + kSQU32);
-        else vcycle_mixed(c, q32, u32, scal + kSQU32);
+        vcycle_mixed(c, q32, u32, scal + kSQU32);
         { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
     const int chunk = 8;
@@ -353,10 +355,8 @@ static int mixed_solve_t(mph_case* c)
         else MPH_CUDA(cudaMemsetAsync(flags + kFlagDone, 0, sizeof(int), st));
         ++outer;
         { k_to32<V><<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, 1.0 / scale, scal, part, counter); MPH_COUNT_LAUNCH(); }
-        MPH_CUDA(cudaMemcpyAsync(scal + kSIn, scal + kSIn0, sizeof(double), cudaMemcpyDeviceToDevice, st));
-        if constexpr (kF32) vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
-        else if (c->vcycle64) vcycle_fp64(c, r32, s32, scal + kSQU32);
-        else vcycle_mixed(c, r32, s32, scal + kSQU32);
+        { k_phase_tol<<<1, 32, 0, st>>>(scal, tol_in2, tol_out2); MPH_COUNT_LAUNCH(); }
+        vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
         bool done = false;
         while (!done) {
             if (graphs) {
@@ -403,10 +403,7 @@ static int mixed_solve_t(mph_case* c)
 
 int run_mixed_solve(mph_case* c)
 {
-    // FP64 CR vectors around the FP32 operators (blocks SpMV and V-cycle)
-    const bool v64 = c->vectors64 && (!c->step_factored || c->inner_blocks);
-    if (v64) return c->dim == 2 ? mixed_solve_t<2, double>(c) : mixed_solve_t<3, double>(c);
-    return c->dim == 2 ? mixed_solve_t<2, float>(c) : mixed_solve_t<3, float>(c);
+    return c->dim == 2 ? mixed_solve_t<2>(c) : mixed_solve_t<3>(c);
 }
 
 }  // namespace mph

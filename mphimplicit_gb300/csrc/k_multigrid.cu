@@ -465,16 +465,6 @@ void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
         vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
 }
 
-// FP32 V-cycle with FP64 vectors in and out (the mixed form's FP64-vector CR)
-void vcycle_mixed(mph_case* c, const double* q, double* u, double* dot_out)
-{
-    DeviceState& d = c->d;
-    if (c->dim == 2)
-        vcycle_t<2, float, double>(c, q, u, d.invDiag, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
-    else
-        vcycle_t<3, float, double>(c, q, u, d.invDiag, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
-}
-
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)
 {
     DeviceState& d = c->d;

@@ -109,14 +109,6 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->inner_blocks = value != 0.0;
         return MPH_OK;
     }
-    if (std::string(name) == "vectors64") {
-        c->vectors64 = value != 0.0;
-        return MPH_OK;
-    }
-    if (std::string(name) == "vcycle64") {
-        c->vcycle64 = value != 0.0;
-        return MPH_OK;
-    }
     return mph::fail(MPH_ERR_ARG, std::string("unknown option: ") + name);
 }
 

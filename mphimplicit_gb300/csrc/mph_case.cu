@@ -170,6 +170,31 @@ static int derive(mph_case* c, const mph_particles* parts)
     for (int t = 0; t < kTypeCount; ++t) {
         P.inert32[t] = (float)(P.density[t] * P.vol / P.vol / P.dt);
         P.lambda32[t] = (float)P.lambda[t];
+        for (int u = 0; u < kTypeCount; ++u) P.vm32[t][u] = (float)(P.visc * P.muij[t][u]);
+    }
+    P.wdA32 = (float)(-P.kfv * P.m2h_rv);
+    P.inv_rv32 = (float)P.inv_rv;
+    P.rV2_32 = (float)(P.rV * P.rV);
+    // size of the viscous part of a row of A against its inertia rho/dt: the
+    // sum of the pair coefficients f over the lattice within RadiusV (largest
+    // viscosity, smallest density), with a factor 4 for compressed packings
+    {
+        double mu_max = 0.0, rho_min = 1.0e300;
+        for (int t = 0; t < kTypeCount; ++t) {
+            mu_max = std::max(mu_max, std::fabs(P.mu[t]));
+            if (P.density[t] > 0.0) rho_min = std::min(rho_min, P.density[t]);
+        }
+        const int range = (int)std::ceil(P.rV / l0);
+        const int rz = two_d ? 0 : range;
+        double fsum = 0.0;
+        for (int ix = -range; ix <= range; ++ix)
+            for (int iy = -range; iy <= range; ++iy)
+                for (int iz = -rz; iz <= rz; ++iz) {
+                    if (ix == 0 && iy == 0 && iz == 0) continue;
+                    const double r = l0 * std::sqrt((double)(ix * ix + iy * iy + iz * iz));
+                    if (r < P.rV) fsum += P.visc * mu_max * P.kfv * (2.0 / P.rV) * (1.0 - r / P.rV) / r;
+                }
+        c->visc_ratio = 4.0 * fsum / (rho_min / P.dt);
     }
     // walls (initializeWall main.cpp:1023-1062; theta = |omega|^2 as written there)
     for (int t = 0; t < 4; ++t)
@@ -609,7 +634,7 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags,
-                    (void*)d.mg_invd32, (void*)d.pe, (void*)d.pe32, (void*)d.tct, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, (void*)d.v64, d.scan_tmp})
+                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

@@ -57,6 +57,8 @@ struct DevParams {
     float w32[3], hw32[3];
     float inert32[kTypeCount];                 // FP32 density/dt and bulk viscosity (mixed-form kernels)
     float lambda32[kTypeCount];
+    float vm32[kTypeCount][kTypeCount];        // FP32 visc * muij, -kfv * m2h_rv, 1/h, rV^2 (pair terms)
+    float wdA32, inv_rv32, rV2_32;
     int exact_only;                            // 1: skip the FP32 pre-classification
     int surface;                               // 1 if any CofA != 0
 };
@@ -108,11 +110,11 @@ struct DeviceState {
     int* dmax = nullptr;
     long long cap_ct_cnt = 0, cap_ct_ptr = 0, cap_ct_j = 0, cap_ct_v = 0, cap_cell_flags = 0;
     // mixed form, factored FP64 operator: (e, f) per neighbour slot of the
-    // fluid rows in FP64 and FP32, and t = C^T x per particle
-    double4* pe = nullptr;
+    // fluid rows in FP32, t = C^T x per particle, FP32 copy of x
     float4* pe32 = nullptr;
     long long cap_pairs = 0;
     double* tct = nullptr;
+    float* x32 = nullptr;
     float* ct_v32 = nullptr;        // FP32 copy of ct_v
     long long cap_ct_v32 = 0;
     float* cval32 = nullptr;        // FP32 copy of the fluid rows' C values
@@ -124,7 +126,6 @@ struct DeviceState {
     float *mg_cof32 = nullptr, *mg_invd32 = nullptr;
     float *mg_q32 = nullptr, *mg_s32 = nullptr, *mg_r32 = nullptr, *mg_res32 = nullptr;
     float* v32 = nullptr;           // mixed form: 7 FP32 CR vectors + FP32 D^-1, each D*Nf
-    double* v64 = nullptr;          // mixed form with FP64 CR vectors: 7 vectors, each D*Nf
     long long cap_mg_cof = 0, cap_mg_vec = 0, cap_mg_cof32 = 0, cap_mg_vec32 = 0;
     // solver vectors [D*Nf]
     double *x = nullptr, *r = nullptr, *s = nullptr, *y = nullptr, *p = nullptr, *q = nullptr, *u = nullptr;
@@ -185,13 +186,12 @@ struct mph_case {
     mph_solve_stats stats{};
     int iter_cap = 0;
     double tol_outer = 1.0e-6;          // ||b - A x|| / ||b|| stop (the reference's rr/rr0 < 1e-12)
+    double visc_ratio = 0.0;            // bound of |viscous part| / |inertia| of A (host estimate)
     double tol_inner = 1.0e-3;          // mixed form: inner relative reduction
     int max_outer = 50;                 // mixed form: refinement steps
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
-    bool vectors64 = false;             // mixed form: FP64 CR vectors around the FP32 operators
-    bool vcycle64 = false;              // with vectors64: FP64 V-cycle (only the SpMV in FP32)
     bool step_factored = false;         // this step's system uses the factored form
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
@@ -283,7 +283,7 @@ int build_ct(mph_case* c);
 bool factored_applies(const mph_case* c);
 int launch_pair_terms(mph_case* c);
 void launch_resid_factored(mph_case* c, const double* x, double* r, double* out);
-void launch_apply32(mph_case* c, const float* x, float* y, int cap, double tol2);
+void launch_apply32(mph_case* c, const float* x, float* y, int cap);
 void launch_mg_level0(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);

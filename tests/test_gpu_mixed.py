@@ -28,8 +28,8 @@ def oracle_residual(ptr, ind, val, b, x):
 
 
 # (factored FP64 operator, inner SpMV on assembled FP32 blocks)
-MODES = [(1, 0), (1, 1), (0, 0)]
-MODE_IDS = ["factored", "factored-blocks", "assembled"]
+MODES = [(1, 1), (1, 0), (0, 0)]
+MODE_IDS = ["factored", "factored-pair-terms", "assembled"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
