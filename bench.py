@@ -8,8 +8,12 @@ z, dt = 5e-5 s, lambda*dt/(rho*l0^2) = 100, seeded +-0.01 l0 jitter:
 files.  One step = the full reference step (sort, neighbours, explicit
 physics, assembly, multigrid build, CR solve).
 
-  value : particle-steps/s with the state resident in HBM, CUDA events on the
-          case stream around K steps (the matrix alone is ~14 GB, far above L2)
+  value : particle-steps/s of the mixed form (FP32 CR + V-cycle, FP64 outer
+          residual; --precision fp64 for the plain form) with the state
+          resident in HBM, CUDA events on the case stream around K steps (the
+          matrix alone is ~7 GB, far above L2); the line also carries the
+          plain FP64 form's value on the same workload and the velocity
+          difference of one step of each form from the same state
   e2e   : the same metric through the public API with host buffers: every
           step uploads the particle state (mph_case_set_state) and reads back
           positions and velocities (mph_get_fields)
@@ -397,7 +401,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cube3d_100")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--inner-tol", type=float, default=1e-3,
                     help="mixed form: relative residual reduction of each FP32 inner solve")
     ap.add_argument("--e2e-steps", type=int, default=2)
