@@ -407,6 +407,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-factored", action="store_true",
                     help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
+    ap.add_argument("--extra-sweeps", type=int, default=0, help="mixed form: extra level-0 smoothing sweeps")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
@@ -450,6 +451,7 @@ def main():
     if prec == PRECISION_MIXED:
         case.set_solver(args.outer_tol, args.inner_tol, 50)
         case.set_option("factored", 0 if args.no_factored else 1)
+        case.set_option("mixed_extra_sweeps", args.extra_sweeps)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)

@@ -119,6 +119,18 @@ int mph_write_prof(const char* path, const mph_particles* parts);
 int mph_case_write_vtk(mph_case* c, const char* path);
 int mph_case_write_prof(mph_case* c, const char* path);
 
+/* Full-precision checkpoint sidecar beside the .prof frames (which keep 7
+ * digits, main.cpp:696-720): count, time, spacing, domain, the wall centres
+ * (main.cpp:2123-2127) and per particle id, type, position and velocity in
+ * binary.  mph_case_checkpoint stores a case in its current particle order;
+ * a case created from the file (ids included) and given its order, wall
+ * centres and time with mph_case_set_state continues bit for bit.
+ * mph_read_checkpoint works like mph_read_grid: first call with NULL buffers
+ * for the count; wall_center receives 4x3 doubles. */
+int mph_write_checkpoint(const char* path, const mph_particles* parts, const double* wall_center);
+int mph_read_checkpoint(const char* path, mph_particles* out, double* wall_center);
+int mph_case_checkpoint(mph_case* c, const char* path);
+
 /* ---- case lifetime ----
  * mph_case_create replaces readGridFile's allocation + initializeWeight /
  * initializeFluid / initializeWall / initializeDomain and the initial
@@ -172,7 +184,10 @@ typedef struct mph_server_stats {
     long long steps;
     double particle_steps, elapsed_s;
 } mph_server_stats;
-int mph_server_create(long long budget_bytes, int workers, mph_server** out);
+/* device: the CUDA device the server's cases live on (< 0: the current one);
+ * one server per device makes the replicas of a multi-GPU node (host-side
+ * assignment, no collective: serving.ReplicaDispatcher). */
+int mph_server_create(long long budget_bytes, int workers, int device, mph_server** out);
 /* out: fields to fill at completion (NULL: none); step_ms: `steps` floats
  * receiving each step's host-measured latency (NULL: none). */
 int mph_server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision,
@@ -203,6 +218,8 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
  *   form (viscous pair terms + C Lambda C^T through the transposed P-lists)
  *   and only FP32 blocks are assembled; CsrCofA then exports the FP32 blocks.
  *   0: FP64 blocks are assembled and copied to FP32.
+ *   "mixed_extra_sweeps" 0 (default) .. 8: mixed form only, extra level-0
+ *   smoothing sweeps before and after the rest of its V-cycle.
  *   "inner_blocks" 1 (default) / 0: factored mixed form only.  0: the inner
  *   FP32 SpMV runs on the FP32 pair terms and no blocks are written
  *   (CsrIndA / CsrCofA exports then fail with MPH_ERR_STATE). */

@@ -36,10 +36,10 @@ __global__ void k_ct_count(int Nf, const int* __restrict__ ncp, const long long*
     for (int a = 0; a < ncp[i]; ++a) atomicAdd(&cnt[nindP[b + a]], 1);
 }
 
-template <int D>
+// column entries in arrival order: row j, column k and the entry's P-list slot
 __global__ void k_ct_fill(int Nf, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
-                          const int* __restrict__ nindP, const double* __restrict__ cval, const long long* __restrict__ ctptr,
-                          int* __restrict__ cur, int* __restrict__ ct_j, double* __restrict__ ct_v)
+                          const int* __restrict__ nindP, const long long* __restrict__ ctptr, int* __restrict__ cur,
+                          int3* __restrict__ tmp)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nf) return;
@@ -47,35 +47,26 @@ __global__ void k_ct_fill(int Nf, const int* __restrict__ ncp, const long long* 
     for (int a = 0; a < ncp[i]; ++a) {
         const int k = nindP[b + a];
         const long long e = ctptr[k] + atomicAdd(&cur[k], 1);
-        ct_j[e] = i;
-#pragma unroll
-        for (int r = 0; r < D; ++r) ct_v[e * D + r] = cval[(b + a) * D + r];
+        tmp[e] = make_int3(i, k, (int)(b + a));
     }
 }
 
-// sort every column by row index (insertion sort: columns hold ~|P| entries)
+// every entry finds its place in its column (rows ascending: its rank among
+// the column's rows, which are distinct) and copies its C values there
 template <int D>
-__global__ void k_ct_sort(int N, const long long* __restrict__ ctptr, int* __restrict__ ct_j, double* __restrict__ ct_v)
+__global__ void k_ct_place(long long total, const long long* __restrict__ ctptr, const int3* __restrict__ tmp,
+                           const double* __restrict__ cval, int* __restrict__ ct_j, double* __restrict__ ct_v)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= N) return;
-    const long long e0 = ctptr[k], e1 = ctptr[k + 1];
-    for (long long e = e0 + 1; e < e1; ++e) {
-        const int j = ct_j[e];
-        double v[3];
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int3 t = tmp[e];
+    const long long e0 = ctptr[t.y], e1 = ctptr[t.y + 1];
+    int rank = 0;
+    for (long long f = e0; f < e1; ++f) rank += tmp[f].x < t.x;
+    const long long d = e0 + rank;
+    ct_j[d] = t.x;
 #pragma unroll
-        for (int r = 0; r < D; ++r) v[r] = ct_v[e * D + r];
-        long long f = e - 1;
-        while (f >= e0 && ct_j[f] > j) {
-            ct_j[f + 1] = ct_j[f];
-#pragma unroll
-            for (int r = 0; r < D; ++r) ct_v[(f + 1) * D + r] = ct_v[f * D + r];
-            --f;
-        }
-        ct_j[f + 1] = j;
-#pragma unroll
-        for (int r = 0; r < D; ++r) ct_v[(f + 1) * D + r] = v[r];
-    }
+    for (int r = 0; r < D; ++r) ct_v[d * D + r] = cval[(long long)t.z * D + r];
 }
 
 __global__ void k_to_f32(long long n, const double* __restrict__ a, float* __restrict__ b)
@@ -108,7 +99,8 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
                  const long long* __restrict__ sptr, int* __restrict__ acol, double* __restrict__ aval,
                  float* __restrict__ aval32, double* __restrict__ bvec, double* __restrict__ invDiag,
                  int* __restrict__ selfk_out, double* __restrict__ part, int* __restrict__ overflow,
-                 const float4* __restrict__ pe32, const float* __restrict__ ct_v32, const float* __restrict__ cval32)
+                 const float4* __restrict__ pe32, const float* __restrict__ ct_v32, const float* __restrict__ cval32,
+                 float* __restrict__ arow32)
 {
     using T = typename std::conditional<MIX, float, double>::type;
     constexpr int DD = D * D;
@@ -251,20 +243,41 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
             const bool fluid = k < nf;
             double vj[3];
             if (!fluid) load_vec<D>(vel, j, vj);
+            // the block f e (x) e is symmetric: the upper triangle is formed once
+            // (f e_r first, then times e_s) and mirrored
+            double fe[3];
+#pragma unroll
+            for (int r = 0; r < D; ++r) fe[r] = f * e[r];
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int s = 0; s < D; ++s) {
-                    const double coef = f * e[s] * e[r];
+                for (int s = r; s < D; ++s) {
+                    const double coef = fe[r] * e[s];
                     selfc[r * D + s] += (T)coef;
-                    if (fluid) acc[k * DD + r * D + s] = (T)-coef;
-                    else sumv[r] += coef * vj[s];
+                    if (fluid) {
+                        acc[k * DD + r * D + s] = (T)-coef;
+                        if (s != r) acc[k * DD + s * D + r] = (T)-coef;
+                    } else {
+                        sumv[r] += coef * vj[s];
+                        if (s != r) sumv[s] += coef * vj[r];
+                    }
                 }
         }
+        // warp sums of the upper triangle, mirrored (the FP32 form sums all entries)
 #pragma unroll
-        for (int t = 0; t < DD; ++t)
+        for (int r = 0; r < D; ++r)
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) selfc[t] += __shfl_xor_sync(0xffffffffu, selfc[t], o);
+            for (int s = 0; s < D; ++s) {
+                if (!MIX && s < r) continue;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) selfc[r * D + s] += __shfl_xor_sync(0xffffffffu, selfc[r * D + s], o);
+            }
+        if (!MIX) {
+#pragma unroll
+            for (int r = 1; r < D; ++r)
+#pragma unroll
+                for (int s = 0; s < r; ++s) selfc[r * D + s] = selfc[s * D + r];
+        }
 #pragma unroll
         for (int r = 0; r < D; ++r)
 #pragma unroll
@@ -284,6 +297,12 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
         // sliced-ELL write-out of the row's blocks (the FP32 form writes them
         // only when its inner SpMV uses them)
         auto write_blocks = [&]() {
+            if (MIX) {   // row-contiguous, coalesced; k_rows_to_slices builds the sliced layout
+                float* dst = arow32 + nb * DD;
+                for (int t = lane; t < nf * DD; t += 32) dst[t] = (float)acc[t];
+                __syncwarp();
+                return;
+            }
             const long long sb = sptr[i >> 5];
             const int ln = i & 31;
             for (int t = lane; t < nf * DD; t += 32) {
@@ -369,6 +388,59 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
     }
 }
 
+// ---- row-contiguous FP32 blocks -> sliced ELL --------------------------------------
+// One block per slice of 32 rows: chunks of kRtsK block columns of the 32 rows
+// are read row by row (coalesced) into shared memory and written in the
+// sliced layout (coalesced), together with the block columns from the
+// neighbour lists; padding slots are written as zeros so every sector is
+// written whole.
+constexpr int kRtsK = 16;
+
+template <int D>
+__global__ void __launch_bounds__(256) k_rows_to_slices(int Nf, const long long* __restrict__ sptr, const int* __restrict__ nfc, const long long* __restrict__ nptr,
+                                                        const int* __restrict__ nind, const float* __restrict__ arow32,
+                                                        int* __restrict__ acol, float* __restrict__ aval32)
+{
+    constexpr int DD = D * D;
+    constexpr int W = kRtsK * DD + 1;          // odd row stride: no bank conflicts
+    __shared__ float tile[32 * W];
+    __shared__ int ctile[32 * (kRtsK + 1)];
+    __shared__ int rn[32];
+    __shared__ long long rb[32];
+    const int sl = blockIdx.x;
+    const int r0 = sl * 32;
+    if (threadIdx.x < 32) {
+        const int i = r0 + threadIdx.x;
+        rn[threadIdx.x] = i < Nf ? nfc[i] : 0;
+        rb[threadIdx.x] = i < Nf ? nptr[i] : 0;
+    }
+    __syncthreads();
+    const long long sb = sptr[sl];
+    const int w = (int)((sptr[sl + 1] - sb) / 32);   // block columns of the slice (its slots / 32 rows)
+    for (int k0 = 0; k0 < w; k0 += kRtsK) {
+        const int kc = min(kRtsK, w - k0);
+        for (int t = threadIdx.x; t < 32 * kRtsK * DD; t += blockDim.x) {
+            const int r = t / (kRtsK * DD), e = t % (kRtsK * DD);
+            const int k = k0 + e / DD;
+            tile[r * W + e] = (e < kc * DD && k < rn[r]) ? arow32[(rb[r] + k0) * DD + e] : 0.f;
+        }
+        for (int t = threadIdx.x; t < 32 * kRtsK; t += blockDim.x) {
+            const int r = t / kRtsK, e = t % kRtsK;
+            ctile[r * (kRtsK + 1) + e] = (e < kc && k0 + e < rn[r]) ? nind[rb[r] + k0 + e] : 0;
+        }
+        __syncthreads();
+        for (int o = threadIdx.x; o < kc * DD * 32; o += blockDim.x) {
+            const int ln = o & 31, ec = o >> 5;                    // ec = k_local*DD + comp
+            aval32[sb * DD + (long long)k0 * DD * 32 + o] = tile[ln * W + ec];
+        }
+        for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+            const int ln = o & 31, kl = o >> 5;
+            acol[sb + (long long)(k0 + kl) * 32 + ln] = ctile[ln * (kRtsK + 1) + kl];
+        }
+        __syncthreads();
+    }
+}
+
 // ---- launcher ---------------------------------------------------------------------
 static int grow_bytes(void** p, long long* cap, long long need)
 {
@@ -399,17 +471,17 @@ int build_ct(mph_case* c)
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     MPH_TRY(grow_bytes((void**)&dv.ct_j, &dv.cap_ct_j, tot * (long long)sizeof(int)));
     MPH_TRY(grow_bytes((void**)&dv.ct_v, &dv.cap_ct_v, tot * D * (long long)sizeof(double)));
+    MPH_TRY(grow_bytes((void**)&dv.ct_tmp, &dv.cap_ct_tmp, tot * (long long)sizeof(int3)));
     int* cnt = dv.ct_cnt;
     int* cur = dv.ct_cnt + (N + 1);
     const unsigned gf = grid_for(Nf, 256);
     { k_ct_count<<<gf, 256, 0, c->stream>>>(Nf, dv.ncp, dv.nptrP, dv.nindP, cnt); MPH_COUNT_LAUNCH(); }
     MPH_TRY(launch_scan_i32_to_i64(c, cnt, dv.ct_ptr, N));
+    { k_ct_fill<<<gf, 256, 0, c->stream>>>(Nf, dv.ncp, dv.nptrP, dv.nindP, dv.ct_ptr, cur, (int3*)dv.ct_tmp); MPH_COUNT_LAUNCH(); }
     if (D == 2) {
-        { k_ct_fill<2><<<gf, 256, 0, c->stream>>>(Nf, dv.ncp, dv.nptrP, dv.nindP, dv.cval, dv.ct_ptr, cur, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
-        { k_ct_sort<2><<<grid_for(N, 256), 256, 0, c->stream>>>(N, dv.ct_ptr, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
+        { k_ct_place<2><<<grid_for(tot, 256), 256, 0, c->stream>>>(tot, dv.ct_ptr, (const int3*)dv.ct_tmp, dv.cval, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_fill<3><<<gf, 256, 0, c->stream>>>(Nf, dv.ncp, dv.nptrP, dv.nindP, dv.cval, dv.ct_ptr, cur, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
-        { k_ct_sort<3><<<grid_for(N, 256), 256, 0, c->stream>>>(N, dv.ct_ptr, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
+        { k_ct_place<3><<<grid_for(tot, 256), 256, 0, c->stream>>>(tot, dv.ct_ptr, (const int3*)dv.ct_tmp, dv.cval, dv.ct_j, dv.ct_v); MPH_COUNT_LAUNCH(); }
     }
     if (c->step_factored) {   // FP32 copy for the FP32 cell-block kernel
         MPH_TRY(grow_bytes((void**)&dv.ct_v32, &dv.cap_ct_v32, tot * D * (long long)sizeof(float)));
@@ -451,18 +523,34 @@ int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done)
     // FP32 blocks: the mixed form's copy, except when its inner SpMV runs on the
     // pair terms (factored form without inner_blocks)
     float* a32 = c->precision == MPH_PRECISION_MIXED && !(mix && !c->inner_blocks) ? dv.aval32 : nullptr;
+    if (mix && a32) {   // FP32 blocks go through the row-contiguous buffer
+        long long slots = 0;
+        MPH_CUDA(cudaMemcpyAsync(&slots, dv.nptr + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+        MPH_CUDA(cudaStreamSynchronize(c->stream));
+        MPH_TRY(grow_bytes((void**)&dv.arow32, &dv.cap_arow32, slots * D * D * (long long)sizeof(float)));
+    }
     auto go = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<P.T, kAsmWarps * 32, smem, c->stream>>>(
             P, M, r[0], r[1], r[2], mwords, kmax, dv.type, dv.bucket, dv.pos, dv.vel, dv.nc, dv.nfc, dv.nptr, dv.nind, dv.ncp,
             dv.nptrP, dv.nindP, dv.cval, dv.pvec, dv.ct_ptr, dv.ct_j, dv.ct_v, dv.sptr, dv.acol, dv.aval, a32, dv.bvec,
-            dv.invDiag, dv.selfk, dv.part, dv.cell_flags, dv.pe32, dv.ct_v32, dv.cval32);
+            dv.invDiag, dv.selfk, dv.part, dv.cell_flags, dv.pe32, dv.ct_v32, dv.cval32, dv.arow32);
         MPH_COUNT_LAUNCH();
     };
     if (D == 2) {
         if (mix) go(k_assemble_cells<2, true>); else go(k_assemble_cells<2, false>);
     } else {
         if (mix) go(k_assemble_cells<3, true>); else go(k_assemble_cells<3, false>);
+    }
+    if (mix && a32) {
+        if (D == 2) {
+            k_rows_to_slices<2><<<c->nslices, 256, 0, c->stream>>>(P.Nf, dv.sptr, dv.nfc, dv.nptr, dv.nind, dv.arow32,
+                                                                   dv.acol, a32);
+        } else {
+            k_rows_to_slices<3><<<c->nslices, 256, 0, c->stream>>>(P.Nf, dv.sptr, dv.nfc, dv.nptr, dv.nind, dv.arow32,
+                                                                   dv.acol, a32);
+        }
+        MPH_COUNT_LAUNCH();
     }
     *done = true;
     return MPH_OK;

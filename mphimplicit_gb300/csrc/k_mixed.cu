@@ -59,14 +59,15 @@ __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ 
         const int n = nfc[i];
 #pragma unroll 4
         for (int k = 0; k < n; ++k) {
-            const int col = cp[(long long)k * 32];
+            // the blocks stream through once (evict-first), leaving L1 to the x gathers
+            const int col = __ldcs(cp + (long long)k * 32);
             float xv[3];
 #pragma unroll
             for (int s = 0; s < D; ++s) xv[s] = (float)xin[(size_t)col * D + s];
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int s = 0; s < D; ++s) y[r] += vp[((long long)k * DD + r * D + s) * 32] * xv[s];
+                for (int s = 0; s < D; ++s) y[r] += __ldcs(vp + ((long long)k * DD + r * D + s) * 32) * xv[s];
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {

@@ -337,39 +337,69 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
     T* cur[kMaxLevels];
     T* oth[kMaxLevels];
     for (int l = A.first; l < A.depth; ++l) { cur[l] = A.Sa[l]; oth[l] = A.Sb[l]; }
-    auto jacobi = [&](int l) {
+    // levels from `narrow` on have at most one row per thread of a block:
+    // block 0 runs them alone, with block barriers instead of cluster ones
+    int narrow = A.depth;
+    for (int l = A.first; l < A.depth; ++l)
+        if (A.L[l].rows <= (int)blockDim.x) { narrow = l; break; }
+    auto csync = [&]() { cluster.sync(); };
+    auto bsync = [&]() { __syncthreads(); };
+    // one smoothing sweep of level l over rows t0, t0 + nt, ...
+    auto jacobi = [&](int l, int t0, int nt, auto sync) {
         const LevelK& L = A.L[l];
-        for (int row = tid; row < L.rows; row += nth) {
+        for (int row = t0; row < L.rows; row += nt) {
             const T r = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
             oth[l][row] = cur[l][row] + A.invd[l][row] * r;
         }
-        cluster.sync();
+        sync();
         T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
     };
-    // down: restriction + pre-smoothing (3 updates, the coarsest 5)
-    for (int l = A.first; l < A.depth; ++l) {
+    // restriction into level l, pre-smoothing (3 updates, the coarsest 5), residual
+    auto down = [&](int l, int t0, int nt, auto sync) {
         const LevelK& L = A.L[l];
-        for (int row = tid; row < L.rows; row += nth) {
+        for (int row = t0; row < L.rows; row += nt) {
             const T q = row_restrict<D, T>(A.L[l - 1], L, A.R[l - 1], row);
             A.Q[l][row] = q;
             cur[l][row] = A.invd[l][row] * q;
         }
-        cluster.sync();
+        sync();
         const int sweeps = (l == A.depth - 1) ? 4 : 2;
-        for (int k = 0; k < sweeps; ++k) jacobi(l);
+        for (int k = 0; k < sweeps; ++k) jacobi(l, t0, nt, sync);
         if (l < A.depth - 1) {
-            for (int row = tid; row < L.rows; row += nth)
-                A.R[l][row] = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
-            cluster.sync();
+            for (int row = t0; row < L.rows; row += nt) A.R[l][row] = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
+            sync();
+        }
+    };
+    // prolongation of level l into level l-1 (S_{l-1} += P S_l)
+    auto prolong = [&](int l, int t0, int nt) {
+        const LevelK& S_ = A.L[l - 1];
+        for (int row = t0; row < S_.rows; row += nt) cur[l - 1][row] = cur[l - 1][row] + cur[l][row_parent<D>(S_, A.L[l], row)];
+    };
+    for (int l = A.first; l < narrow; ++l) down(l, tid, nth, csync);
+    if (cluster.block_rank() == 0 && narrow < A.depth) {
+        const int t0 = threadIdx.x, nt = blockDim.x;
+        for (int l = narrow; l < A.depth; ++l) down(l, t0, nt, bsync);
+        for (int l = A.depth - 1; l > narrow; --l) {
+            prolong(l, t0, nt);
+            bsync();
+            for (int k = 0; k < 3; ++k) jacobi(l - 1, t0, nt, bsync);   // post-smoothing (3 updates)
+        }
+        if (narrow > A.first) {
+            prolong(narrow, t0, nt);
+        } else {   // every small level is narrow: block 0 also prolongates into the finer level
+            const LevelK& S_ = A.L[A.first - 1];
+            for (int row = t0; row < S_.rows; row += nt)
+                A.Sfine[row] = A.Sfine[row] + cur[A.first][row_parent<D>(S_, A.L[A.first], row)];
         }
     }
-    // up: prolongation + post-smoothing (3 updates)
-    for (int l = A.depth - 1; l > A.first; --l) {
-        const LevelK& S_ = A.L[l - 1];
-        for (int row = tid; row < S_.rows; row += nth)
-            cur[l - 1][row] = cur[l - 1][row] + cur[l][row_parent<D>(S_, A.L[l], row)];
-        cluster.sync();
-        for (int k = 0; k < 3; ++k) jacobi(l - 1);
+    if (narrow == A.first) return;   // done by block 0 (whose pointer swaps the others do not know)
+    csync();
+    for (int l = min(narrow, A.depth - 1); l > A.first; --l) {
+        if (l < narrow) {
+            prolong(l, tid, nth);
+            csync();
+        }
+        for (int k = 0; k < 3; ++k) jacobi(l - 1, tid, nth, csync);
     }
     // prolongation into the finer, grid-wide level
     const LevelK& S_ = A.L[A.first - 1];
@@ -380,7 +410,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
 // ---- host-side V-cycle -----------------------------------------------------------
 template <int D, typename T, typename TQ>
 static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T* cof, const T* invd, T* Qp, T* Sa, T* Sb,
-                     T* Rp, double* dot_out)
+                     T* Rp, double* dot_out, int extra0 = 0)
 {
     const int depth = c->depth;
     cudaStream_t st = c->stream;
@@ -407,7 +437,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     // down, grid-wide levels
     { k_mg_p2g<D, T, TQ><<<grid_for(L[0].rows, 128), 128, 0, st>>>(c->dp, L[0], c->d.bucket, q, invd + ov(0), Qp + ov(0),
                                                                    cur[0], flags); MPH_COUNT_LAUNCH(); }
-    jacobi(0);                                            // level 0: 2 updates
+    for (int k = 0; k < 1 + extra0; ++k) jacobi(0);      // level 0: 2 updates (+ extra0)
     for (int l = 1; l < first; ++l) {
         residual(l - 1);
         { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], Rp + ov(l - 1), invd + ov(l), Qp + ov(l),
@@ -446,7 +476,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         for (int k = 0; k < 3; ++k) jacobi(l);
         prolong(l);
     }
-    for (int k = 0; k < 2; ++k) jacobi(0);               // level 0 post-smoothing
+    for (int k = 0; k < 2 + extra0; ++k) jacobi(0);      // level 0 post-smoothing
     const int n = c->dp.Nf * D;
     const int blocks = std::min<int>(grid_for(n, 256), kReduceBlocks);
     { k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
@@ -460,9 +490,11 @@ void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
     DeviceState& d = c->d;
     const float* invDiag32 = d.v32 + 7 * (size_t)c->dp.Nf * c->dim;
     if (c->dim == 2)
-        vcycle_t<2, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
+        vcycle_t<2, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out,
+                                  c->mixed_extra_sweeps);
     else
-        vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out);
+        vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out,
+                                  c->mixed_extra_sweeps);
 }
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)

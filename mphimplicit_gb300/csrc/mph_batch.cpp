@@ -59,7 +59,10 @@ int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, i
     b += (double)N * (nb + np) * 4.0 + (double)N * 32.0;      // neighbour lists and row pointers
     const double blocks = 1.10 * (double)Nf * nb;             // A, with slice padding
     b += blocks * (DD * 8.0 + 4.0);
-    if (precision == MPH_PRECISION_MIXED) b += blocks * DD * 4.0;
+    if (precision == MPH_PRECISION_MIXED) {
+        b += 2.0 * blocks * DD * 4.0;                         // FP32 blocks, sliced and row-contiguous
+        b += (double)Nf * nb * 16.0;                          // FP32 pair terms
+    }
     b += (double)Nf * np * (D * 8.0) * 2.0;                   // C and its transpose values
     b += (double)Nf * np * 4.0 * 2.0 + (double)N * 24.0;      // transpose indices and pointers
     b += (double)Nf * S * DD * 8.0;                           // level-0 stencils
@@ -260,12 +263,13 @@ struct mph_server {
 
 namespace mph {
 
-int server_create(long long budget, int workers, mph_server** out)
+int server_create(long long budget, int workers, int device, mph_server** out)
 {
     if (!out || budget <= 0) return fail(MPH_ERR_ARG, "server needs an output handle and a positive budget");
     *out = nullptr;
     auto* s = new mph_server();
-    cudaGetDevice(&s->device);
+    if (device >= 0) s->device = device;
+    else cudaGetDevice(&s->device);
     s->budget = budget;
     const int nw = workers > 0 ? workers : 16;
     for (int w = 0; w < nw; ++w) s->workers.emplace_back([s] { s->worker(); });

@@ -12,6 +12,9 @@ int read_grid(const char* path, mph_particles* o);
 int write_prof(const char* path, const mph_particles* p);
 int case_write_prof(mph_case* c, const char* path);
 int case_write_vtk(mph_case* c, const char* path);
+int write_checkpoint(const char* path, const mph_particles* p, const double* wall_center);
+int read_checkpoint(const char* path, mph_particles* p, double* wall_center);
+int case_checkpoint(mph_case* c, const char* path);
 }  // namespace mph
 
 #define GUARD(expr)                                                              \
@@ -34,6 +37,15 @@ int mph_read_grid(const char* path, mph_particles* out) { GUARD(mph::read_grid(p
 int mph_write_prof(const char* path, const mph_particles* parts) { GUARD(mph::write_prof(path, parts)) }
 int mph_case_write_vtk(mph_case* c, const char* path) { NEED(c); GUARD(mph::case_write_vtk(c, path)) }
 int mph_case_write_prof(mph_case* c, const char* path) { NEED(c); GUARD(mph::case_write_prof(c, path)) }
+int mph_write_checkpoint(const char* path, const mph_particles* parts, const double* wall_center)
+{
+    GUARD(mph::write_checkpoint(path, parts, wall_center))
+}
+int mph_read_checkpoint(const char* path, mph_particles* out, double* wall_center)
+{
+    GUARD(mph::read_checkpoint(path, out, wall_center))
+}
+int mph_case_checkpoint(mph_case* c, const char* path) { NEED(c); GUARD(mph::case_checkpoint(c, path)) }
 
 int mph_case_create(const mph_params* prm, const mph_particles* parts, int dim, int precision, void* stream, mph_case** out)
 {
@@ -63,7 +75,10 @@ int mph_case_footprint(const mph_params* prm, const mph_particles* parts, int di
 {
     GUARD(mph::case_footprint(prm, parts, dim, precision, bytes))
 }
-int mph_server_create(long long budget_bytes, int workers, mph_server** out) { GUARD(mph::server_create(budget_bytes, workers, out)) }
+int mph_server_create(long long budget_bytes, int workers, int device, mph_server** out)
+{
+    GUARD(mph::server_create(budget_bytes, workers, device, out))
+}
 int mph_server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision, int steps,
                       const mph_fields* out, float* step_ms, long long* ticket)
 {
@@ -107,6 +122,11 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
     }
     if (std::string(name) == "inner_blocks") {
         c->inner_blocks = value != 0.0;
+        return MPH_OK;
+    }
+    if (std::string(name) == "mixed_extra_sweeps") {
+        if (!(value >= 0.0 && value <= 8.0)) return mph::fail(MPH_ERR_ARG, "mixed_extra_sweeps must be 0..8");
+        c->mixed_extra_sweeps = (int)value;
         return MPH_OK;
     }
     return mph::fail(MPH_ERR_ARG, std::string("unknown option: ") + name);

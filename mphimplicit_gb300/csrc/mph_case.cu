@@ -231,6 +231,8 @@ static int derive(mph_case* c, const mph_particles* parts)
     for (int d = 0; d < 3; ++d) {
         P.dmin[d] = parts->domain_min[d];
         dmax[d] = parts->domain_max[d];
+        c->prm_domain_min[d] = parts->domain_min[d];
+        c->prm_domain_max[d] = parts->domain_max[d];
         P.dw[d] = dmax[d] - P.dmin[d];
         P.hw[d] = 0.5 * P.dw[d];
         P.wsafe[d] = 0.75 * P.dw[d];
@@ -633,8 +635,8 @@ int case_destroy(mph_case* c)
     for (void* p : {(void*)d.nind, (void*)d.nindP, (void*)d.acol, (void*)d.aval, (void*)d.aval32, (void*)d.cval,
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
-                    (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags,
-                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
+                    (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags, d.ct_tmp,
+                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

@@ -108,7 +108,8 @@ struct DeviceState {
     double* ct_v = nullptr;
     int* cell_flags = nullptr;
     int* dmax = nullptr;
-    long long cap_ct_cnt = 0, cap_ct_ptr = 0, cap_ct_j = 0, cap_ct_v = 0, cap_cell_flags = 0;
+    void* ct_tmp = nullptr;         // (row, column, P-slot) per entry before placement
+    long long cap_ct_cnt = 0, cap_ct_ptr = 0, cap_ct_j = 0, cap_ct_v = 0, cap_cell_flags = 0, cap_ct_tmp = 0;
     // mixed form, factored FP64 operator: (e, f) per neighbour slot of the
     // fluid rows in FP32, t = C^T x per particle, FP32 copy of x
     float4* pe32 = nullptr;
@@ -117,6 +118,8 @@ struct DeviceState {
     float* x32 = nullptr;
     float* ct_v32 = nullptr;        // FP32 copy of ct_v
     long long cap_ct_v32 = 0;
+    float* arow32 = nullptr;        // FP32 blocks, row-contiguous at neighbour-list offsets (before slicing)
+    long long cap_arow32 = 0;
     float* cval32 = nullptr;        // FP32 copy of the fluid rows' C values
     long long cap_cval32 = 0;
     float* tct32 = nullptr;         // t = C^T x of the FP32 inner operator
@@ -169,6 +172,7 @@ struct mph_case {
     mph::DevParams dp{};
     double time = 0.0;
     double z_plane = 0.0;               // z of every particle of a 2D case
+    double prm_domain_min[3]{}, prm_domain_max[3]{};   // the .grid header's domain
     double wallC[4][3]{}, wallV[4][3]{}, wallW[4][3]{}, wallR[4][3][3]{};
     double Swa = 1, Swg = 1, Swp = 1, Swv = 1;
     int fB = 0, fE = 0, wB = 0, wE = 0;
@@ -192,6 +196,7 @@ struct mph_case {
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
+    int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
@@ -238,7 +243,7 @@ int case_profile(mph_case* c, int enable);
 // batching and serving (mph_batch.cpp)
 int batch_step(mph_case** cases, int ncases, int nsteps, int workers);
 int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, int precision, long long* bytes);
-int server_create(long long budget, int workers, mph_server** out);
+int server_create(long long budget, int workers, int device, mph_server** out);
 int server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision, int steps,
                   const mph_fields* out, float* step_ms, long long* ticket);
 int server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count);

@@ -11,6 +11,7 @@
 //           (writeVtkFile, main.cpp:722-883)
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "mph_internal.h"
@@ -230,6 +231,121 @@ int case_write_vtk(mph_case* c, const char* path)
     std::fprintf(fp, "\n");
     std::fclose(fp);
     return MPH_OK;
+}
+
+// ---- full-precision checkpoint sidecar ------------------------------------------
+// The .prof frame keeps 7 significant digits (main.cpp:696-720); restarting a
+// run from it changes the result.  The sidecar keeps the state in binary:
+//   "MPHCKPT1", int32 count, double time, double spacing, double min[3],
+//   double max[3], double wall_center[4][3], int32 id[count], int32
+//   type[count], double pos[count][3], double vel[count][3]
+// (host byte order; both build hosts are little-endian).  A case restored
+// from it in the stored particle order continues bit for bit.
+static const char kCkptMagic[8] = {'M', 'P', 'H', 'C', 'K', 'P', 'T', '1'};
+
+int write_checkpoint(const char* path, const mph_particles* p, const double* wall_center)
+{
+    if (!path || !p || !p->type || !p->pos || !p->vel || p->count < 0) return fail(MPH_ERR_ARG, "null argument");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(MPH_ERR_IO, std::string("cannot open ") + path);
+    const int n = p->count;
+    std::vector<int> id(n);
+    for (int i = 0; i < n; ++i) id[i] = p->id ? p->id[i] : i;
+    double wc[12] = {0};
+    if (wall_center) std::memcpy(wc, wall_center, sizeof(wc));
+    bool ok = std::fwrite(kCkptMagic, 1, 8, f) == 8;
+    ok = ok && std::fwrite(&n, sizeof(int), 1, f) == 1;
+    ok = ok && std::fwrite(&p->time, sizeof(double), 1, f) == 1;
+    ok = ok && std::fwrite(&p->spacing, sizeof(double), 1, f) == 1;
+    ok = ok && std::fwrite(p->domain_min, sizeof(double), 3, f) == 3;
+    ok = ok && std::fwrite(p->domain_max, sizeof(double), 3, f) == 3;
+    ok = ok && std::fwrite(wc, sizeof(double), 12, f) == 12;
+    ok = ok && std::fwrite(id.data(), sizeof(int), (size_t)n, f) == (size_t)n;
+    ok = ok && std::fwrite(p->type, sizeof(int), (size_t)n, f) == (size_t)n;
+    ok = ok && std::fwrite(p->pos, sizeof(double), (size_t)n * 3, f) == (size_t)n * 3;
+    ok = ok && std::fwrite(p->vel, sizeof(double), (size_t)n * 3, f) == (size_t)n * 3;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MPH_OK : fail(MPH_ERR_IO, std::string("write failed: ") + path);
+}
+
+int read_checkpoint(const char* path, mph_particles* p, double* wall_center)
+{
+    if (!path || !p) return fail(MPH_ERR_ARG, "null argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(MPH_ERR_IO, std::string("cannot open ") + path);
+    char magic[8];
+    int n = -1;
+    double wc[12];
+    mph_particles h = *p;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCkptMagic, 8) == 0;
+    ok = ok && std::fread(&n, sizeof(int), 1, f) == 1 && n >= 0;
+    ok = ok && std::fread(&h.time, sizeof(double), 1, f) == 1;
+    ok = ok && std::fread(&h.spacing, sizeof(double), 1, f) == 1;
+    ok = ok && std::fread(h.domain_min, sizeof(double), 3, f) == 3;
+    ok = ok && std::fread(h.domain_max, sizeof(double), 3, f) == 3;
+    ok = ok && std::fread(wc, sizeof(double), 12, f) == 12;
+    if (!ok) {
+        std::fclose(f);
+        return fail(MPH_ERR_IO, std::string("not a checkpoint file: ") + path);
+    }
+    h.count = n;
+    if (!p->type || !p->pos || !p->vel) {   // first call: the count only
+        std::fclose(f);
+        *p = h;
+        p->type = nullptr;
+        p->pos = p->vel = nullptr;
+        p->id = nullptr;
+        return MPH_OK;
+    }
+    if (p->count < n) {
+        std::fclose(f);
+        return fail(MPH_ERR_ARG, "buffers smaller than the checkpoint's particle count");
+    }
+    std::vector<int> id(n);
+    ok = std::fread(id.data(), sizeof(int), (size_t)n, f) == (size_t)n;
+    ok = ok && std::fread(p->type, sizeof(int), (size_t)n, f) == (size_t)n;
+    ok = ok && std::fread(p->pos, sizeof(double), (size_t)n * 3, f) == (size_t)n * 3;
+    ok = ok && std::fread(p->vel, sizeof(double), (size_t)n * 3, f) == (size_t)n * 3;
+    std::fclose(f);
+    if (!ok) return fail(MPH_ERR_IO, std::string("checkpoint file is short: ") + path);
+    if (p->id) std::memcpy(p->id, id.data(), (size_t)n * sizeof(int));
+    int* type = p->type;
+    double *pos = p->pos, *vel = p->vel;
+    int* pid = p->id;
+    *p = h;
+    p->type = type;
+    p->pos = pos;
+    p->vel = vel;
+    p->id = pid;
+    if (wall_center) std::memcpy(wall_center, wc, sizeof(wc));
+    return MPH_OK;
+}
+
+int case_checkpoint(mph_case* c, const char* path)
+{
+    if (!c || !path) return fail(MPH_ERR_ARG, "null argument");
+    const int n = c->dp.N;
+    std::vector<int> id(n), type(n);
+    std::vector<double> pos((size_t)n * 3), vel((size_t)n * 3);
+    mph_fields f{};
+    f.id = id.data();
+    f.type = type.data();
+    f.pos = pos.data();
+    f.vel = vel.data();
+    MPH_TRY(case_get_fields(c, &f));
+    mph_particles p{};
+    p.count = n;
+    p.time = c->time;
+    p.spacing = c->dp.l0;
+    for (int d = 0; d < 3; ++d) {
+        p.domain_min[d] = c->prm_domain_min[d];
+        p.domain_max[d] = c->prm_domain_max[d];
+    }
+    p.type = type.data();
+    p.pos = pos.data();
+    p.vel = vel.data();
+    p.id = id.data();
+    return write_checkpoint(path, &p, &c->wallC[0][0]);
 }
 
 }  // namespace mph

@@ -45,6 +45,9 @@ def load_library(path: str = LIB_PATH):
         "mph_write_prof": ([cp, vp], ip),
         "mph_case_write_vtk": ([vp, cp], ip),
         "mph_case_write_prof": ([vp, cp], ip),
+        "mph_write_checkpoint": ([cp, vp, vp], ip),
+        "mph_read_checkpoint": ([cp, vp, vp], ip),
+        "mph_case_checkpoint": ([vp, cp], ip),
         "mph_case_create": ([vp, vp, ip, ip, vp, ctypes.POINTER(vp)], ip),
         "mph_case_destroy": ([vp], ip),
         "mph_case_set_stream": ([vp, vp], ip),
@@ -105,15 +108,44 @@ def read_grid(path: str) -> casegen.Particles:
     return casegen.Particles(s.time, s.spacing, np.array(s.domain_min[:]), np.array(s.domain_max[:]), types, pos, vel)
 
 
+def write_checkpoint(path: str, parts: casegen.Particles, ids: Optional[np.ndarray] = None,
+                     wall_center: Optional[np.ndarray] = None):
+    """Full-precision checkpoint sidecar of a particle state."""
+    ps = ParticlesC(parts, ids)
+    wc = None if wall_center is None else np.ascontiguousarray(wall_center, dtype=np.float64).reshape(-1)
+    _check(load_library().mph_write_checkpoint(path.encode(), ctypes.byref(ps.struct),
+                                               None if wc is None else wc.ctypes.data_as(ctypes.c_void_p)))
+
+
+def read_checkpoint(path: str):
+    """(particles, ids, wall_center[4][3]) of a checkpoint file."""
+    lib = load_library()
+    s = MphParticles()
+    _check(lib.mph_read_checkpoint(path.encode(), ctypes.byref(s), None))
+    n = s.count
+    types = np.zeros(n, np.int32)
+    ids = np.zeros(n, np.int32)
+    pos = np.zeros((n, 3))
+    vel = np.zeros((n, 3))
+    wc = np.zeros((4, 3))
+    s.type = np_ptr(types, ctypes.c_int)
+    s.id = np_ptr(ids, ctypes.c_int)
+    s.pos = np_ptr(pos)
+    s.vel = np_ptr(vel)
+    _check(lib.mph_read_checkpoint(path.encode(), ctypes.byref(s), wc.ctypes.data_as(ctypes.c_void_p)))
+    parts = casegen.Particles(s.time, s.spacing, np.array(s.domain_min[:]), np.array(s.domain_max[:]), types, pos, vel)
+    return parts, ids, wc
+
+
 class Case:
     """One simulation case resident on the GPU."""
 
     def __init__(self, params: casegen.Params, parts: casegen.Particles, dim: int,
-                 precision: int = PRECISION_FP64, stream: Optional[int] = None):
+                 precision: int = PRECISION_FP64, stream: Optional[int] = None, ids: Optional[np.ndarray] = None):
         self.lib = load_library()
         self.dim = dim
         self._p = params_to_c(params)
-        self._parts = ParticlesC(parts)
+        self._parts = ParticlesC(parts, ids)
         h = ctypes.c_void_p()
         _check(self.lib.mph_case_create(ctypes.byref(self._p), ctypes.byref(self._parts.struct), dim, precision,
                                         ctypes.c_void_p(stream or 0), ctypes.byref(h)))
@@ -216,6 +248,20 @@ class Case:
         out.update({f"kern_n_{s}": int(v[11 + k]) for k, s in enumerate(kern)})
         out.update({"slots": int(v[15]), "nnb": int(v[16]), "nnbP": int(v[17])})
         return out
+
+    def checkpoint(self, path: str):
+        _check(self.lib.mph_case_checkpoint(self.h, path.encode()))
+
+    @classmethod
+    def restore(cls, params: casegen.Params, path: str, dim: int, precision: int = PRECISION_FP64,
+                stream: Optional[int] = None) -> "Case":
+        """A case continuing from a checkpoint: created from the stored
+        particles (ids included), then given the stored order, wall centres
+        and time."""
+        parts, ids, wc = read_checkpoint(path)
+        c = cls(params, parts, dim, precision=precision, stream=stream, ids=ids)
+        c.set_state(parts, ids, wc)
+        return c
 
     def write_vtk(self, path: str):
         _check(self.lib.mph_case_write_vtk(self.h, path.encode()))

@@ -40,7 +40,7 @@ def _lib():
         decl = {
             "mph_case_footprint": ([vp, vp, ip, ip, ctypes.POINTER(ctypes.c_longlong)], ip),
             "mph_batch_step_workers": ([ctypes.POINTER(vp), ip, ip, ip], ip),
-            "mph_server_create": ([ctypes.c_longlong, ip, ctypes.POINTER(vp)], ip),
+            "mph_server_create": ([ctypes.c_longlong, ip, ip, ctypes.POINTER(vp)], ip),
             "mph_server_submit": ([vp, vp, vp, ip, ip, ip, vp, vp, ctypes.POINTER(ctypes.c_longlong)], ip),
             "mph_server_poll": ([vp, ctypes.POINTER(MphServerResult), ip, ip, ctypes.POINTER(ip)], ip),
             "mph_server_stats_get": ([vp, ctypes.POINTER(MphServerStats)], ip),
@@ -77,10 +77,10 @@ def batch_step(cases, nsteps: int = 1, workers: int = 0) -> int:
 class Server:
     """Continuous-batching server on the current CUDA device."""
 
-    def __init__(self, budget_bytes: int, workers: int = 16):
+    def __init__(self, budget_bytes: int, workers: int = 16, device: int = -1):
         self.lib = _lib()
         h = ctypes.c_void_p()
-        _check(self.lib.mph_server_create(int(budget_bytes), workers, ctypes.byref(h)))
+        _check(self.lib.mph_server_create(int(budget_bytes), workers, device, ctypes.byref(h)))
         self.h = h
         self._live: Dict[int, tuple] = {}
 
@@ -140,3 +140,51 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class ReplicaDispatcher:
+    """Serving on several GPUs of one node: one Server per device, each
+    request sent to the device with the most uncommitted budget (the
+    footprints of its requests not yet finished), results gathered from all
+    of them.  Host-side only: replicas share nothing and need no collective.
+    `server_factory(device)` makes a server (tests pass fakes)."""
+
+    def __init__(self, devices, budget_bytes: int, workers: int = 16, server_factory=None):
+        make = server_factory or (lambda d: Server(budget_bytes, workers, device=d))
+        self.devices = list(devices)
+        self.servers = [make(d) for d in self.devices]
+        self.budget = int(budget_bytes)
+        self.queued = [0] * len(self.servers)      # footprints submitted and not yet finished
+        self.route = {}                            # dispatcher ticket -> (replica, local ticket, footprint)
+        self.back = {}                             # (replica, local ticket) -> dispatcher ticket
+        self.next_ticket = 1
+
+    def submit(self, params, parts, dim: int, steps: int, precision: int = PRECISION_FP64, fields=("id", "pos", "vel"),
+               footprint_bytes: Optional[int] = None) -> int:
+        fp = footprint_bytes if footprint_bytes is not None else footprint(params, parts, dim, precision)
+        k = min(range(len(self.servers)), key=lambda r: (self.queued[r], r))
+        local = self.servers[k].submit(params, parts, dim, steps, precision=precision, fields=fields)
+        t = self.next_ticket
+        self.next_ticket += 1
+        self.queued[k] += fp
+        self.route[t] = (k, local, fp)
+        self.back[(k, local)] = t
+        return t
+
+    def poll(self, wait_ms: int = 0) -> List[dict]:
+        out = []
+        for k, srv in enumerate(self.servers):
+            for r in srv.poll(wait_ms=wait_ms if not out else 0):
+                t = self.back.pop((k, r["ticket"]))
+                self.queued[k] -= self.route.pop(t)[2]
+                r = dict(r)
+                r["ticket"], r["device"] = t, self.devices[k]
+                out.append(r)
+        return out
+
+    def outstanding(self) -> int:
+        return len(self.route)
+
+    def close(self):
+        for srv in self.servers:
+            srv.close()

@@ -155,3 +155,27 @@ def test_server_rejects_requests_beyond_budget(lib):
         srv.submit(p, s, 2, steps=0)
     assert srv.stats()["pending"] == 0
     srv.close()
+
+
+def test_checkpoint_roundtrip_is_exact(tmp_path, lib):
+    rng = np.random.default_rng(7)
+    p, s = casegen.square_drop_2d(scale=0.1, seed=0)
+    s = casegen.Particles(1.25e-3, s.spacing, s.domain_min, s.domain_max, s.types,
+                          s.pos + rng.uniform(-1e-9, 1e-9, s.pos.shape), rng.standard_normal(s.vel.shape))
+    ids = rng.permutation(len(s.types)).astype(np.int32)
+    wc = rng.standard_normal((4, 3))
+    path = str(tmp_path / "state.ckpt")
+    engine.write_checkpoint(path, s, ids, wc)
+    r, rid, rwc = engine.read_checkpoint(path)
+    assert r.time == s.time and r.spacing == s.spacing
+    assert np.array_equal(r.domain_min, s.domain_min) and np.array_equal(r.domain_max, s.domain_max)
+    assert np.array_equal(r.types, s.types) and np.array_equal(rid, ids)
+    assert np.array_equal(r.pos, s.pos) and np.array_equal(r.vel, s.vel) and np.array_equal(rwc, wc)
+
+
+def test_checkpoint_rejects_other_files(tmp_path, lib):
+    bad = tmp_path / "box.grid"
+    bad.write_text("0.0\n0.01\n")
+    with pytest.raises(engine.MphError) as e:
+        engine.read_checkpoint(str(bad))
+    assert e.value.status == 2
