@@ -84,7 +84,7 @@ def measured_peaks():
 def ncu_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` on the bench workload from the
     committed ncu summary (profiles/), or None."""
-    path = os.path.join(REPO, "profiles", f"{kernel}_cube3d_100.md")
+    path = os.path.join(REPO, "profiles", f"{kernel.split('+')[-1]}_cube3d_100.md")
     if not os.path.exists(path):
         return None
     m = re.search(r"dram_bytes_per_launch_full:\s*([0-9.eE+]+)", open(path).read())
@@ -146,6 +146,23 @@ def spmv_bytes(prof, scal, dim, vb=8):
     blocks = scal["NonzeroCountA"] / (dim * dim)
     nsl = (nf + 31) // 32
     return blocks * (dim * dim * vb + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * vb
+
+
+def pair_apply_bytes(prof, scal, dim):
+    """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
+    (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
+    transposed P-list slot, entry counts and slice pointers, s gathered once,
+    t written.  k_visc_pen32: column + D FP32 values of g = sqrt(f) e per
+    fluid slot, column + D FP32 lambda C per P-slot, the 6-entry diagonal,
+    row lengths and slice pointers, s read once, t gathered once, y written."""
+    nf = int(scal["FluidParticleEnd"])
+    n = int(scal["ParticleCount"])
+    slots = scal["NonzeroCountA"] / (dim * dim)
+    pslots = scal["NonzeroCountC"] / dim
+    nsl, nct = (nf + 31) // 32, (n + 31) // 32
+    ct = pslots * (dim * 4 + 4) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
+    vp = (slots + pslots) * (dim * 4 + 4) + nf * (24 + 8) + 2 * (nsl + 1) * 8 + 2 * dim * nf * 4 + n * 4
+    return ct + vp
 
 
 def assemble_bytes(prof, scal, dim):
@@ -408,6 +425,8 @@ def main():
     ap.add_argument("--no-factored", action="store_true",
                     help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
     ap.add_argument("--extra-sweeps", type=int, default=0, help="mixed form: extra level-0 smoothing sweeps")
+    ap.add_argument("--inner-blocks", type=int, default=-1, choices=[-1, 0, 1],
+                    help="mixed form: inner operator on FP32 blocks (1) or sliced pair terms (0); -1 keeps the engine default")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=60)
@@ -452,6 +471,8 @@ def main():
         case.set_solver(args.outer_tol, args.inner_tol, 50)
         case.set_option("factored", 0 if args.no_factored else 1)
         case.set_option("mixed_extra_sweeps", args.extra_sweeps)
+        if args.inner_blocks >= 0:
+            case.set_option("inner_blocks", args.inner_blocks)
     N, Nf = case.count, case.fluid_count
     for _ in range(args.warmup):
         case.step(1)
@@ -507,7 +528,9 @@ def main():
     # roofline of the dominant kernel (CUDA events on the case stream)
     peak, peak_kind = measured_peaks()
     vb = 4 if prec == PRECISION_MIXED else 8
-    kern = {"spmv": ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
+    pairs = case.solve_stats().get("inner_form") == 2
+    kern = {"spmv": ("k_ct_apply32+k_visc_pen32", pair_apply_bytes) if pairs else
+                    ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
             "assemble_a": ("k_assemble_cells", assemble_bytes)}
     dom = max(kern, key=lambda k: prof[f"kern_ms_{k}"])
     nlaunch = max(prof[f"kern_n_{dom}"], 1)

@@ -100,6 +100,8 @@ typedef struct mph_solve_stats {
     double rr0, rr, rs0, rs;
     int status;
     int outer_iterations;    /* mixed form: FP64 refinement steps (0 for the FP64 form) */
+    int inner_form;          /* operator of the CR iterations: 0 FP64 blocks, 1 FP32 blocks,
+                                2 FP32 pair terms (mixed form, factored, option inner_blocks 0) */
 } mph_solve_stats;
 
 typedef struct mph_case mph_case;

@@ -71,7 +71,7 @@ class MphFields(ctypes.Structure):
 class MphSolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("rr0", ctypes.c_double), ("rr", ctypes.c_double),
                 ("rs0", ctypes.c_double), ("rs", ctypes.c_double), ("status", ctypes.c_int),
-                ("outer_iterations", ctypes.c_int)]
+                ("outer_iterations", ctypes.c_int), ("inner_form", ctypes.c_int)]
 
 
 def params_to_c(p: casegen.Params) -> MphParams:

@@ -405,6 +405,19 @@ static int ensure(void** p, long long* cap, long long need, size_t elem)
     return MPH_OK;
 }
 
+// Slice pointers of a sliced layout of 32-row slices over per-row counts:
+// width[s] = 32 x the longest row of slice s, ptr = its exclusive scan, and
+// the slot total on the host.
+int launch_slice_ptr(mph_case* c, int rows, const int* counts, int* width, long long* ptr, long long* total)
+{
+    const int ns = (rows + 31) / 32;
+    { k_slice_width<<<grid_for((long long)ns * 32, 256), 256, 0, c->stream>>>(rows, counts, width); MPH_COUNT_LAUNCH(); }
+    MPH_TRY(launch_scan_i32_to_i64(c, width, ptr, ns));
+    MPH_CUDA(cudaMemcpyAsync(total, ptr + ns, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    return MPH_OK;
+}
+
 int launch_assemble(mph_case* c)
 {
     const DevParams& P = c->dp;
@@ -476,10 +489,12 @@ int launch_assemble(mph_case* c)
     bool cells = false;
     c->ct_ready = false;
     c->step_factored = factored_applies(c);
+    c->step_pairs = c->step_factored && !c->inner_blocks && c->visc_nonneg;
     if (c->step_factored) {
         // mixed form: FP64 pair terms and b, transposed P-lists (the factored
         // FP64 operator), then FP32 blocks only
         MPH_TRY(build_ct(c));
+        if (c->step_pairs) MPH_TRY(launch_ct_slices(c));
         MPH_TRY(launch_pair_terms(c));
     }
     if (c->cell_assembly) MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
@@ -494,6 +509,7 @@ int launch_assemble(mph_case* c)
                                                  c->d.nptr, c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,
                                                  c->d.acol, c->d.aval, a32, c->d.bvec, c->d.invDiag, c->d.selfk, c->d.part); MPH_COUNT_LAUNCH(); }
     }
+    if (c->step_pairs) MPH_TRY(launch_pairs_to_slices(c));
     if (pon) prof_end(c, 2, pe);
     return MPH_OK;
 }

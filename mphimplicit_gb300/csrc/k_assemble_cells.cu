@@ -520,9 +520,9 @@ int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done)
     }
     int r[3] = {0, 0, 0};
     for (int d = 0; d < D; ++d) r[d] = (int)std::ceil(P.maxR / P.cw[d]);
-    // FP32 blocks: the mixed form's copy, except when its inner SpMV runs on the
-    // pair terms (factored form without inner_blocks)
-    float* a32 = c->precision == MPH_PRECISION_MIXED && !(mix && !c->inner_blocks) ? dv.aval32 : nullptr;
+    // FP32 blocks: the mixed form's copy, except when its inner operator runs
+    // on the sliced pair terms
+    float* a32 = c->precision == MPH_PRECISION_MIXED && !c->step_pairs ? dv.aval32 : nullptr;
     if (mix && a32) {   // FP32 blocks go through the row-contiguous buffer
         long long slots = 0;
         MPH_CUDA(cudaMemcpyAsync(&slots, dv.nptr + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));

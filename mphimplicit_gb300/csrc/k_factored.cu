@@ -17,10 +17,11 @@
 //
 // k_pair_terms stores (e, f) per neighbour slot of every fluid row in FP32
 // (used by the FP32 blocks and by the viscous part of the FP64 residual) and b
-// in FP64.  The only FP64 work per slot is the exact minimum-image separation,
-// against the nine-entry block and its accumulation of the assembled form; in
-// the residual only inertia and C Lambda C^T (about 20 P-slots a row) are
-// FP64.
+// in FP64; for the FP32 inner operator without blocks also the FP32 diagonal
+// block and the lambda-scaled C values.  The only FP64 work per slot is the
+// minimum-image separation, against the nine-entry block and its accumulation of
+// the assembled form; in the residual only inertia and C Lambda C^T (about 20
+// P-slots a row) are FP64.
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -41,7 +42,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
-             float4* __restrict__ pe32, double* __restrict__ bvec)
+             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ sdiag32, float* __restrict__ cvl32)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -54,6 +55,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         load_vec<D>(pos, i, xi);
         load_vec<D>(vel, i, vi);
         float sumw[3] = {0.f, 0.f, 0.f};
+        float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over all slots: xx xy xz yy yz zz
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
             float e[3] = {0.f, 0.f, 0.f};
@@ -84,15 +86,41 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                 }
             }
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
+            sd[0] += f * e[0] * e[0];
+            sd[1] += f * e[0] * e[1];
+            sd[2] += f * e[0] * e[2];
+            sd[3] += f * e[1] * e[1];
+            sd[4] += f * e[1] * e[2];
+            sd[5] += f * e[2] * e[2];
+        }
+        if (sdiag32) {   // the FP32 diagonal block of the inner operator: viscous + inertia
+#pragma unroll
+            for (int t = 0; t < 6; ++t)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sd[t] += __shfl_xor_sync(0xffffffffu, sd[t], o);
+            if (lane == 0) {
+                const float in32 = P.inert32[ti];
+                sd[0] += in32;
+                sd[3] += in32;
+                if (D == 3) sd[5] += in32;
+#pragma unroll
+                for (int t = 0; t < 6; ++t) sdiag32[(size_t)i * 6 + t] = sd[t];
+            }
         }
         // - C p over the row's P-neighbours (FP64)
         double sumv[3] = {(double)sumw[0], (double)sumw[1], (double)sumw[2]};
         const long long pb = nptrP[i];
         const int np = ncp[i];
         for (int a = lane; a < np; a += 32) {
-            const double pk = pvec[nindP[pb + a]];
+            const int k = nindP[pb + a];
+            const double pk = pvec[k];
 #pragma unroll
             for (int r = 0; r < D; ++r) sumv[r] -= cval[(pb + a) * D + r] * pk;
+            if (cvl32) {   // lambda_k C_ik for the FP32 inner operator
+                const double lam = P.lambda[type[k]];
+#pragma unroll
+                for (int r = 0; r < D; ++r) cvl32[(pb + a) * D + r] = (float)(cval[(pb + a) * D + r] * lam);
+            }
         }
 #pragma unroll
         for (int r = 0; r < D; ++r)
@@ -194,17 +222,25 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 }
 
 // ---- FP32 inner operator of the mixed form, without assembled blocks --------------
-// The inner CR's y = A32 s from the FP32 pair terms: t = C^T s per particle
-// (k_ct_apply32, which also runs the iteration's convergence test), then per
-// fluid row inertia + viscous pair terms + C Lambda t, and (s, y) into the
-// iteration's rho slot (k_apply32).  Same recurrences and flags as k_spmv32.
+// The inner CR's y = A32 s from the FP32 pair terms in two launches, both one
+// thread per row over sliced lists (entry e of row i at slice base + e*32 +
+// lane, its D values at slice base * D + (e*D + d)*32 + lane: coalesced):
+//   k_ct_apply32   t = C^T s per particle over the transposed P-lists, after
+//                  the iteration's convergence test;
+//   k_visc_pen32   y_i = (inertia + sum_all f e (x) e) s_i
+//                        - sum_{fluid j} g (g . s_j) + sum_k lambda_k C_ik t_k
+//                  with g = sqrt(f) e (f >= 0, so a fluid pair's block
+//                  -f e (x) e is -g (x) g: D floats a slot against D*D for a
+//                  block), and (s, y) into the iteration's rho slot.
+// Same recurrences and flags as k_spmv32.
 constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 
 template <int D>
-__global__ void k_ct_apply32(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
-                             const float* __restrict__ ct_v32, const float* __restrict__ x, float* __restrict__ t,
-                             const double* __restrict__ scal, int* __restrict__ flags, int cap)
+__global__ void __launch_bounds__(256) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
+                                                    const int* __restrict__ ctscol, const float* __restrict__ ctsval,
+                                                    const float* __restrict__ x, float* __restrict__ t,
+                                                    const double* __restrict__ scal, int* __restrict__ flags, int cap)
 {
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
@@ -213,7 +249,6 @@ __global__ void k_ct_apply32(int N, const long long* __restrict__ ctptr, const i
     const double rr = it == 0 ? rr0 : scal[kSIn];
     const bool bad = !(rr == rr);
     if (it >= cap || rr / rr0 < tol2 || bad) {
-        __syncthreads();
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             flags[kFlagDone] = 1;
             if (bad) flags[kFlagBad] = 1;
@@ -222,77 +257,144 @@ __global__ void k_ct_apply32(int N, const long long* __restrict__ ctptr, const i
     }
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
+    const int lane = k & 31;
+    const long long base = ctsptr[k >> 5];
+    const int* cp = ctscol + base + lane;
+    const float* vp = ctsval + base * D + lane;
     float s = 0.f;
-    const long long e1 = ctptr[k + 1];
-    for (long long e = ctptr[k]; e < e1; ++e) {
-        const int j = ct_j[e];
+    const int n = ctcnt[k];
+#pragma unroll 4
+    for (int e = 0; e < n; ++e) {
+        const int j = __ldcs(cp + (long long)e * 32);
 #pragma unroll
-        for (int d = 0; d < D; ++d) s += ct_v32[e * D + d] * x[(size_t)j * D + d];
+        for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * x[(size_t)j * D + d];
     }
     t[k] = s;
 }
 
 template <int D>
-__global__ void __launch_bounds__(kPairWarps * 32)
-k_apply32(DevParams P, const int* __restrict__ type, const int* __restrict__ nc, const int* __restrict__ nfc,
-          const long long* __restrict__ nptr, const int* __restrict__ nind, const float4* __restrict__ pe32,
-          const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
-          const float* __restrict__ cval32, const float* __restrict__ t, const float* __restrict__ x,
-          float* __restrict__ y, double* __restrict__ scal, const int* __restrict__ flags,
-          double* __restrict__ partials, unsigned* __restrict__ counter)
+__global__ void __launch_bounds__(128)
+k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
+             const float* __restrict__ pes, const float* __restrict__ sdiag, const int* __restrict__ ncp,
+             const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
+             const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
+             const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
-    const int lane = threadIdx.x & 31;
-    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double acc = 0.0;
-    for (int i = wid; i < P.Nf; i += nwarps) {
+    if (i < Nf) {
+        const int lane = i & 31;
         float xi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
-        float yv[3] = {0.f, 0.f, 0.f};
-        const long long nb = nptr[i];
-        const int n = nc[i], nf = nfc[i];
-        for (int k = lane; k < n; k += 32) {
-            const float4 p = pe32[nb + k];
-            const float e[3] = {p.x, p.y, p.z};
-            float dx[3] = {xi[0], xi[1], xi[2]};
-            if (k < nf) {
-                const int j = nind[nb + k];
+        const float* S = sdiag + (size_t)i * 6;
+        float yv[3];
+        yv[0] = S[0] * xi[0] + S[1] * xi[1] + S[2] * xi[2];
+        yv[1] = S[1] * xi[0] + S[3] * xi[1] + S[4] * xi[2];
+        yv[2] = S[2] * xi[0] + S[4] * xi[1] + S[5] * xi[2];
+        {   // fluid pairs: - g (g . x_j)
+            const long long base = sptr[i >> 5];
+            const int* cp = acol + base + lane;
+            const float* vp = pes + base * D + lane;
+            const int n = nfc[i];
+#pragma unroll 4
+            for (int k = 0; k < n; ++k) {
+                const int col = __ldcs(cp + (long long)k * 32);
+                float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-                for (int d = 0; d < D; ++d) dx[d] -= x[(size_t)j * D + d];
+                for (int d = 0; d < D; ++d) g[d] = __ldcs(vp + ((long long)k * D + d) * 32);
+                float gx = 0.f;
+#pragma unroll
+                for (int d = 0; d < D; ++d) gx += g[d] * x[(size_t)col * D + d];
+#pragma unroll
+                for (int d = 0; d < D; ++d) yv[d] -= gx * g[d];
             }
-            float ed = 0.f;
-#pragma unroll
-            for (int d = 0; d < D; ++d) ed += e[d] * dx[d];
-            const float sc = p.w * ed;
-#pragma unroll
-            for (int d = 0; d < D; ++d) yv[d] += sc * e[d];
         }
-        const long long pb = nptrP[i];
-        const int np = ncp[i];
-        for (int a = lane; a < np; a += 32) {
-            const int k = nindP[pb + a];
-            const float lt = (float)P.lambda[type[k]] * t[k];
+        {   // C Lambda t over the row's P-neighbours
+            const long long base = psptr[i >> 5];
+            const int* cp = pscol + base + lane;
+            const float* vp = psval + base * D + lane;
+            const int np = ncp[i];
+#pragma unroll 4
+            for (int a = 0; a < np; ++a) {
+                const float tk = t[__ldcs(cp + (long long)a * 32)];
 #pragma unroll
-            for (int d = 0; d < D; ++d) yv[d] += cval32[(pb + a) * D + d] * lt;
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) yv[d] += __shfl_xor_sync(0xffffffffu, yv[d], o);
-        if (lane == 0) {
-            const float inert = (float)(P.density[type[i]] * P.vol / P.vol / P.dt);
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                const float v = inert * xi[d] + yv[d];
-                y[(size_t)i * D + d] = v;
-                acc += (double)xi[d] * (double)v;
+                for (int d = 0; d < D; ++d) yv[d] += __ldcs(vp + ((long long)a * D + d) * 32) * tk;
             }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            y[(size_t)i * D + d] = yv[d];
+            acc += (double)xi[d] * (double)yv[d];
         }
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
+}
+
+// Rows of a CSR list (count, row pointer, column, D FP32 values an entry) ->
+// the sliced layout, one CTA per slice of 32 rows: chunks of kLtsK entries of
+// the 32 rows are read row by row (coalesced) into shared memory and written
+// slice-wise (coalesced), padding slots as zeros.  PAIRS: the values are the
+// pair terms (e, f), stored as g = sqrt(f) e.
+constexpr int kLtsK = 32;
+
+template <int D, bool PAIRS>
+__global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long long* __restrict__ sptr, const int* __restrict__ cnt,
+                                                        const long long* __restrict__ rptr, const int* __restrict__ cols,
+                                                        const float4* __restrict__ pe32, const float* __restrict__ v32,
+                                                        int* __restrict__ scol, float* __restrict__ sval)
+{
+    constexpr int W = kLtsK * D + 1;   // odd row stride: no bank conflicts
+    __shared__ float tile[32 * W];
+    __shared__ int ctile[32 * (kLtsK + 1)];
+    __shared__ int rn[32];
+    __shared__ long long rb[32];
+    const int sl = blockIdx.x;
+    if (threadIdx.x < 32) {
+        const int i = sl * 32 + threadIdx.x;
+        rn[threadIdx.x] = i < rows ? cnt[i] : 0;
+        rb[threadIdx.x] = i < rows ? rptr[i] : 0;
+    }
+    __syncthreads();
+    const long long sb = sptr[sl];
+    const int w = (int)((sptr[sl + 1] - sb) / 32);   // entries per row of the slice
+    for (int k0 = 0; k0 < w; k0 += kLtsK) {
+        const int kc = min(kLtsK, w - k0);
+        for (int t = threadIdx.x; t < 32 * kLtsK; t += blockDim.x) {
+            const int r = t / kLtsK, kl = t % kLtsK;
+            float v[3] = {0.f, 0.f, 0.f};
+            int col = 0;
+            if (kl < kc && k0 + kl < rn[r]) {
+                const long long e = rb[r] + k0 + kl;
+                col = cols[e];
+                if (PAIRS) {
+                    const float4 pv = pe32[e];
+                    const float sf = sqrtf(pv.w);
+                    v[0] = sf * pv.x;
+                    v[1] = sf * pv.y;
+                    v[2] = sf * pv.z;
+                } else {
+#pragma unroll
+                    for (int d = 0; d < D; ++d) v[d] = v32[e * D + d];
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < D; ++d) tile[r * W + kl * D + d] = v[d];
+            ctile[r * (kLtsK + 1) + kl] = col;
+        }
+        __syncthreads();
+        for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
+            const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
+            sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+        }
+        for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+            const int ln = o & 31, kl = o >> 5;
+            scol[sb + (long long)(k0 + kl) * 32 + ln] = ctile[ln * (kLtsK + 1) + kl];
+        }
+        __syncthreads();
+    }
 }
 
 void launch_apply32(mph_case* c, const float* x, float* y, int cap)
@@ -301,19 +403,42 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     const DevParams& P = c->dp;
     unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
     const unsigned gt = grid_for(P.N, 256);
-    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
+    const unsigned gv = grid_for(P.Nf, 128);
     if (c->dim == 2) {
-        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_apply32<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
-                                                            d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
+        { k_visc_pen32<2><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+                                                     d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_apply32<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP, d.nindP,
-                                                            d.cval32, d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
+        { k_visc_pen32<3><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+                                                     d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     }
 }
 
 // ---- host side ---------------------------------------------------------------------
+static int grow_f(float** p, long long* cap, long long need)
+{
+    if (need <= *cap) return MPH_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const long long n = need + need / 8 + 1024;
+    MPH_CUDA(cudaMalloc((void**)p, (size_t)n * sizeof(float)));
+    *cap = n;
+    return MPH_OK;
+}
+static int grow_i(int** p, long long* cap, long long need)
+{
+    if (need <= *cap) return MPH_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const long long n = need + need / 8 + 1024;
+    MPH_CUDA(cudaMalloc((void**)p, (size_t)n * sizeof(int)));
+    *cap = n;
+    return MPH_OK;
+}
+
 static int grow_pairs(mph_case* c, long long slots)
 {
     DeviceState& d = c->d;
@@ -360,13 +485,79 @@ int launch_pair_terms(mph_case* c)
         d.cap_cval32 = ncv + ncv / 8 + 1024;
     }
     { k_cval_f32<<<grid_for(ncv, 256), 256, 0, c->stream>>>(ncv, d.cval, d.cval32); MPH_COUNT_LAUNCH(); }
+    float* sdiag = nullptr;
+    float* cvl = nullptr;
+    if (c->step_pairs) {   // FP32 inner operator on the pair terms
+        if (!d.sdiag32) MPH_CUDA(cudaMalloc((void**)&d.sdiag32, (size_t)P.Nf * 6 * sizeof(float)));
+        MPH_TRY(grow_f(&d.cvl32, &d.cap_cvl32, ncv));
+        sdiag = d.sdiag32;
+        cvl = d.cvl32;
+    }
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
+    }
+    return MPH_OK;
+}
+
+// The sliced pair terms g = sqrt(f) e with the block columns, and the sliced
+// lambda-scaled P-lists, of the fluid rows (after k_pair_terms).
+int launch_pairs_to_slices(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    const int D = c->dim;
+    if (c->nslices == 0) return MPH_OK;
+    MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
+    if (!d.psptr) {
+        MPH_CUDA(cudaMalloc((void**)&d.psptr, (size_t)(c->nslices + 1) * sizeof(long long)));
+        MPH_CUDA(cudaMalloc((void**)&d.pswidth, (size_t)(c->nslices + 1) * sizeof(int)));
+    }
+    long long pslots = 0;
+    MPH_TRY(launch_slice_ptr(c, P.Nf, d.ncp, d.pswidth, d.psptr, &pslots));
+    MPH_TRY(grow_i(&d.pscol, &d.cap_pscol, pslots));
+    MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * D));
+    if (D == 2) {
+        { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
+                                                                      d.pes32); MPH_COUNT_LAUNCH(); }
+        { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
+                                                                       d.pscol, d.psval); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
+                                                                      d.pes32); MPH_COUNT_LAUNCH(); }
+        { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
+                                                                       d.pscol, d.psval); MPH_COUNT_LAUNCH(); }
+    }
+    return MPH_OK;
+}
+
+// The transposed P-lists (C in FP32) of every particle in the sliced layout
+// (after build_ct).
+int launch_ct_slices(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    const int D = c->dim;
+    const int ns = (P.N + 31) / 32;
+    if (ns == 0) return MPH_OK;
+    if (!d.ctsptr) {
+        MPH_CUDA(cudaMalloc((void**)&d.ctsptr, (size_t)(ns + 1) * sizeof(long long)));
+        MPH_CUDA(cudaMalloc((void**)&d.ctswidth, (size_t)(ns + 1) * sizeof(int)));
+    }
+    long long slots = 0;
+    MPH_TRY(launch_slice_ptr(c, P.N, d.ct_cnt, d.ctswidth, d.ctsptr, &slots));
+    MPH_TRY(grow_i(&d.ctscol, &d.cap_ctscol, slots));
+    MPH_TRY(grow_f(&d.ctsval, &d.cap_ctsval, slots * D));
+    if (D == 2) {
+        { k_list_to_slices<2, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
+                                                               d.ctsval); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_list_to_slices<3, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
+                                                               d.ctsval); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }

@@ -318,7 +318,7 @@ static int mixed_solve_t(mph_case* c)
     // and replays as a graph.  Iterations after a stop return at once.
     auto iteration = [&, c](cudaEvent_t* e) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
-        if (c->step_factored && !c->inner_blocks) {
+        if (c->step_pairs) {
             launch_apply32(c, s32, y32, cap);   // FP32 pair terms, no assembled blocks
         } else {
             k_spmv32<D, 1, V><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, part,
@@ -398,6 +398,7 @@ static int mixed_solve_t(mph_case* c)
     c->stats.rs0 = 0.0;
     c->stats.rs = 0.0;
     c->stats.outer_iterations = outer;
+    c->stats.inner_form = c->step_pairs ? 2 : 1;
     c->stats.status = bad ? MPH_ERR_NAN : (hs[kSRR] / hs[kSRR0] < tol_out2 || hs[kSRR] == 0.0 ? MPH_OK : MPH_ERR_NOT_CONVERGED);
     return MPH_OK;
 }

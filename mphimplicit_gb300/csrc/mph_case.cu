@@ -173,6 +173,12 @@ static int derive(mph_case* c, const mph_particles* parts)
         for (int u = 0; u < kTypeCount; ++u) P.vm32[t][u] = (float)(P.visc * P.muij[t][u]);
     }
     P.wdA32 = (float)(-P.kfv * P.m2h_rv);
+    // the pair terms of the FP32 inner operator are stored as sqrt(f) e, which
+    // needs f >= 0 for every pair of types
+    c->visc_nonneg = P.wdA32 >= 0.f;
+    for (int t = 0; t < kTypeCount; ++t)
+        for (int u = 0; u < kTypeCount; ++u)
+            if (!(P.vm32[t][u] >= 0.f)) c->visc_nonneg = false;
     P.inv_rv32 = (float)P.inv_rv;
     P.rV2_32 = (float)(P.rV * P.rV);
     // size of the viscous part of a row of A against its inertia rho/dt: the
@@ -636,7 +642,10 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags, d.ct_tmp,
-                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32, (void*)d.tct32, d.scan_tmp})
+                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
+                    (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
+                    (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
+                    d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

@@ -108,7 +108,7 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
         }
         return MPH_OK;
     }
-    if ((name == "CsrIndA" || name == "CsrCofA") && c->step_factored && !c->inner_blocks)
+    if (name == "CsrCofA" && c->step_pairs)
         return fail(MPH_ERR_STATE, name + ": this step assembled no blocks (mixed form, factored operator; "
                                           "set option \"inner_blocks\" to 1 to keep FP32 blocks)");
     if (name == "CsrPtrA" || name == "CsrIndA" || name == "CsrCofA") {

@@ -123,6 +123,22 @@ struct DeviceState {
     float* cval32 = nullptr;        // FP32 copy of the fluid rows' C values
     long long cap_cval32 = 0;
     float* tct32 = nullptr;         // t = C^T x of the FP32 inner operator
+    // FP32 inner operator on pair terms: g = sqrt(f) e per fluid slot in the
+    // sliced (k, component, lane) layout, the FP32 diagonal block (inertia +
+    // sum f e (x) e, 6 entries a row), C scaled by lambda of its P-neighbour
+    // (aligned with the P-lists), and the P-lists (lambda-scaled C) and
+    // transposed P-lists (C) in sliced layouts: slice pointers, widths,
+    // columns, D FP32 values a slot
+    float* pes32 = nullptr;
+    long long cap_pes32 = 0;
+    float* sdiag32 = nullptr;
+    float* cvl32 = nullptr;
+    long long cap_cvl32 = 0;
+    long long *psptr = nullptr, *ctsptr = nullptr;
+    int *pswidth = nullptr, *ctswidth = nullptr;
+    int *pscol = nullptr, *ctscol = nullptr;
+    float *psval = nullptr, *ctsval = nullptr;
+    long long cap_pscol = 0, cap_psval = 0, cap_ctscol = 0, cap_ctsval = 0;
     // multigrid
     double *mg_cof = nullptr, *mg_invd = nullptr;
     double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr, *mg_res = nullptr;   // Q, S ping-pong pair, residual
@@ -198,6 +214,8 @@ struct mph_case {
     bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
+    bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
+    bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
     cudaGraphExec_t cr_exec = nullptr;  // FP64 CR chunk
@@ -276,6 +294,7 @@ void launch_cell_ranges_and_permute(mph_case* c);
 void launch_fluid_bbox(mph_case* c);
 void launch_neighbor_count(mph_case* c);
 int launch_scan_i32_to_i64(mph_case* c, const int* in, long long* out, int n);
+int launch_slice_ptr(mph_case* c, int rows, const int* counts, int* width, long long* ptr, long long* total);
 void launch_neighbor_fill(mph_case* c);
 void launch_explicit(mph_case* c);
 void launch_explicit_density_only(mph_case* c);
@@ -289,6 +308,8 @@ bool factored_applies(const mph_case* c);
 int launch_pair_terms(mph_case* c);
 void launch_resid_factored(mph_case* c, const double* x, double* r, double* out);
 void launch_apply32(mph_case* c, const float* x, float* y, int cap);
+int launch_pairs_to_slices(mph_case* c);
+int launch_ct_slices(mph_case* c);
 void launch_mg_level0(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);

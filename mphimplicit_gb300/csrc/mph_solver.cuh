@@ -114,16 +114,15 @@ inline unsigned long long graph_signature(const mph_case* c, double tol, int cap
 {
     unsigned long long h = 1469598103934665603ull;
     // the particle arrays swap with their alternates every step and no
-    // captured kernel reads them (the type array only on the pair-term path)
+    // captured kernel reads them
     DeviceState d = c->d;
     d.pos = d.vel = d.force = d.pos_alt = d.vel_alt = nullptr;
     d.pos32 = nullptr;
-    d.id = d.id_alt = d.type_alt = nullptr;
-    if (!(c->step_factored && !c->inner_blocks)) d.type = nullptr;
+    d.id = d.id_alt = d.type_alt = d.type = nullptr;
     h = fnv1a(h, &d, sizeof(d));
     h = fnv1a(h, &c->dp, sizeof(c->dp));
     if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));
-    const long long misc[] = {c->depth, c->nslices, c->nslots, c->precision, c->step_factored, c->inner_blocks, c->mixed_extra_sweeps,
+    const long long misc[] = {c->depth, c->nslices, c->nslots, c->precision, c->step_factored, c->step_pairs, c->mixed_extra_sweeps,
                               cap, c->mg_rows_total, c->mg_cof_total};
     h = fnv1a(h, misc, sizeof(misc));
     h = fnv1a(h, &tol, sizeof(tol));

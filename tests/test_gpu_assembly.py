@@ -116,3 +116,34 @@ def test_pair_term_inner_operator_solves(engine_lib, case):
     va = vec_proj(a.export("Velocity"), dim)[:nf]
     vb = vec_proj(b.export("Velocity"), dim)[:nf]
     assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 2e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_sliced_pair_terms_match_blocks(engine_lib, case):
+    """The inner operator on the sliced pair terms (g = sqrt(f) e, sliced
+    P-lists and transposed P-lists) is the FP32 block operator in another
+    storage: same block columns, and a solve with either takes about the same
+    iterations to the same velocity (both are FP32 roundings of one operator,
+    the outer residual is FP64).  The reference's tolerance 1e-6: the factored
+    form, which the pair terms need, is not used far below it."""
+    name, dim, params, parts = case
+    cs = {}
+    for blocks in (1, 0):
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_option("inner_blocks", blocks)
+        for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
+            g.stage(st)
+        cols = g.export("CsrIndA")
+        g.stage("solve")
+        assert g.solve_stats()["status"] == 0
+        cs[blocks] = (g, cols)
+    (a, ia), (b, ib) = cs[0], cs[1]
+    assert np.array_equal(ia, ib)
+    sa, sb = a.solve_stats(), b.solve_stats()
+    assert (sa["inner_form"], sb["inner_form"]) == (2, 1)
+    assert abs(sa["iter"] - sb["iter"]) <= max(2, sb["iter"] // 10), (sa, sb)
+    assert abs(sa["outer"] - sb["outer"]) <= 1
+    nf = a.fluid_count
+    va = vec_proj(a.export("Velocity"), dim)[:nf]
+    vb = vec_proj(b.export("Velocity"), dim)[:nf]
+    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 1e-5
