@@ -222,9 +222,11 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
  *   0: FP64 blocks are assembled and copied to FP32.
  *   "mixed_extra_sweeps" 0 (default) .. 8: mixed form only, extra level-0
  *   smoothing sweeps before and after the rest of its V-cycle.
- *   "inner_blocks" 1 (default) / 0: factored mixed form only.  0: the inner
- *   FP32 SpMV runs on the FP32 pair terms and no blocks are written
- *   (CsrIndA / CsrCofA exports then fail with MPH_ERR_STATE). */
+ *   "inner_blocks" 0 (default) / 1: factored mixed form only.  0: the inner
+ *   FP32 operator runs on the sliced FP32 pair terms and P-lists and no
+ *   blocks are written (CsrCofA export then fails with MPH_ERR_STATE; the
+ *   block columns CsrIndA still export).  1: FP32 blocks are assembled and
+ *   the inner SpMV runs on them. */
 int mph_case_set_option(mph_case* c, const char* name, double value);
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);

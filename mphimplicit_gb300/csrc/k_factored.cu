@@ -17,9 +17,10 @@
 //
 // k_pair_terms stores (e, f) per neighbour slot of every fluid row in FP32
 // (used by the FP32 blocks and by the viscous part of the FP64 residual) and b
-// in FP64; for the FP32 inner operator without blocks also the FP32 diagonal
-// block and the lambda-scaled C values.  The only FP64 work per slot is the
-// minimum-image separation, against the nine-entry block and its accumulation of
+// in FP64; for the FP32 inner operator without blocks also the wall part of
+// the FP32 viscous diagonal block, the FP32 inertia and the lambda-scaled C
+// values.  The only FP64 work per slot is the
+// position difference, against the nine-entry block and its accumulation of
 // the assembled form; in the residual only inertia and C Lambda C^T (about 20
 // P-slots a row) are FP64.
 #include "mph_device.cuh"
@@ -31,7 +32,9 @@ constexpr int kPairWarps = 8;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
 // (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).  The
-// separation is the exact FP64 minimum image of the neighbour search; the rest
+// separation is the FP64 difference of the positions rounded to FP32 (the
+// minimum image of the neighbour search, which it equals to within one FP64
+// rounding, is evaluated only for periodic images); the rest
 // of the viscous term is FP32: it is about nu dt / l0^2 (~1e-3) of the
 // inertia term, so its FP32 rounding moves A x by ~1e-10 of |b| (the host
 // keeps the factored form off when that bound would reach 1e-2 of the outer
@@ -55,18 +58,30 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         load_vec<D>(pos, i, xi);
         load_vec<D>(vel, i, vi);
         float sumw[3] = {0.f, 0.f, 0.f};
-        float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over all slots: xx xy xz yy yz zz
+        float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over the wall slots: xx xy xz yy yz zz
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
             float e[3] = {0.f, 0.f, 0.f};
             float f = 0.f;
             if (j != i) {
-                double xj[3], q[3];
+                // x_j - x_i rounded to FP32; the exact minimum image only when
+                // a component is not well inside a quarter of the domain width
+                // (a periodic image), where the two could differ
+                double xj[3];
                 load_vec<D>(pos, j, xj);
-                sep_vec<D>(P, xj, xi, q);
                 float q32[3] = {0.f, 0.f, 0.f};
+                bool inner = true;
 #pragma unroll
-                for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
+                for (int d = 0; d < D; ++d) {
+                    q32[d] = (float)(xj[d] - xi[d]);
+                    inner = inner && fabsf(q32[d]) < 0.48f * P.hw32[d];
+                }
+                if (!inner) {
+                    double q[3];
+                    sep_vec<D>(P, xj, xi, q);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
+                }
                 const float r2 = q32[0] * q32[0] + q32[1] * q32[1] + q32[2] * q32[2];
                 if (r2 != 0.f && P.rV2_32 - r2 > 0.f) {
                     const float inv = rsqrtf(r2);
@@ -82,29 +97,26 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                         for (int d = 0; d < D; ++d) ev += e[d] * (float)vj[d];
 #pragma unroll
                         for (int r = 0; r < D; ++r) sumw[r] += f * e[r] * ev;
+                        sd[0] += f * e[0] * e[0];
+                        sd[1] += f * e[0] * e[1];
+                        sd[2] += f * e[0] * e[2];
+                        sd[3] += f * e[1] * e[1];
+                        sd[4] += f * e[1] * e[2];
+                        sd[5] += f * e[2] * e[2];
                     }
                 }
             }
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
-            sd[0] += f * e[0] * e[0];
-            sd[1] += f * e[0] * e[1];
-            sd[2] += f * e[0] * e[2];
-            sd[3] += f * e[1] * e[1];
-            sd[4] += f * e[1] * e[2];
-            sd[5] += f * e[2] * e[2];
         }
-        if (sdiag32) {   // the FP32 diagonal block of the inner operator: viscous + inertia
+        if (sdiag32) {   // the row's wall part of the viscous diagonal block and its FP32 inertia
 #pragma unroll
             for (int t = 0; t < 6; ++t)
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sd[t] += __shfl_xor_sync(0xffffffffu, sd[t], o);
             if (lane == 0) {
-                const float in32 = P.inert32[ti];
-                sd[0] += in32;
-                sd[3] += in32;
-                if (D == 3) sd[5] += in32;
-#pragma unroll
-                for (int t = 0; t < 6; ++t) sdiag32[(size_t)i * 6 + t] = sd[t];
+                float4* o = reinterpret_cast<float4*>(sdiag32 + (size_t)i * 8);
+                o[0] = make_float4(sd[0], sd[1], sd[2], sd[3]);
+                o[1] = make_float4(sd[4], sd[5], P.inert32[ti], 0.f);
             }
         }
         // - C p over the row's P-neighbours (FP64)
@@ -227,11 +239,13 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 // lane, its D values at slice base * D + (e*D + d)*32 + lane: coalesced):
 //   k_ct_apply32   t = C^T s per particle over the transposed P-lists, after
 //                  the iteration's convergence test;
-//   k_visc_pen32   y_i = (inertia + sum_all f e (x) e) s_i
-//                        - sum_{fluid j} g (g . s_j) + sum_k lambda_k C_ik t_k
-//                  with g = sqrt(f) e (f >= 0, so a fluid pair's block
-//                  -f e (x) e is -g (x) g: D floats a slot against D*D for a
-//                  block), and (s, y) into the iteration's rho slot.
+//   k_visc_pen32   y_i = (inertia + sum_{wall j} f e (x) e) s_i
+//                        + sum_{fluid j} g (g . (s_i - s_j)) + sum_k lambda_k C_ik t_k
+//                  with g = sqrt(f) e (f >= 0, so a fluid pair's terms
+//                  f e (x) e are g (x) g: D floats a slot against D*D for a
+//                  block), and (s, y) into the iteration's rho slot.  The
+//                  pairs act on differences s_i - s_j, so the viscous sum has
+//                  no cancellation between a large diagonal and its row.
 // Same recurrences and flags as k_spmv32.
 constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
@@ -272,6 +286,37 @@ __global__ void __launch_bounds__(256) k_ct_apply32(int N, const long long* __re
     t[k] = s;
 }
 
+// The viscous part of row i in FP32 from the sliced pair terms:
+// yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)).
+template <int D>
+__device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, const float* __restrict__ sdiag,
+                                           const int* __restrict__ nfc, const long long* __restrict__ sptr,
+                                           const int* __restrict__ acol, const float* __restrict__ pes,
+                                           const float* __restrict__ x, float* yv)
+{
+    const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
+    const float4 s1 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8 + 4);
+    yv[0] = s0.x * xi[0] + s0.y * xi[1] + s0.z * xi[2];
+    yv[1] = s0.y * xi[0] + s0.w * xi[1] + s1.x * xi[2];
+    yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
+    const long long base = sptr[i >> 5];
+    const int* cp = acol + base + lane;
+    const float* vp = pes + base * D + lane;
+    const int n = nfc[i];
+#pragma unroll 4
+    for (int k = 0; k < n; ++k) {
+        const int col = __ldcs(cp + (long long)k * 32);
+        float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[d] = __ldcs(vp + ((long long)k * D + d) * 32);
+        float gx = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - x[(size_t)col * D + d]);
+#pragma unroll
+        for (int d = 0; d < D; ++d) yv[d] += gx * g[d];
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(128)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
@@ -289,29 +334,11 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
         float xi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
-        const float* S = sdiag + (size_t)i * 6;
         float yv[3];
-        yv[0] = S[0] * xi[0] + S[1] * xi[1] + S[2] * xi[2];
-        yv[1] = S[1] * xi[0] + S[3] * xi[1] + S[4] * xi[2];
-        yv[2] = S[2] * xi[0] + S[4] * xi[1] + S[5] * xi[2];
-        {   // fluid pairs: - g (g . x_j)
-            const long long base = sptr[i >> 5];
-            const int* cp = acol + base + lane;
-            const float* vp = pes + base * D + lane;
-            const int n = nfc[i];
-#pragma unroll 4
-            for (int k = 0; k < n; ++k) {
-                const int col = __ldcs(cp + (long long)k * 32);
-                float g[3] = {0.f, 0.f, 0.f};
+        visc_row32<D>(i, lane, xi, sdiag, nfc, sptr, acol, pes, x, yv);
+        const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
-                for (int d = 0; d < D; ++d) g[d] = __ldcs(vp + ((long long)k * D + d) * 32);
-                float gx = 0.f;
-#pragma unroll
-                for (int d = 0; d < D; ++d) gx += g[d] * x[(size_t)col * D + d];
-#pragma unroll
-                for (int d = 0; d < D; ++d) yv[d] -= gx * g[d];
-            }
-        }
+        for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
         {   // C Lambda t over the row's P-neighbours
             const long long base = psptr[i >> 5];
             const int* cp = pscol + base + lane;
@@ -395,6 +422,47 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
         }
         __syncthreads();
     }
+}
+
+// r = b - A x on the pair-term path, one thread per row: the viscous part in
+// FP32 on x32 from the sliced pair terms (as the inner operator), inertia and
+// C Lambda t (t = C^T x) in FP64; (r, r) -> *out.
+template <int D>
+__global__ void __launch_bounds__(128)
+k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __restrict__ nfc, const long long* __restrict__ sptr,
+              const int* __restrict__ acol, const float* __restrict__ pes, const float* __restrict__ sdiag,
+              const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
+              const double* __restrict__ cval, const double* __restrict__ t, const double* __restrict__ x,
+              const float* __restrict__ x32, const double* __restrict__ b, double* __restrict__ r,
+              double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (i < Nf) {
+        float xi[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) xi[d] = x32[(size_t)i * D + d];
+        float yv[3];
+        visc_row32<D>(i, i & 31, xi, sdiag, nfc, sptr, acol, pes, x32, yv);
+        double y[3] = {(double)yv[0], (double)yv[1], (double)yv[2]};
+        const long long pb = nptrP[i];
+        const int np = ncp[i];
+        for (int a = 0; a < np; ++a) {
+            const int k = nindP[pb + a];
+            const double lt = P.lambda[type[k]] * t[k];
+#pragma unroll
+            for (int d = 0; d < D; ++d) y[d] += cval[(pb + a) * D + d] * lt;
+        }
+        const double inert = P.density[type[i]] * P.vol / P.vol / P.dt;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const size_t k = (size_t)i * D + d;
+            const double rv = b[k] - (inert * x[k] + y[d]);
+            r[k] = rv;
+            acc += rv * rv;
+        }
+    }
+    reduce_finalize(acc, partials, counter, out);
 }
 
 void launch_apply32(mph_case* c, const float* x, float* y, int cap)
@@ -488,7 +556,7 @@ int launch_pair_terms(mph_case* c)
     float* sdiag = nullptr;
     float* cvl = nullptr;
     if (c->step_pairs) {   // FP32 inner operator on the pair terms
-        if (!d.sdiag32) MPH_CUDA(cudaMalloc((void**)&d.sdiag32, (size_t)P.Nf * 6 * sizeof(float)));
+        if (!d.sdiag32) MPH_CUDA(cudaMalloc((void**)&d.sdiag32, (size_t)P.Nf * 8 * sizeof(float)));
         MPH_TRY(grow_f(&d.cvl32, &d.cap_cvl32, ncv));
         sdiag = d.sdiag32;
         cvl = d.cvl32;
@@ -571,6 +639,19 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
     const long long nv = (long long)P.Nf * c->dim;
     { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
+    if (c->step_pairs) {
+        const unsigned gr = grid_for(P.Nf, 128);
+        if (c->dim == 2) {
+            { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+            { k_resid_pairs<2><<<gr, 128, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+                                                          d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+        } else {
+            { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+            { k_resid_pairs<3><<<gr, 128, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+                                                          d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
+        }
+        return;
+    }
     if (c->dim == 2) {
         { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
         { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,

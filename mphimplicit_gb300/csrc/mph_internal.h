@@ -211,7 +211,7 @@ struct mph_case {
     int max_outer = 50;                 // mixed form: refinement steps
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
-    bool inner_blocks = true;           // factored form: inner FP32 SpMV on assembled blocks (else pair terms)
+    bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
