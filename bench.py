@@ -152,16 +152,18 @@ def pair_apply_bytes(prof, scal, dim):
     """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
     (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
     transposed P-list slot, entry counts and slice pointers, s gathered once,
-    t written.  k_visc_pen32: column + D FP32 values of g = sqrt(f) e per
-    fluid slot, column + D FP32 lambda C per P-slot, the 6-entry diagonal,
-    row lengths and slice pointers, s read once, t gathered once, y written."""
+    t written.  k_visc_pen32: column + D FP16 values of g = sqrt(f) e per
+    fluid slot, column + D FP32 lambda C per P-slot, the 8-float diagonal /
+    inertia record, row lengths, slice pointers and scales, s read once, t
+    gathered once, y written."""
     nf = int(scal["FluidParticleEnd"])
     n = int(scal["ParticleCount"])
     slots = scal["NonzeroCountA"] / (dim * dim)
     pslots = scal["NonzeroCountC"] / dim
     nsl, nct = (nf + 31) // 32, (n + 31) // 32
     ct = pslots * (dim * 4 + 4) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
-    vp = (slots + pslots) * (dim * 4 + 4) + nf * (24 + 8) + 2 * (nsl + 1) * 8 + 2 * dim * nf * 4 + n * 4
+    vp = slots * (dim * 2 + 4) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
+        + 2 * dim * nf * 4 + n * 4
     return ct + vp
 
 

@@ -120,22 +120,6 @@ __global__ void __launch_bounds__(128) k_vector_p(DevParams P, const int* __rest
     pvec[i] = p + sum;
 }
 
-struct Level0Map {
-    int mn[3], cnt[3], st[3];
-    int S;          // st0*st1*st2
-    int folded;     // 1 if some active axis has fewer than 3 grid cells
-};
-
-template <int D>
-__device__ __forceinline__ int stencil_slot(const DevParams& P, const Level0Map& M, const int* gi, int keyj)
-{
-    int jc[3];
-    key_coords(P, keyj, jc);
-    int o[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) o[d] = ((jc[d] - M.mn[d]) - gi[d] + 1 + M.cnt[d]) % M.cnt[d];
-    return M.st[2] * M.st[1] * o[0] + M.st[2] * o[1] + o[2];
-}
 
 template <int D>
 __device__ __forceinline__ void flush_part(double* __restrict__ prow, int slot, const double (&acc)[D][D], bool add)
@@ -497,7 +481,10 @@ int launch_assemble(mph_case* c)
         if (c->step_pairs) MPH_TRY(launch_ct_slices(c));
         MPH_TRY(launch_pair_terms(c));
     }
-    if (c->cell_assembly) MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
+    if (c->cell_assembly) {
+        if (c->step_pairs) MPH_TRY(launch_part_pairs(c, M, &cells));   // no blocks: level-0 stencils and D^-1 only
+        else MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
+    }
     const int* only = cells ? c->d.cell_flags : nullptr;
     float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;
     if (D == 2) {

@@ -23,6 +23,8 @@
 // position difference, against the nine-entry block and its accumulation of
 // the assembled form; in the residual only inertia and C Lambda C^T (about 20
 // P-slots a row) are FP64.
+#include <cuda_fp16.h>
+
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -242,10 +244,14 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 //   k_visc_pen32   y_i = (inertia + sum_{wall j} f e (x) e) s_i
 //                        + sum_{fluid j} g (g . (s_i - s_j)) + sum_k lambda_k C_ik t_k
 //                  with g = sqrt(f) e (f >= 0, so a fluid pair's terms
-//                  f e (x) e are g (x) g: D floats a slot against D*D for a
-//                  block), and (s, y) into the iteration's rho slot.  The
-//                  pairs act on differences s_i - s_j, so the viscous sum has
-//                  no cancellation between a large diagonal and its row.
+//                  f e (x) e are g (x) g), read as FP16 scaled per slice: 6
+//                  bytes a slot in 3-D against 36 for an FP32 block (the
+//                  viscous part is a few 1e-3 of the operator, so the 2^-11
+//                  rounding of g moves the inner operator by ~1e-5 of itself;
+//                  the FP64 outer residual takes the FP32 g).  (s, y) goes
+//                  into the iteration's rho slot.  The pairs act on
+//                  differences s_i - s_j, so the viscous sum has no
+//                  cancellation between a large diagonal and its row.
 // Same recurrences and flags as k_spmv32.
 constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
@@ -287,11 +293,13 @@ __global__ void __launch_bounds__(256) k_ct_apply32(int N, const long long* __re
 }
 
 // The viscous part of row i in FP32 from the sliced pair terms:
-// yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)).
-template <int D>
+// yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)), with g from the FP32
+// slices (pes32) or from the FP16 slices times the slice scale (HALF).
+template <int D, bool HALF>
 __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, const float* __restrict__ sdiag,
                                            const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                            const int* __restrict__ acol, const float* __restrict__ pes,
+                                           const unsigned short* __restrict__ pes16, const float* __restrict__ pscale,
                                            const float* __restrict__ x, float* yv)
 {
     const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
@@ -301,27 +309,34 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
     const long long base = sptr[i >> 5];
     const int* cp = acol + base + lane;
-    const float* vp = pes + base * D + lane;
+    const long long vo = base * D + lane;
     const int n = nfc[i];
+    float ys[3] = {0.f, 0.f, 0.f};
 #pragma unroll 4
     for (int k = 0; k < n; ++k) {
         const int col = __ldcs(cp + (long long)k * 32);
         float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int d = 0; d < D; ++d) g[d] = __ldcs(vp + ((long long)k * D + d) * 32);
+        for (int d = 0; d < D; ++d) {
+            const long long o = vo + ((long long)k * D + d) * 32;
+            g[d] = HALF ? __half2float(__ushort_as_half(__ldcs(pes16 + o))) : __ldcs(pes + o);
+        }
         float gx = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - x[(size_t)col * D + d]);
 #pragma unroll
-        for (int d = 0; d < D; ++d) yv[d] += gx * g[d];
+        for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
     }
+    const float s2 = HALF ? pscale[i >> 5] * pscale[i >> 5] : 1.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) yv[d] += ys[d] * s2;
 }
 
 template <int D>
 __global__ void __launch_bounds__(128)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
-             const float* __restrict__ pes, const float* __restrict__ sdiag, const int* __restrict__ ncp,
-             const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
+             const unsigned short* __restrict__ pes16, const float* __restrict__ pscale, const float* __restrict__ sdiag,
+             const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
              const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
@@ -335,7 +350,7 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
         float yv[3];
-        visc_row32<D>(i, lane, xi, sdiag, nfc, sptr, acol, pes, x, yv);
+        visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv);
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
@@ -364,14 +379,17 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 // the sliced layout, one CTA per slice of 32 rows: chunks of kLtsK entries of
 // the 32 rows are read row by row (coalesced) into shared memory and written
 // slice-wise (coalesced), padding slots as zeros.  PAIRS: the values are the
-// pair terms (e, f), stored as g = sqrt(f) e.
+// pair terms (e, f), stored as g = sqrt(f) e in FP32 and, for the inner
+// operator, in FP16 scaled per slice (g / sigma, sigma = the slice's largest
+// |g| component / 2^15: relative rounding 2^-11, no overflow).
 constexpr int kLtsK = 32;
 
 template <int D, bool PAIRS>
 __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long long* __restrict__ sptr, const int* __restrict__ cnt,
                                                         const long long* __restrict__ rptr, const int* __restrict__ cols,
                                                         const float4* __restrict__ pe32, const float* __restrict__ v32,
-                                                        int* __restrict__ scol, float* __restrict__ sval)
+                                                        int* __restrict__ scol, float* __restrict__ sval,
+                                                        unsigned short* __restrict__ sval16, float* __restrict__ sscale)
 {
     constexpr int W = kLtsK * D + 1;   // odd row stride: no bank conflicts
     __shared__ float tile[32 * W];
@@ -387,6 +405,27 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
     __syncthreads();
     const long long sb = sptr[sl];
     const int w = (int)((sptr[sl + 1] - sb) / 32);   // entries per row of the slice
+    float inv16 = 0.f;
+    if (PAIRS) {   // the slice's largest |g| component maps to 2^15 in the FP16 copy
+        __shared__ float wmax[8];
+        float m = 0.f;
+        for (int t = threadIdx.x; t < 32 * w; t += blockDim.x) {
+            const int r = t / w, k = t % w;
+            if (k < rn[r]) {
+                const float4 pv = pe32[rb[r] + k];
+                m = fmaxf(m, sqrtf(pv.w) * fmaxf(fabsf(pv.x), fmaxf(fabsf(pv.y), fabsf(pv.z))));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+        __syncthreads();
+        m = 0.f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) m = fmaxf(m, wmax[k]);
+        const float sigma = m / 32768.f;
+        inv16 = m > 0.f ? 1.f / sigma : 0.f;
+        if (threadIdx.x == 0) sscale[sl] = sigma;
+    }
     for (int k0 = 0; k0 < w; k0 += kLtsK) {
         const int kc = min(kLtsK, w - k0);
         for (int t = threadIdx.x; t < 32 * kLtsK; t += blockDim.x) {
@@ -414,7 +453,9 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
         __syncthreads();
         for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
             const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
-            sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+            const float v = tile[ln * W + ec];
+            sval[sb * D + (long long)k0 * D * 32 + o] = v;
+            if (PAIRS) sval16[sb * D + (long long)k0 * D * 32 + o] = __half_as_ushort(__float2half_rn(v * inv16));
         }
         for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
             const int ln = o & 31, kl = o >> 5;
@@ -443,7 +484,7 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x32[(size_t)i * D + d];
         float yv[3];
-        visc_row32<D>(i, i & 31, xi, sdiag, nfc, sptr, acol, pes, x32, yv);
+        visc_row32<D, false>(i, i & 31, xi, sdiag, nfc, sptr, acol, pes, nullptr, nullptr, x32, yv);
         double y[3] = {(double)yv[0], (double)yv[1], (double)yv[2]};
         const long long pb = nptrP[i];
         const int np = ncp[i];
@@ -474,12 +515,221 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     const unsigned gv = grid_for(P.Nf, 128);
     if (c->dim == 2) {
         { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<2><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+        { k_visc_pen32<2><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
                                                      d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     } else {
         { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<3><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+        { k_visc_pen32<3><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
                                                      d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+    }
+}
+
+// ---- level-0 multigrid stencils and D^-1 on the pair-term path --------------------
+// The Galerkin level-0 matrix sums each fluid row's blocks of A per neighbour
+// cell (part[i][slot], read by k_mg_level0).  Without assembled blocks:
+//  - viscous: a fluid neighbour j gives -f e (x) e to the slot of its cell,
+//    and every neighbour (fluid or wall) f e (x) e to the row's own slot,
+//    with the inertia;
+//  - C Lambda C^T: row i's blocks sum, over its P-neighbours k, to
+//    lambda_k C_ik (x) W_k(c), where W_k(c) is the sum of C_jk over the
+//    transposed P-list of k inside cell c.  Every such j is a neighbour of i
+//    (2 RadiusP < MaxRadius, the condition of the factored form) and the
+//    cells are at least MaxRadius wide, so W_k has at most 2^D cells.
+// Both kernels sum in a fixed order (no atomics), so the result is the same
+// bits on every run.  A row whose neighbour list is not grouped into at most
+// 3^D cells, or one of whose P-neighbours has more than kWBins cells, flags its
+// cell; the per-row FP64 kernel then assembles that cell's rows.
+constexpr int kWBins = 8;
+
+// W_k: (cell key, sum of C_jk over the rows j of that cell) for every particle
+template <int D>
+__global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
+                                                  const float* __restrict__ ct_v32, const int* __restrict__ key,
+                                                  int* __restrict__ wkey, float* __restrict__ wval)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    int bk[kWBins];
+    float bw[kWBins][3];
+#pragma unroll
+    for (int b = 0; b < kWBins; ++b) {
+        bk[b] = -1;
+        bw[b][0] = bw[b][1] = bw[b][2] = 0.f;
+    }
+    bool over = false;
+    const long long e1 = ctptr[k + 1];
+    for (long long e = ctptr[k]; e < e1; ++e) {
+        const int kj = key[ct_j[e]];
+        float cv[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) cv[d] = ct_v32[e * D + d];
+        bool placed = false;
+#pragma unroll
+        for (int b = 0; b < kWBins; ++b) {   // bins fill in order: a match comes before the first free bin
+            if (!placed && (bk[b] == kj || bk[b] < 0)) {
+                bk[b] = kj;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) bw[b][d] += cv[d];
+                placed = true;
+            }
+        }
+        over = over || !placed;
+    }
+#pragma unroll
+    for (int b = 0; b < kWBins; ++b) {
+        wkey[(size_t)k * kWBins + b] = (over && b == 0) ? -2 : bk[b];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) wval[((size_t)k * kWBins + b) * 3 + d] = bw[b][d];
+    }
+}
+
+// part[i][slot] (FP64 store of FP32 sums) and invDiag of every fluid row, one
+// warp per row with the row's stencil accumulated in shared memory.
+template <int D>
+__global__ void __launch_bounds__(kPairWarps * 32)
+k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* __restrict__ type, const int* __restrict__ nc,
+             const int* __restrict__ nfc, const long long* __restrict__ nptr, const int* __restrict__ nind,
+             const float4* __restrict__ pe32, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
+             const int* __restrict__ nindP, const float* __restrict__ cval32, const float* __restrict__ cvl32,
+             const int* __restrict__ wkey, const float* __restrict__ wval, double* __restrict__ part,
+             double* __restrict__ invDiag, int* __restrict__ cell_flags)
+{
+    constexpr int DD = D * D;
+    constexpr int SMAX = D == 3 ? 27 : 9;
+    __shared__ float sacc[kPairWarps][SMAX * DD];
+    __shared__ int srun[kPairWarps][SMAX + 1];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    float* acc = sacc[wl];
+    int* run = srun[wl];
+    const unsigned full = 0xffffffffu;
+    for (int i = wid; i < P.Nf; i += nwarps) {
+        for (int t = lane; t < SMAX * DD; t += 32) acc[t] = 0.f;
+        const int ki = key[i];
+        int ic[3], gi[3];
+        key_coords(P, ki, ic);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gi[d] = ic[d] - M.mn[d];
+        const long long nb = nptr[i];
+        const int n = nc[i], nf = nfc[i];
+        // runs of equal cell in the fluid part of the neighbour list
+        int nrun = 0;
+        for (int k0 = 0; k0 < nf; k0 += 32) {
+            const int k = k0 + lane;
+            const int kj = k < nf ? key[nind[nb + k]] : -1;
+            int kp = __shfl_up_sync(full, kj, 1);
+            if (lane == 0) kp = k0 > 0 ? key[nind[nb + k0 - 1]] : -1;
+            const bool start = k < nf && kj != kp;
+            const unsigned bal = __ballot_sync(full, start);
+            const int at = nrun + __popc(bal & ((1u << lane) - 1u));
+            if (start && at < SMAX) run[at] = k;
+            nrun += __popc(bal);
+        }
+        bool bad = nrun > SMAX;
+        if (lane == 0) run[min(nrun, SMAX)] = nf;
+        __syncwarp();
+        // viscous: lane r sums run r in list order; every term also enters the own slot
+        float tv[DD];
+#pragma unroll
+        for (int t = 0; t < DD; ++t) tv[t] = 0.f;
+        if (!bad && lane < nrun) {
+            const int k0 = run[lane], k1 = run[lane + 1];
+            float rsum[DD];
+#pragma unroll
+            for (int t = 0; t < DD; ++t) rsum[t] = 0.f;
+            for (int k = k0; k < k1; ++k) {
+                const float4 pv = pe32[nb + k];
+                const float e[3] = {pv.x, pv.y, pv.z};
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) rsum[r * D + c] += pv.w * e[r] * e[c];
+            }
+            const int slot = stencil_slot<D>(P, M, gi, key[nind[nb + k0]]);
+#pragma unroll
+            for (int t = 0; t < DD; ++t) {
+                acc[slot * DD + t] = -rsum[t];
+                tv[t] = rsum[t];
+            }
+        }
+        for (int k = nf + lane; k < n; k += 32) {   // wall neighbours: own slot only
+            const float4 pv = pe32[nb + k];
+            const float e[3] = {pv.x, pv.y, pv.z};
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) tv[r * D + c] += pv.w * e[r] * e[c];
+        }
+        // lambda_k C_ik[r]^2 for the diagonal of the own block
+        const long long pb = nptrP[i];
+        const int np = ncp[i];
+        float dp[3] = {0.f, 0.f, 0.f};
+        for (int a = lane; a < np; a += 32) {
+#pragma unroll
+            for (int r = 0; r < D; ++r) dp[r] += cvl32[(pb + a) * D + r] * cval32[(pb + a) * D + r];
+        }
+#pragma unroll
+        for (int t = 0; t < DD; ++t)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tv[t] += __shfl_xor_sync(full, tv[t], o);
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) dp[r] += __shfl_xor_sync(full, dp[r], o);
+        __syncwarp();
+        const int si = stencil_slot<D>(P, M, gi, ki);
+        const float in32 = P.inert32[type[i]];
+        if (lane == 0 && !bad) {
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) acc[si * DD + r * D + c] += tv[r * D + c] + (r == c ? in32 : 0.f);
+        }
+        __syncwarp();
+        // C Lambda C^T: P-neighbours in order; the bins of one W_k are distinct cells
+        for (int a0 = 0; a0 < np && !bad; a0 += 32) {
+            const int a = a0 + lane;
+            int kk = 0;
+            float cl[3] = {0.f, 0.f, 0.f};
+            if (a < np) {
+                kk = nindP[pb + a];
+#pragma unroll
+                for (int r = 0; r < D; ++r) cl[r] = cvl32[(pb + a) * D + r];
+            }
+            const int na = min(32, np - a0);
+            for (int q = 0; q < na; ++q) {
+                const int k = __shfl_sync(full, kk, q);
+                float cq[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) cq[r] = __shfl_sync(full, cl[r], q);
+                bool over = false;
+                for (int t = lane; t < kWBins * DD; t += 32) {
+                    const int b = t / DD, rs = t - b * DD;
+                    const int wk = wkey[(size_t)k * kWBins + b];
+                    if (wk == -2) over = true;
+                    if (wk < 0) continue;
+                    const int slot = stencil_slot<D>(P, M, gi, wk);
+                    acc[slot * DD + rs] += cq[rs / D] * wval[((size_t)k * kWBins + b) * 3 + rs % D];
+                }
+                bad = __any_sync(full, over) || bad;
+                __syncwarp();
+            }
+        }
+        if (bad) {
+            if (lane == 0) cell_flags[ki] = 1;   // the per-row kernel assembles this cell
+            continue;
+        }
+        double* prow = part + (size_t)i * M.S * DD;
+        for (int t = lane; t < SMAX * DD; t += 32) prow[t] = (double)acc[t];
+        if (lane == 0) {
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                const float dg = in32 + tv[r * D + r] + dp[r];
+                invDiag[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -581,6 +831,15 @@ int launch_pairs_to_slices(mph_case* c)
     const int D = c->dim;
     if (c->nslices == 0) return MPH_OK;
     MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
+    if (c->nslots * D > d.cap_pes16) {
+        if (d.pes16) cudaFree(d.pes16);
+        d.pes16 = nullptr;
+        d.cap_pes16 = 0;
+        const long long n = c->nslots * D + c->nslots * D / 8 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.pes16, (size_t)n * sizeof(unsigned short)));
+        d.cap_pes16 = n;
+    }
+    if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)(c->nslices + 1) * sizeof(float)));
     if (!d.psptr) {
         MPH_CUDA(cudaMalloc((void**)&d.psptr, (size_t)(c->nslices + 1) * sizeof(long long)));
         MPH_CUDA(cudaMalloc((void**)&d.pswidth, (size_t)(c->nslices + 1) * sizeof(int)));
@@ -591,14 +850,14 @@ int launch_pairs_to_slices(mph_case* c)
     MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * D));
     if (D == 2) {
         { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, d.pes16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       d.pscol, d.psval); MPH_COUNT_LAUNCH(); }
+                                                                       d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, d.pes16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       d.pscol, d.psval); MPH_COUNT_LAUNCH(); }
+                                                                       d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }
@@ -622,10 +881,10 @@ int launch_ct_slices(mph_case* c)
     MPH_TRY(grow_f(&d.ctsval, &d.cap_ctsval, slots * D));
     if (D == 2) {
         { k_list_to_slices<2, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
-                                                               d.ctsval); MPH_COUNT_LAUNCH(); }
+                                                               d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
-                                                               d.ctsval); MPH_COUNT_LAUNCH(); }
+                                                               d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }
@@ -663,6 +922,47 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
                                                                    d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter,
                                                                    out); MPH_COUNT_LAUNCH(); }
     }
+}
+
+// Level-0 partial stencils and D^-1 on the pair-term path (instead of the
+// cell-block kernel).  *done = false when the grids are too small for it
+// (an axis with fewer than 3 cells): the per-row kernel then assembles every
+// row; otherwise per-cell fallback flags are left in c->d.cell_flags.
+int launch_part_pairs(mph_case* c, const Level0Map& M, bool* done)
+{
+    *done = false;
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    const int D = c->dim;
+    for (int a = 0; a < D; ++a)
+        if (P.cc[a] < 3 || M.cnt[a] < 3) return MPH_OK;
+    if (!d.wkey) {
+        MPH_CUDA(cudaMalloc((void**)&d.wkey, (size_t)P.N * kWBins * sizeof(int)));
+        MPH_CUDA(cudaMalloc((void**)&d.wval, (size_t)P.N * kWBins * 3 * sizeof(float)));
+    }
+    const long long fbytes = (long long)(P.T + 1) * sizeof(int);   // capacity kept in bytes
+    if (fbytes > d.cap_cell_flags) {
+        if (d.cell_flags) cudaFree(d.cell_flags);
+        d.cell_flags = nullptr;
+        d.cap_cell_flags = 0;
+        MPH_CUDA(cudaMalloc((void**)&d.cell_flags, (size_t)(fbytes + fbytes / 8 + 1024)));
+        d.cap_cell_flags = fbytes + fbytes / 8 + 1024;
+    }
+    MPH_CUDA(cudaMemsetAsync(d.cell_flags, 0, (size_t)(P.T + 1) * sizeof(int), c->stream));
+    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
+    if (D == 2) {
+        { k_ct_cells<2><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.key, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
+        { k_part_pairs<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.part, d.invDiag,
+                                                               d.cell_flags); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_ct_cells<3><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.key, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
+        { k_part_pairs<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.part, d.invDiag,
+                                                               d.cell_flags); MPH_COUNT_LAUNCH(); }
+    }
+    *done = true;
+    return MPH_OK;
 }
 
 }  // namespace mph

@@ -178,8 +178,15 @@ void launch_mg_invd(mph_case* c)
 }
 
 // ---- V-cycle row operations ------------------------------------------------------
-// Q - A S for one row (the reference's csrmv with alpha = -1, beta = 1)
-template <int D, typename T>
+// Q - A S for one row (the reference's csrmv with alpha = -1, beta = 1).
+// UNROLL (the cluster kernel of the small levels, where a few SMs run each
+// sweep and every row's loads wait in line): with the full 3^D stencil the
+// loops are unrolled below the outer axis, so a row's coefficient and S loads
+// are issued a stencil plane at a time instead of one latency per stencil
+// cell (fully unrolled, the kernel spills), and the wrapped column
+// coordinates are formed once per axis; the summation order is the same.
+// The grid-wide levels keep the plain loop (measured faster there).
+template <int D, typename T, bool UNROLL = false>
 __device__ __forceinline__ T row_residual(const LevelK& L, const T* __restrict__ cofT, const T* __restrict__ Q,
                                           const T* __restrict__ S, int row)
 {
@@ -187,6 +194,29 @@ __device__ __forceinline__ T row_residual(const LevelK& L, const T* __restrict__
     int p[3];
     grid_coords(L, g, p);
     T sum = 0;
+    constexpr int SZ = D == 3 ? 3 : 1;
+    if (UNROLL && L.st[0] == 3 && L.st[1] == 3 && L.st[2] == SZ) {
+        int ys[3], zs[SZ];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ys[k] = ((p[1] + k - 1 + L.cnt[1]) % L.cnt[1]) * L.cnt[2];
+#pragma unroll
+        for (int k = 0; k < SZ; ++k) zs[k] = (p[2] + k - 1 + L.cnt[2]) % L.cnt[2];
+#pragma unroll 1
+        for (int ix = 0; ix < 3; ++ix) {
+            const int xw = ((p[0] + ix - 1 + L.cnt[0]) % L.cnt[0]) * (L.cnt[1] * L.cnt[2]);
+            const T* cx = cofT + (size_t)ix * (3 * SZ * D) * L.rows + row;
+#pragma unroll
+            for (int iy = 0; iy < 3; ++iy)
+#pragma unroll
+                for (int iz = 0; iz < SZ; ++iz) {
+                    const int jg = xw + ys[iy] + zs[iz];
+#pragma unroll
+                    for (int sD = 0; sD < D; ++sD)
+                        sum += (-cx[(size_t)((iy * SZ + iz) * D + sD) * L.rows]) * S[jg * D + sD];
+                }
+        }
+        return Q[row] + sum;
+    }
     int e = 0;
     for (int ix = 0; ix < L.st[0]; ++ix)
         for (int iy = 0; iy < L.st[1]; ++iy)
@@ -348,7 +378,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
     auto jacobi = [&](int l, int t0, int nt, auto sync) {
         const LevelK& L = A.L[l];
         for (int row = t0; row < L.rows; row += nt) {
-            const T r = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
+            const T r = row_residual<D, T, true>(L, A.cof[l], A.Q[l], cur[l], row);
             oth[l][row] = cur[l][row] + A.invd[l][row] * r;
         }
         sync();
@@ -366,7 +396,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
         const int sweeps = (l == A.depth - 1) ? 4 : 2;
         for (int k = 0; k < sweeps; ++k) jacobi(l, t0, nt, sync);
         if (l < A.depth - 1) {
-            for (int row = t0; row < L.rows; row += nt) A.R[l][row] = row_residual<D, T>(L, A.cof[l], A.Q[l], cur[l], row);
+            for (int row = t0; row < L.rows; row += nt) A.R[l][row] = row_residual<D, T, true>(L, A.cof[l], A.Q[l], cur[l], row);
             sync();
         }
     };

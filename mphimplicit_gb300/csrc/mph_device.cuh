@@ -116,6 +116,27 @@ __device__ __forceinline__ void key_coords(const DevParams& P, int k, int* c)
     c[2] = k % P.cc[2];
 }
 
+// The level-0 multigrid grid (the fluid-cell bounding box of the neighbour
+// grid) as the assembly sees it: a row's partial stencil has one D x D block
+// per neighbour cell slot (st0*st1*st2 slots, periodic on the grid index).
+struct Level0Map {
+    int mn[3], cnt[3], st[3];
+    int S;          // st0*st1*st2
+    int folded;     // 1 if some active axis has fewer than 3 grid cells
+};
+
+// slot of the cell of key keyj in the stencil of the cell at grid coords gi
+template <int D>
+__device__ __forceinline__ int stencil_slot(const DevParams& P, const Level0Map& M, const int* gi, int keyj)
+{
+    int jc[3];
+    key_coords(P, keyj, jc);
+    int o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o[d] = ((jc[d] - M.mn[d]) - gi[d] + 1 + M.cnt[d]) % M.cnt[d];
+    return M.st[2] * M.st[1] * o[0] + M.st[2] * o[1] + o[2];
+}
+
 inline unsigned grid_for(long long n, int block)
 {
     long long g = (n + block - 1) / block;

@@ -131,6 +131,11 @@ struct DeviceState {
     // columns, D FP32 values a slot
     float* pes32 = nullptr;
     long long cap_pes32 = 0;
+    unsigned short* pes16 = nullptr;   // the inner operator's copy of g: FP16, scaled per slice
+    long long cap_pes16 = 0;
+    float* pscale = nullptr;           // per slice: g = pes16 * pscale
+    int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
+    float* wval = nullptr;             // the sums of C_jk over each (level-0 stencils of the pair path)
     float* sdiag32 = nullptr;
     float* cvl32 = nullptr;
     long long cap_cvl32 = 0;
@@ -310,6 +315,7 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
 void launch_apply32(mph_case* c, const float* x, float* y, int cap);
 int launch_pairs_to_slices(mph_case* c);
 int launch_ct_slices(mph_case* c);
+int launch_part_pairs(mph_case* c, const struct Level0Map& M, bool* done);
 void launch_mg_level0(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);

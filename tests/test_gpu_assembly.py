@@ -122,7 +122,8 @@ def test_pair_term_inner_operator_solves(engine_lib, case):
 def test_sliced_pair_terms_match_blocks(engine_lib, case):
     """The inner operator on the sliced pair terms (g = sqrt(f) e, sliced
     P-lists and transposed P-lists) is the FP32 block operator in another
-    storage: same block columns, and a solve with either takes about the same
+    storage: same block columns, the same D^-1 and multigrid levels (built
+    without blocks on the pair path), and a solve with either takes about the same
     iterations to the same velocity (both are FP32 roundings of one operator,
     the outer residual is FP64).  The reference's tolerance 1e-6: the factored
     form, which the pair terms need, is not used far below it."""
@@ -134,11 +135,17 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
         for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
             g.stage(st)
         cols = g.export("CsrIndA")
+        mg = [g.export("InvDiagA")] + [g.export(f"MultiGridCsrCofA:{L}") for L in range(int(g.scalars()["MultiGridDepth"]))]
         g.stage("solve")
         assert g.solve_stats()["status"] == 0
-        cs[blocks] = (g, cols)
-    (a, ia), (b, ib) = cs[0], cs[1]
+        cs[blocks] = (g, cols, mg)
+    (a, ia, ma), (b, ib, mb) = cs[0], cs[1]
     assert np.array_equal(ia, ib)
+    # D^-1 and the multigrid levels: from the pair terms (k_part_pairs) and
+    # from the FP32 blocks, FP32 sums in different orders
+    assert len(ma) == len(mb)
+    for L, (x, y) in enumerate(zip(ma, mb)):
+        assert rel(x, y) <= 1e-6, L
     sa, sb = a.solve_stats(), b.solve_stats()
     assert (sa["inner_form"], sb["inner_form"]) == (2, 1)
     assert abs(sa["iter"] - sb["iter"]) <= max(2, sb["iter"] // 10), (sa, sb)
