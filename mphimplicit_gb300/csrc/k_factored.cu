@@ -584,7 +584,12 @@ __global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __rest
 }
 
 // part[i][slot] (FP64 store of FP32 sums) and invDiag of every fluid row, one
-// warp per row with the row's stencil accumulated in shared memory.
+// warp per row with the row's stencil accumulated in shared memory.  Global
+// loads are issued ahead of the ordered accumulation: the cell keys of the
+// next 32 neighbours while a chunk is scanned for runs, and the W_k bins of
+// up to 32 P-neighbours at once into a per-warp stage.
+constexpr int kPartStage = 16;   // P-neighbours staged at a time
+
 template <int D>
 __global__ void __launch_bounds__(kPairWarps * 32)
 k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* __restrict__ type, const int* __restrict__ nc,
@@ -598,11 +603,19 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
     constexpr int SMAX = D == 3 ? 27 : 9;
     __shared__ float sacc[kPairWarps][SMAX * DD];
     __shared__ int srun[kPairWarps][SMAX + 1];
+    __shared__ int srkey[kPairWarps][SMAX];
+    __shared__ int sslot[kPairWarps][kPartStage * kWBins];
+    __shared__ float sval[kPairWarps][kPartStage * kWBins * 3];
+    __shared__ float scl[kPairWarps][kPartStage * 3];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     float* acc = sacc[wl];
     int* run = srun[wl];
+    int* rkey = srkey[wl];
+    int* stslot = sslot[wl];
+    float* stval = sval[wl];
+    float* stcl = scl[wl];
     const unsigned full = 0xffffffffu;
     for (int i = wid; i < P.Nf; i += nwarps) {
         for (int t = lane; t < SMAX * DD; t += 32) acc[t] = 0.f;
@@ -614,16 +627,22 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
         const long long nb = nptr[i];
         const int n = nc[i], nf = nfc[i];
         // runs of equal cell in the fluid part of the neighbour list
-        int nrun = 0;
+        int nrun = 0, last = -1;
+        int kjn = lane < nf ? key[nind[nb + lane]] : -1;
         for (int k0 = 0; k0 < nf; k0 += 32) {
             const int k = k0 + lane;
-            const int kj = k < nf ? key[nind[nb + k]] : -1;
+            const int kj = kjn;
+            kjn = k + 32 < nf ? key[nind[nb + k + 32]] : -1;   // next chunk, issued ahead
             int kp = __shfl_up_sync(full, kj, 1);
-            if (lane == 0) kp = k0 > 0 ? key[nind[nb + k0 - 1]] : -1;
+            if (lane == 0) kp = last;
+            last = __shfl_sync(full, kj, 31);
             const bool start = k < nf && kj != kp;
             const unsigned bal = __ballot_sync(full, start);
             const int at = nrun + __popc(bal & ((1u << lane) - 1u));
-            if (start && at < SMAX) run[at] = k;
+            if (start && at < SMAX) {
+                run[at] = k;
+                rkey[at] = kj;
+            }
             nrun += __popc(bal);
         }
         bool bad = nrun > SMAX;
@@ -638,6 +657,7 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
             float rsum[DD];
 #pragma unroll
             for (int t = 0; t < DD; ++t) rsum[t] = 0.f;
+#pragma unroll 4
             for (int k = k0; k < k1; ++k) {
                 const float4 pv = pe32[nb + k];
                 const float e[3] = {pv.x, pv.y, pv.z};
@@ -646,7 +666,7 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
 #pragma unroll
                     for (int c = 0; c < D; ++c) rsum[r * D + c] += pv.w * e[r] * e[c];
             }
-            const int slot = stencil_slot<D>(P, M, gi, key[nind[nb + k0]]);
+            const int slot = stencil_slot<D>(P, M, gi, rkey[lane]);
 #pragma unroll
             for (int t = 0; t < DD; ++t) {
                 acc[slot * DD + t] = -rsum[t];
@@ -688,36 +708,41 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
         }
         __syncwarp();
         // C Lambda C^T: P-neighbours in order; the bins of one W_k are distinct cells
-        for (int a0 = 0; a0 < np && !bad; a0 += 32) {
-            const int a = a0 + lane;
-            int kk = 0;
-            float cl[3] = {0.f, 0.f, 0.f};
-            if (a < np) {
-                kk = nindP[pb + a];
-#pragma unroll
-                for (int r = 0; r < D; ++r) cl[r] = cvl32[(pb + a) * D + r];
-            }
-            const int na = min(32, np - a0);
-            for (int q = 0; q < na; ++q) {
-                const int k = __shfl_sync(full, kk, q);
-                float cq[3];
-#pragma unroll
-                for (int r = 0; r < 3; ++r) cq[r] = __shfl_sync(full, cl[r], q);
-                bool over = false;
-                for (int t = lane; t < kWBins * DD; t += 32) {
-                    const int b = t / DD, rs = t - b * DD;
+        for (int a0 = 0; a0 < np && !bad; a0 += kPartStage) {
+            const int na = min(kPartStage, np - a0);
+            bool over = false;
+            for (int t = lane; t < kPartStage * kWBins; t += 32) {   // stage the bins (slot, W) of na P-neighbours
+                const int q = t / kWBins, b = t % kWBins;
+                int slot = -1;
+                if (q < na) {
+                    const int k = nindP[pb + a0 + q];
                     const int wk = wkey[(size_t)k * kWBins + b];
                     if (wk == -2) over = true;
-                    if (wk < 0) continue;
-                    const int slot = stencil_slot<D>(P, M, gi, wk);
-                    acc[slot * DD + rs] += cq[rs / D] * wval[((size_t)k * kWBins + b) * 3 + rs % D];
+                    if (wk >= 0) {
+                        slot = stencil_slot<D>(P, M, gi, wk);
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) stval[t * 3 + d] = wval[((size_t)k * kWBins + b) * 3 + d];
+                    }
                 }
-                bad = __any_sync(full, over) || bad;
+                stslot[t] = slot;
+            }
+            for (int t = lane; t < na * 3; t += 32) stcl[t] = t % 3 < D ? cvl32[(pb + a0 + t / 3) * D + t % 3] : 0.f;
+            bad = __any_sync(full, over) || bad;
+            __syncwarp();
+            if (bad) break;
+            for (int q = 0; q < na; ++q) {
+                for (int t = lane; t < kWBins * DD; t += 32) {
+                    const int b = t / DD, rs = t - b * DD;
+                    const int slot = stslot[q * kWBins + b];
+                    if (slot < 0) continue;
+                    acc[slot * DD + rs] += stcl[q * 3 + rs / D] * stval[(q * kWBins + b) * 3 + rs % D];
+                }
                 __syncwarp();
             }
         }
         if (bad) {
             if (lane == 0) cell_flags[ki] = 1;   // the per-row kernel assembles this cell
+            __syncwarp();
             continue;
         }
         double* prow = part + (size_t)i * M.S * DD;
