@@ -32,6 +32,16 @@ namespace mph {
 
 constexpr int kPairWarps = 8;
 
+// Tuning of the inner operator's viscous loop: slots unrolled per step and
+// the minimum resident blocks of k_visc_pen32 (register cap).
+#ifndef MPH_PAIR_UNROLL
+#define MPH_PAIR_UNROLL 4
+#endif
+#ifndef MPH_PAIR_MINB
+#define MPH_PAIR_MINB 1
+#endif
+constexpr int kPairUnroll = MPH_PAIR_UNROLL;
+
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
 // (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).  The
 // separation is the FP64 difference of the positions rounded to FP32 (the
@@ -312,7 +322,7 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     const long long vo = base * D + lane;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
-#pragma unroll 4
+#pragma unroll (kPairUnroll)
     for (int k = 0; k < n; ++k) {
         const int col = __ldcs(cp + (long long)k * 32);
         float g[3] = {0.f, 0.f, 0.f};
@@ -333,7 +343,7 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
 }
 
 template <int D>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, MPH_PAIR_MINB)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ pes16, const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
