@@ -19,10 +19,10 @@
 // (used by the FP32 blocks and by the viscous part of the FP64 residual) and b
 // in FP64; for the FP32 inner operator without blocks also the wall part of
 // the FP32 viscous diagonal block, the FP32 inertia and the lambda-scaled C
-// values.  The only FP64 work per slot is the
-// position difference, against the nine-entry block and its accumulation of
-// the assembled form; in the residual only inertia and C Lambda C^T (about 20
-// P-slots a row) are FP64.
+// values.  No FP64 arithmetic is done per slot (the separation comes from
+// two-float positions), against the nine-entry FP64 block and its
+// accumulation of the assembled form; in the residual only inertia and
+// C Lambda C^T (about 20 P-slots a row) are FP64.
 #include <cuda_fp16.h>
 
 #include "mph_device.cuh"
@@ -40,20 +40,26 @@ constexpr int kPairWarps = 8;
 #ifndef MPH_PAIR_MINB
 #define MPH_PAIR_MINB 1
 #endif
+// slots ahead of the viscous loop whose column and g records are prefetched
+// into L2 (0: none)
+#ifndef MPH_PAIR_PF
+#define MPH_PAIR_PF 0
+#endif
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
 // (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).  The
-// separation is the FP64 difference of the positions rounded to FP32 (the
-// minimum image of the neighbour search, which it equals to within one FP64
-// rounding, is evaluated only for periodic images); the rest
+// separation is the difference of the two-float positions (pos32, poslo32),
+// within about one FP32 ulp of the FP64 difference (the exact minimum image
+// of the neighbour search is evaluated only for periodic images); the rest
 // of the viscous term is FP32: it is about nu dt / l0^2 (~1e-3) of the
 // inertia term, so its FP32 rounding moves A x by ~1e-10 of |b| (the host
 // keeps the factored form off when that bound would reach 1e-2 of the outer
 // tolerance).  Inertia and C p stay FP64.
 template <int D>
 __global__ void __launch_bounds__(kPairWarps * 32)
-k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const double* __restrict__ vel,
+k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const float* __restrict__ pos32,
+             const float* __restrict__ poslo32, const double* __restrict__ vel,
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
@@ -66,9 +72,11 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         const int ti = type[i];
         const long long nb = nptr[i];
         const int n = nc[i], nf = nfc[i];
-        double xi[3], vi[3];
-        load_vec<D>(pos, i, xi);
+        double vi[3];
         load_vec<D>(vel, i, vi);
+        float hi[3], li[3];
+        load_f32<D>(pos32, i, hi);
+        load_f32<D>(poslo32, i, li);
         float sumw[3] = {0.f, 0.f, 0.f};
         float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over the wall slots: xx xy xz yy yz zz
         for (int k = lane; k < n; k += 32) {
@@ -76,20 +84,26 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
             float e[3] = {0.f, 0.f, 0.f};
             float f = 0.f;
             if (j != i) {
-                // x_j - x_i rounded to FP32; the exact minimum image only when
-                // a component is not well inside a quarter of the domain width
-                // (a periodic image), where the two could differ
-                double xj[3];
-                load_vec<D>(pos, j, xj);
+                // x_j - x_i from the two-float positions: the high parts of
+                // nearby positions subtract with one FP32 rounding at most,
+                // so q is within about one FP32 ulp of the FP64 difference,
+                // with no FP64 arithmetic; the exact minimum image only when
+                // a component is not well inside a quarter of the domain
+                // width (a periodic image)
+                float hj[3], lj[3];
+                load_f32<D>(pos32, j, hj);
+                load_f32<D>(poslo32, j, lj);
                 float q32[3] = {0.f, 0.f, 0.f};
                 bool inner = true;
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    q32[d] = (float)(xj[d] - xi[d]);
+                    q32[d] = (hj[d] - hi[d]) + (lj[d] - li[d]);
                     inner = inner && fabsf(q32[d]) < 0.48f * P.hw32[d];
                 }
                 if (!inner) {
-                    double q[3];
+                    double xi[3], xj[3], q[3];
+                    load_vec<D>(pos, i, xi);
+                    load_vec<D>(pos, j, xj);
                     sep_vec<D>(P, xj, xi, q);
 #pragma unroll
                     for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
@@ -322,8 +336,14 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     const long long vo = base * D + lane;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
+    const int wsl = MPH_PAIR_PF > 0 ? (int)((sptr[(i >> 5) + 1] - base) / 32) : 0;   // slots of the slice
 #pragma unroll (kPairUnroll)
     for (int k = 0; k < n; ++k) {
+        if (MPH_PAIR_PF > 0 && HALF && k + MPH_PAIR_PF < wsl) {   // this lane's share of slot k+PF's records
+            const long long kp = k + MPH_PAIR_PF;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + kp * 32));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(pes16 + base * D + kp * D * 32 + (long long)lane * D));
+        }
         const int col = __ldcs(cp + (long long)k * 32);
         float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -848,10 +868,10 @@ int launch_pair_terms(mph_case* c)
     }
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
     if (c->dim == 2) {
-        { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+        { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
                                                                d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+        { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
                                                                d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;

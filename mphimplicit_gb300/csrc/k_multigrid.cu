@@ -22,9 +22,13 @@
 //         barriers, so the small levels cost one launch and read their
 //         stencils through the L2 ports of eight SMs.
 //         The last kernel adds G2P S_0 to D^-1 q and forms the (q, u) dot.
+//         The mixed form's FP32 sweeps on grid-wide levels run three threads
+//         a row (k_mg_sweep3), one stencil plane each.
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "mph_device.cuh"
+
 #include "mph_solver.cuh"
 
 namespace cg = cooperative_groups;
@@ -279,6 +283,54 @@ __global__ void k_mg_residual(LevelK L, const T* __restrict__ cofT, const T* __r
     R[row] = row_residual<D, T>(L, cofT, Q, S, row);
 }
 
+// FP32 sweeps of the mixed form's V-cycle on grid-wide levels with the full
+// 3^D stencil: three threads per row, one stencil plane (fixed first
+// coordinate) each, summed in plane order (10 rows a warp, lanes 30 and 31
+// idle).  A row's stencil is then three short load chains instead of one of
+// 3^D cells, and the level has three times the threads in flight.  RESID:
+// R = Q - A S; else S_out = S + invD (Q - A S).
+template <int D, bool RESID>
+__global__ void k_mg_sweep3(LevelK L, const float* __restrict__ cofT, const float* __restrict__ invd, const float* __restrict__ Q,
+                            const float* __restrict__ Sin, float* __restrict__ out, const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    constexpr int SZ = D == 3 ? 3 : 1;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int rw = lane / 3, ix = lane - 3 * rw;
+    const int row = warp * 10 + rw;
+    const bool valid = lane < 30 && row < L.rows;
+    float part = 0.f;
+    if (valid) {
+        int p[3];
+        grid_coords(L, row / D, p);
+        const int xw = ((p[0] + ix - 1 + L.cnt[0]) % L.cnt[0]) * (L.cnt[1] * L.cnt[2]);
+        int ys[3], zs[SZ];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ys[k] = ((p[1] + k - 1 + L.cnt[1]) % L.cnt[1]) * L.cnt[2];
+#pragma unroll
+        for (int k = 0; k < SZ; ++k) zs[k] = (p[2] + k - 1 + L.cnt[2]) % L.cnt[2];
+        const float* cx = cofT + (size_t)ix * (3 * SZ * D) * L.rows + row;
+#pragma unroll
+        for (int iy = 0; iy < 3; ++iy)
+#pragma unroll
+            for (int iz = 0; iz < SZ; ++iz) {
+                const int jg = xw + ys[iy] + zs[iz];
+#pragma unroll
+                for (int sD = 0; sD < D; ++sD) part += (-cx[(size_t)((iy * SZ + iz) * D + sD) * L.rows]) * Sin[jg * D + sD];
+            }
+    }
+    const int b = min(3 * rw, 29);
+    const float p0 = __shfl_sync(0xffffffffu, part, b);
+    const float p1 = __shfl_sync(0xffffffffu, part, b + 1);
+    const float p2 = __shfl_sync(0xffffffffu, part, b + 2);
+    if (valid && ix == 0) {
+        const float r = Q[row] + ((p0 + p1) + p2);
+        if (RESID) out[row] = r;
+        else out[row] = Sin[row] + invd[row] * r;
+    }
+}
+
 // Q_L = R r_{L-1};  S_L = invD_L Q_L (the first smoothing update from S = 0)
 template <int D, typename T>
 __global__ void k_mg_restrict(LevelK S_, LevelK L, const T* __restrict__ RS, const T* __restrict__ invdL, T* __restrict__ QL,
@@ -456,12 +508,31 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     int first = depth;
     for (int l = 1; l < depth; ++l)
         if (L[l].rows <= kCtaRows) { first = l; break; }
+    // FP32 levels with the full stencil: the three-threads-a-row sweep
+    auto split = [&](int l) {
+        constexpr int SZ = D == 3 ? 3 : 1;
+        return std::is_same<T, float>::value && L[l].st[0] == 3 && L[l].st[1] == 3 && L[l].st[2] == SZ;
+    };
+    auto grid3 = [&](int l) { return (unsigned)((L[l].rows + 39) / 40); };   // 4 warps of 10 rows a block
     auto jacobi = [&](int l) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (split(l)) {
+                { k_mg_sweep3<D, false><<<grid3(l), 128, 0, st>>>(L[l], cof + oc(l), invd + ov(l), Qp + ov(l), cur[l], oth[l], flags); MPH_COUNT_LAUNCH(); }
+                T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
+                return;
+            }
+        }
         { k_mg_jacobi<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + oc(l), invd + ov(l), Qp + ov(l), cur[l], oth[l],
                                                                        flags); MPH_COUNT_LAUNCH(); }
         T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
     };
     auto residual = [&](int l) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (split(l)) {
+                { k_mg_sweep3<D, true><<<grid3(l), 128, 0, st>>>(L[l], cof + oc(l), nullptr, Qp + ov(l), cur[l], Rp + ov(l), flags); MPH_COUNT_LAUNCH(); }
+                return;
+            }
+        }
         { k_mg_residual<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l], cof + oc(l), Qp + ov(l), cur[l], Rp + ov(l), flags); MPH_COUNT_LAUNCH(); }
     };
     // down, grid-wide levels
@@ -526,6 +597,7 @@ void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
         vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out,
                                   c->mixed_extra_sweeps);
 }
+
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)
 {

@@ -331,6 +331,7 @@ int case_alloc_particles(mph_case* c)
     MPH_TRY(dalloc(c, &d.pos_alt, N * VSn));
     MPH_TRY(dalloc(c, &d.vel_alt, N * VSn));
     MPH_TRY(dalloc(c, &d.pos32, N * VSn));
+    MPH_TRY(dalloc(c, &d.poslo32, N * VSn));
     MPH_TRY(dalloc(c, &d.type, N));
     MPH_TRY(dalloc(c, &d.id, N));
     MPH_TRY(dalloc(c, &d.type_alt, N));

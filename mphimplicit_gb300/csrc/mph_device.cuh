@@ -60,6 +60,18 @@ __device__ __forceinline__ void load_vec(const double* __restrict__ a, int i, do
         v[0] = t0.x; v[1] = t0.y; v[2] = t1.x;
     }
 }
+// FP32 [N][VS] record (float2 in 2-D, float4 in 3-D)
+template <int D>
+__device__ __forceinline__ void load_f32(const float* __restrict__ a, int i, float* v)
+{
+    if (D == 2) {
+        const float2 t = reinterpret_cast<const float2*>(a)[i];
+        v[0] = t.x; v[1] = t.y; v[2] = 0.f;
+    } else {
+        const float4 t = reinterpret_cast<const float4*>(a)[i];
+        v[0] = t.x; v[1] = t.y; v[2] = t.z;
+    }
+}
 template <int D>
 __device__ __forceinline__ void store_vec(double* a, int i, const double* v)
 {

@@ -6,6 +6,9 @@
 //   pos32                           : float[N][VS] copy used only to pre-classify
 //                                      neighbour candidates (exact FP64 decides
 //                                      every pair near a radius)
+//   poslo32                         : float[N][VS], x - pos32 rounded to FP32:
+//                                      (pos32, poslo32) is a two-float position
+//                                      for the FP32 pair terms of the mixed form
 //   neighbour lists                 : CSR, int64 row pointers, int32 columns,
 //                                      as the reference (main.cpp:92-97)
 //   matrix A                        : sliced ELL of DxD blocks, 32 block rows per
@@ -76,6 +79,7 @@ struct DeviceState {
     double *pos = nullptr, *vel = nullptr, *force = nullptr;
     double *pos_alt = nullptr, *vel_alt = nullptr;
     float* pos32 = nullptr;
+    float* poslo32 = nullptr;
     int *type = nullptr, *id = nullptr, *type_alt = nullptr, *id_alt = nullptr;
     double *densA = nullptr, *gcen = nullptr, *presA = nullptr, *vsp = nullptr;
     double *divP = nullptr, *presP = nullptr, *virP = nullptr, *virS = nullptr;
