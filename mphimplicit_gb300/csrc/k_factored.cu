@@ -40,11 +40,6 @@ constexpr int kPairWarps = 8;
 #ifndef MPH_PAIR_MINB
 #define MPH_PAIR_MINB 1
 #endif
-// slots ahead of the viscous loop whose column and g records are prefetched
-// into L2 (0: none)
-#ifndef MPH_PAIR_PF
-#define MPH_PAIR_PF 0
-#endif
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
@@ -336,14 +331,8 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     const long long vo = base * D + lane;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
-    const int wsl = MPH_PAIR_PF > 0 ? (int)((sptr[(i >> 5) + 1] - base) / 32) : 0;   // slots of the slice
 #pragma unroll (kPairUnroll)
     for (int k = 0; k < n; ++k) {
-        if (MPH_PAIR_PF > 0 && HALF && k + MPH_PAIR_PF < wsl) {   // this lane's share of slot k+PF's records
-            const long long kp = k + MPH_PAIR_PF;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + kp * 32));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(pes16 + base * D + kp * D * 32 + (long long)lane * D));
-        }
         const int col = __ldcs(cp + (long long)k * 32);
         float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll

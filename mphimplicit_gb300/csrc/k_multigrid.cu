@@ -283,43 +283,79 @@ __global__ void k_mg_residual(LevelK L, const T* __restrict__ cofT, const T* __r
     R[row] = row_residual<D, T>(L, cofT, Q, S, row);
 }
 
-// FP32 sweeps of the mixed form's V-cycle on grid-wide levels with the full
-// 3^D stencil: three threads per row, one stencil plane (fixed first
-// coordinate) each, summed in plane order (10 rows a warp, lanes 30 and 31
-// idle).  A row's stencil is then three short load chains instead of one of
-// 3^D cells, and the level has three times the threads in flight.  RESID:
-// R = Q - A S; else S_out = S + invD (Q - A S).
+// FP32 sweeps of the mixed form's V-cycle on levels with the full 3^D
+// stencil: three threads per row, one stencil plane (fixed first coordinate)
+// each, summed in plane order (10 rows a warp, lanes 30 and 31 idle).  A
+// row's stencil is then three short load chains instead of one of 3^D
+// cells, with three times the threads in flight.  RESID: R = Q - A S; else
+// S_out = S + invD (Q - A S).  Warp gw of nw walks the rows 10 at a time.
+template <int D>
+__device__ __forceinline__ float plane_part(const LevelK& L, const float* __restrict__ cofT, const float* __restrict__ Sin, int row,
+                                            int ix)
+{
+    constexpr int SZ = D == 3 ? 3 : 1;
+    int p[3];
+    grid_coords(L, row / D, p);
+    const int xw = ((p[0] + ix - 1 + L.cnt[0]) % L.cnt[0]) * (L.cnt[1] * L.cnt[2]);
+    int ys[3], zs[SZ];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ys[k] = ((p[1] + k - 1 + L.cnt[1]) % L.cnt[1]) * L.cnt[2];
+#pragma unroll
+    for (int k = 0; k < SZ; ++k) zs[k] = (p[2] + k - 1 + L.cnt[2]) % L.cnt[2];
+    const float* cx = cofT + (size_t)ix * (3 * SZ * D) * L.rows + row;
+    float part = 0.f;
+#pragma unroll
+    for (int iy = 0; iy < 3; ++iy)
+#pragma unroll
+        for (int iz = 0; iz < SZ; ++iz) {
+            const int jg = xw + ys[iy] + zs[iz];
+#pragma unroll
+            for (int sD = 0; sD < D; ++sD) part += (-cx[(size_t)((iy * SZ + iz) * D + sD) * L.rows]) * Sin[jg * D + sD];
+        }
+    return part;
+}
+
+template <int D, bool RESID>
+__device__ __forceinline__ void sweep3_rows(const LevelK& L, const float* __restrict__ cofT, const float* __restrict__ invd,
+                                            const float* __restrict__ Q, const float* __restrict__ Sin, float* __restrict__ out,
+                                            int gw, int nw)
+{
+    const int lane = threadIdx.x & 31;
+    const int rw = lane / 3, ix = lane - 3 * rw;
+    const int b = min(3 * rw, 29);
+    for (int base = gw * 10; base < L.rows; base += nw * 10) {
+        const int row = base + rw;
+        const bool valid = lane < 30 && row < L.rows;
+        const float part = valid ? plane_part<D>(L, cofT, Sin, row, ix) : 0.f;
+        const float p0 = __shfl_sync(0xffffffffu, part, b);
+        const float p1 = __shfl_sync(0xffffffffu, part, b + 1);
+        const float p2 = __shfl_sync(0xffffffffu, part, b + 2);
+        if (valid && ix == 0) {
+            const float r = Q[row] + ((p0 + p1) + p2);
+            if (RESID) out[row] = r;
+            else out[row] = Sin[row] + invd[row] * r;
+        }
+    }
+}
+
+__host__ __device__ inline bool full_stencil(const LevelK& L, int D)
+{
+    return L.st[0] == 3 && L.st[1] == 3 && L.st[2] == (D == 3 ? 3 : 1);
+}
+
+// one warp of 10 rows per launch slot (the grid covers the level once)
 template <int D, bool RESID>
 __global__ void k_mg_sweep3(LevelK L, const float* __restrict__ cofT, const float* __restrict__ invd, const float* __restrict__ Q,
                             const float* __restrict__ Sin, float* __restrict__ out, const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
-    constexpr int SZ = D == 3 ? 3 : 1;
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int rw = lane / 3, ix = lane - 3 * rw;
     const int row = warp * 10 + rw;
     const bool valid = lane < 30 && row < L.rows;
     float part = 0.f;
-    if (valid) {
-        int p[3];
-        grid_coords(L, row / D, p);
-        const int xw = ((p[0] + ix - 1 + L.cnt[0]) % L.cnt[0]) * (L.cnt[1] * L.cnt[2]);
-        int ys[3], zs[SZ];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) ys[k] = ((p[1] + k - 1 + L.cnt[1]) % L.cnt[1]) * L.cnt[2];
-#pragma unroll
-        for (int k = 0; k < SZ; ++k) zs[k] = (p[2] + k - 1 + L.cnt[2]) % L.cnt[2];
-        const float* cx = cofT + (size_t)ix * (3 * SZ * D) * L.rows + row;
-#pragma unroll
-        for (int iy = 0; iy < 3; ++iy)
-#pragma unroll
-            for (int iz = 0; iz < SZ; ++iz) {
-                const int jg = xw + ys[iy] + zs[iz];
-#pragma unroll
-                for (int sD = 0; sD < D; ++sD) part += (-cx[(size_t)((iy * SZ + iz) * D + sD) * L.rows]) * Sin[jg * D + sD];
-            }
-    }
+    if (valid) part = plane_part<D>(L, cofT, Sin, row, ix);
     const int b = min(3 * rw, 29);
     const float p0 = __shfl_sync(0xffffffffu, part, b);
     const float p1 = __shfl_sync(0xffffffffu, part, b + 1);
@@ -429,6 +465,14 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
     // one smoothing sweep of level l over rows t0, t0 + nt, ...
     auto jacobi = [&](int l, int t0, int nt, auto sync) {
         const LevelK& L = A.L[l];
+        if constexpr (std::is_same<T, float>::value) {
+            if (full_stencil(L, D)) {   // three threads a row (t0, nt: multiples of 32)
+                sweep3_rows<D, false>(L, A.cof[l], A.invd[l], A.Q[l], cur[l], oth[l], t0 >> 5, nt >> 5);
+                sync();
+                T* t = cur[l]; cur[l] = oth[l]; oth[l] = t;
+                return;
+            }
+        }
         for (int row = t0; row < L.rows; row += nt) {
             const T r = row_residual<D, T, true>(L, A.cof[l], A.Q[l], cur[l], row);
             oth[l][row] = cur[l][row] + A.invd[l][row] * r;
@@ -448,7 +492,15 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
         const int sweeps = (l == A.depth - 1) ? 4 : 2;
         for (int k = 0; k < sweeps; ++k) jacobi(l, t0, nt, sync);
         if (l < A.depth - 1) {
-            for (int row = t0; row < L.rows; row += nt) A.R[l][row] = row_residual<D, T, true>(L, A.cof[l], A.Q[l], cur[l], row);
+            bool done3 = false;
+            if constexpr (std::is_same<T, float>::value) {
+                if (full_stencil(L, D)) {
+                    sweep3_rows<D, true>(L, A.cof[l], nullptr, A.Q[l], cur[l], A.R[l], t0 >> 5, nt >> 5);
+                    done3 = true;
+                }
+            }
+            if (!done3)
+                for (int row = t0; row < L.rows; row += nt) A.R[l][row] = row_residual<D, T, true>(L, A.cof[l], A.Q[l], cur[l], row);
             sync();
         }
     };
@@ -509,10 +561,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     for (int l = 1; l < depth; ++l)
         if (L[l].rows <= kCtaRows) { first = l; break; }
     // FP32 levels with the full stencil: the three-threads-a-row sweep
-    auto split = [&](int l) {
-        constexpr int SZ = D == 3 ? 3 : 1;
-        return std::is_same<T, float>::value && L[l].st[0] == 3 && L[l].st[1] == 3 && L[l].st[2] == SZ;
-    };
+    auto split = [&](int l) { return std::is_same<T, float>::value && full_stencil(L[l], D); };
     auto grid3 = [&](int l) { return (unsigned)((L[l].rows + 39) / 40); };   // 4 warps of 10 rows a block
     auto jacobi = [&](int l) {
         if constexpr (std::is_same<T, float>::value) {
@@ -597,7 +646,6 @@ void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out)
         vcycle_t<3, float, float>(c, q, u, invDiag32, d.mg_cof32, d.mg_invd32, d.mg_q32, d.mg_s32, d.mg_r32, d.mg_res32, dot_out,
                                   c->mixed_extra_sweeps);
 }
-
 
 void vcycle_fp64(mph_case* c, const double* q, double* u, double* dot_out)
 {
