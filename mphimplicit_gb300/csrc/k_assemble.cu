@@ -474,6 +474,7 @@ int launch_assemble(mph_case* c)
     c->ct_ready = false;
     c->step_factored = factored_applies(c);
     c->step_pairs = c->step_factored && !c->inner_blocks && c->visc_nonneg;
+    c->level0_done = false;
     if (c->step_factored) {
         // mixed form: FP64 pair terms and b, transposed P-lists (the factored
         // FP64 operator), then FP32 blocks only

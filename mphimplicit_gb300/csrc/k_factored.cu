@@ -544,8 +544,9 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 }
 
 // ---- level-0 multigrid stencils and D^-1 on the pair-term path --------------------
-// The Galerkin level-0 matrix sums each fluid row's blocks of A per neighbour
-// cell (part[i][slot], read by k_mg_level0).  Without assembled blocks:
+// The Galerkin level-0 matrix (calculateMultiGridCsrA, main.cpp:3245) sums
+// the blocks of A of a cell's fluid rows per neighbour cell.  Without
+// assembled blocks, row i contributes:
 //  - viscous: a fluid neighbour j gives -f e (x) e to the slot of its cell,
 //    and every neighbour (fluid or wall) f e (x) e to the row's own slot,
 //    with the inertia;
@@ -557,13 +558,40 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 // Both kernels sum in a fixed order (no atomics), so the result is the same
 // bits on every run.  A row whose neighbour list is not grouped into at most
 // 3^D cells, or one of whose P-neighbours has more than kWBins cells, flags its
-// cell; the per-row FP64 kernel then assembles that cell's rows.
+// cell; the per-row FP64 kernel then assembles that cell's rows and
+// k_mg_level0 that cell's level-0 rows.
 constexpr int kWBins = 8;
 
-// W_k: (cell key, sum of C_jk over the rows j of that cell) for every particle
+// Neighbour-grid cell coordinates packed 10 bits an axis (grids of at most
+// 1024 cells an axis), so the stencil slot of one cell seen from another is
+// a few integer operations instead of the divisions of key_coords.
+__global__ void k_pack_cells(int N, DevParams P, const int* __restrict__ key, int* __restrict__ ccell)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    int c[3];
+    key_coords(P, key[i], c);
+    ccell[i] = c[0] | (c[1] << 10) | (c[2] << 20);
+}
+
+// stencil_slot for packed cell coordinates: the same slot, ((cj - ci) + 1)
+// modulo the level-0 grid on every axis
+__device__ __forceinline__ int slot_packed(const Level0Map& M, int pi, int pj)
+{
+    int o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int v = ((pj >> (10 * d)) & 1023) - ((pi >> (10 * d)) & 1023) + 1;
+        if ((unsigned)v >= (unsigned)min(3, M.cnt[d])) v = ((v % M.cnt[d]) + M.cnt[d]) % M.cnt[d];   // wrapped (rare)
+        o[d] = v;
+    }
+    return M.st[2] * M.st[1] * o[0] + M.st[2] * o[1] + o[2];
+}
+
+// W_k: (packed cell, sum of C_jk over the rows j of that cell) for every particle
 template <int D>
 __global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
-                                                  const float* __restrict__ ct_v32, const int* __restrict__ key,
+                                                  const float* __restrict__ ct_v32, const int* __restrict__ ccell,
                                                   int* __restrict__ wkey, float* __restrict__ wval)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -578,7 +606,7 @@ __global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __rest
     bool over = false;
     const long long e1 = ctptr[k + 1];
     for (long long e = ctptr[k]; e < e1; ++e) {
-        const int kj = key[ct_j[e]];
+        const int kj = ccell[ct_j[e]];
         float cv[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < D; ++d) cv[d] = ct_v32[e * D + d];
@@ -602,8 +630,10 @@ __global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __rest
     }
 }
 
-// part[i][slot] (FP64 store of FP32 sums) and invDiag of every fluid row, one
-// warp per row with the row's stencil accumulated in shared memory.  Global
+// The level-0 stencil rows (FP64 store of FP32 sums) and invDiag, one warp
+// per level-0 cell: its fluid rows in order, each row's blocks accumulated
+// into the cell's stencil in shared memory, written entry-major as
+// k_mg_level0 writes it (zeros for a cell without fluid).  Global
 // loads are issued ahead of the ordered accumulation: the cell keys of the
 // next 32 neighbours while a chunk is scanned for runs, and the W_k bins of
 // up to 32 P-neighbours at once into a per-warp stage.
@@ -611,12 +641,13 @@ constexpr int kPartStage = 16;   // P-neighbours staged at a time
 
 template <int D>
 __global__ void __launch_bounds__(kPairWarps * 32)
-k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* __restrict__ type, const int* __restrict__ nc,
+k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* __restrict__ ccell, const int* __restrict__ type,
+             const int* __restrict__ nc,
              const int* __restrict__ nfc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const float4* __restrict__ pe32, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const float* __restrict__ cval32, const float* __restrict__ cvl32,
-             const int* __restrict__ wkey, const float* __restrict__ wval, double* __restrict__ part,
-             double* __restrict__ invDiag, int* __restrict__ cell_flags)
+             const int* __restrict__ wkey, const float* __restrict__ wval, const int* __restrict__ bucket,
+             double* __restrict__ cof0, double* __restrict__ invDiag, int* __restrict__ cell_flags)
 {
     constexpr int DD = D * D;
     constexpr int SMAX = D == 3 ? 27 : 9;
@@ -636,142 +667,156 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
     float* stval = sval[wl];
     float* stcl = scl[wl];
     const unsigned full = 0xffffffffu;
-    for (int i = wid; i < P.Nf; i += nwarps) {
+    const int cells0 = M.cnt[0] * M.cnt[1] * M.cnt[2];
+    const int rows0 = D * cells0;
+    for (int g0 = wid; g0 < cells0; g0 += nwarps) {   // one level-0 cell: its fluid rows in order
         for (int t = lane; t < SMAX * DD; t += 32) acc[t] = 0.f;
-        const int ki = key[i];
-        int ic[3], gi[3];
-        key_coords(P, ki, ic);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) gi[d] = ic[d] - M.mn[d];
-        const long long nb = nptr[i];
-        const int n = nc[i], nf = nfc[i];
-        // runs of equal cell in the fluid part of the neighbour list
-        int nrun = 0, last = -1;
-        int kjn = lane < nf ? key[nind[nb + lane]] : -1;
-        for (int k0 = 0; k0 < nf; k0 += 32) {
-            const int k = k0 + lane;
-            const int kj = kjn;
-            kjn = k + 32 < nf ? key[nind[nb + k + 32]] : -1;   // next chunk, issued ahead
-            int kp = __shfl_up_sync(full, kj, 1);
-            if (lane == 0) kp = last;
-            last = __shfl_sync(full, kj, 31);
-            const bool start = k < nf && kj != kp;
-            const unsigned bal = __ballot_sync(full, start);
-            const int at = nrun + __popc(bal & ((1u << lane) - 1u));
-            if (start && at < SMAX) {
-                run[at] = k;
-                rkey[at] = kj;
-            }
-            nrun += __popc(bal);
-        }
-        bool bad = nrun > SMAX;
-        if (lane == 0) run[min(nrun, SMAX)] = nf;
+        const int cx = g0 / (M.cnt[1] * M.cnt[2]) + M.mn[0], cy = (g0 / M.cnt[2]) % M.cnt[1] + M.mn[1], cz = g0 % M.cnt[2] + M.mn[2];
+        const bool ingrid = cx < P.cc[0] && cy < P.cc[1] && cz < P.cc[2];
+        const int icell = ingrid ? cell_id(P, cx, cy, cz) : 0;
+        const int r0 = ingrid ? bucket[icell] : 0, r1 = ingrid ? bucket[icell + 1] : 0;
+        bool cellbad = false;
         __syncwarp();
-        // viscous: lane r sums run r in list order; every term also enters the own slot
-        float tv[DD];
+        for (int i = r0; i < r1; ++i) {
+            const int pi = ccell[i];
+            const long long nb = nptr[i];
+            const int n = nc[i], nf = nfc[i];
+            // runs of equal cell in the fluid part of the neighbour list
+            int nrun = 0, last = -1;
+            int kjn = lane < nf ? ccell[nind[nb + lane]] : -1;
+            for (int k0 = 0; k0 < nf; k0 += 32) {
+                const int k = k0 + lane;
+                const int kj = kjn;
+                kjn = k + 32 < nf ? ccell[nind[nb + k + 32]] : -1;   // next chunk, issued ahead
+                int kp = __shfl_up_sync(full, kj, 1);
+                if (lane == 0) kp = last;
+                last = __shfl_sync(full, kj, 31);
+                const bool start = k < nf && kj != kp;
+                const unsigned bal = __ballot_sync(full, start);
+                const int at = nrun + __popc(bal & ((1u << lane) - 1u));
+                if (start && at < SMAX) {
+                    run[at] = k;
+                    rkey[at] = kj;
+                }
+                nrun += __popc(bal);
+            }
+            bool bad = nrun > SMAX;
+            if (lane == 0) run[min(nrun, SMAX)] = nf;
+            __syncwarp();
+            // viscous: lane r sums run r in list order; every term also enters the own slot
+            float tv[DD];
 #pragma unroll
-        for (int t = 0; t < DD; ++t) tv[t] = 0.f;
-        if (!bad && lane < nrun) {
-            const int k0 = run[lane], k1 = run[lane + 1];
-            float rsum[DD];
+            for (int t = 0; t < DD; ++t) tv[t] = 0.f;
+            if (!bad && lane < nrun) {
+                const int k0 = run[lane], k1 = run[lane + 1];
+                float rsum[DD];
 #pragma unroll
-            for (int t = 0; t < DD; ++t) rsum[t] = 0.f;
+                for (int t = 0; t < DD; ++t) rsum[t] = 0.f;
 #pragma unroll 4
-            for (int k = k0; k < k1; ++k) {
+                for (int k = k0; k < k1; ++k) {
+                    const float4 pv = pe32[nb + k];
+                    const float e[3] = {pv.x, pv.y, pv.z};
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) rsum[r * D + c] += pv.w * e[r] * e[c];
+                }
+                const int slot = slot_packed(M, pi, rkey[lane]);
+#pragma unroll
+                for (int t = 0; t < DD; ++t) {
+                    acc[slot * DD + t] -= rsum[t];
+                    tv[t] = rsum[t];
+                }
+            }
+            for (int k = nf + lane; k < n; k += 32) {   // wall neighbours: own slot only
                 const float4 pv = pe32[nb + k];
                 const float e[3] = {pv.x, pv.y, pv.z};
 #pragma unroll
                 for (int r = 0; r < D; ++r)
 #pragma unroll
-                    for (int c = 0; c < D; ++c) rsum[r * D + c] += pv.w * e[r] * e[c];
+                    for (int c = 0; c < D; ++c) tv[r * D + c] += pv.w * e[r] * e[c];
             }
-            const int slot = stencil_slot<D>(P, M, gi, rkey[lane]);
+            // lambda_k C_ik[r]^2 for the diagonal of the own block
+            const long long pb = nptrP[i];
+            const int np = ncp[i];
+            float dp[3] = {0.f, 0.f, 0.f};
+            for (int a = lane; a < np; a += 32) {
 #pragma unroll
-            for (int t = 0; t < DD; ++t) {
-                acc[slot * DD + t] = -rsum[t];
-                tv[t] = rsum[t];
+                for (int r = 0; r < D; ++r) dp[r] += cvl32[(pb + a) * D + r] * cval32[(pb + a) * D + r];
             }
-        }
-        for (int k = nf + lane; k < n; k += 32) {   // wall neighbours: own slot only
-            const float4 pv = pe32[nb + k];
-            const float e[3] = {pv.x, pv.y, pv.z};
+#pragma unroll
+            for (int t = 0; t < DD; ++t)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) tv[t] += __shfl_xor_sync(full, tv[t], o);
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
-                for (int c = 0; c < D; ++c) tv[r * D + c] += pv.w * e[r] * e[c];
-        }
-        // lambda_k C_ik[r]^2 for the diagonal of the own block
-        const long long pb = nptrP[i];
-        const int np = ncp[i];
-        float dp[3] = {0.f, 0.f, 0.f};
-        for (int a = lane; a < np; a += 32) {
-#pragma unroll
-            for (int r = 0; r < D; ++r) dp[r] += cvl32[(pb + a) * D + r] * cval32[(pb + a) * D + r];
-        }
-#pragma unroll
-        for (int t = 0; t < DD; ++t)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) tv[t] += __shfl_xor_sync(full, tv[t], o);
-#pragma unroll
-        for (int r = 0; r < D; ++r)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) dp[r] += __shfl_xor_sync(full, dp[r], o);
-        __syncwarp();
-        const int si = stencil_slot<D>(P, M, gi, ki);
-        const float in32 = P.inert32[type[i]];
-        if (lane == 0 && !bad) {
-#pragma unroll
-            for (int r = 0; r < D; ++r)
-#pragma unroll
-                for (int c = 0; c < D; ++c) acc[si * DD + r * D + c] += tv[r * D + c] + (r == c ? in32 : 0.f);
-        }
-        __syncwarp();
-        // C Lambda C^T: P-neighbours in order; the bins of one W_k are distinct cells
-        for (int a0 = 0; a0 < np && !bad; a0 += kPartStage) {
-            const int na = min(kPartStage, np - a0);
-            bool over = false;
-            for (int t = lane; t < kPartStage * kWBins; t += 32) {   // stage the bins (slot, W) of na P-neighbours
-                const int q = t / kWBins, b = t % kWBins;
-                int slot = -1;
-                if (q < na) {
-                    const int k = nindP[pb + a0 + q];
-                    const int wk = wkey[(size_t)k * kWBins + b];
-                    if (wk == -2) over = true;
-                    if (wk >= 0) {
-                        slot = stencil_slot<D>(P, M, gi, wk);
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) stval[t * 3 + d] = wval[((size_t)k * kWBins + b) * 3 + d];
-                    }
-                }
-                stslot[t] = slot;
-            }
-            for (int t = lane; t < na * 3; t += 32) stcl[t] = t % 3 < D ? cvl32[(pb + a0 + t / 3) * D + t % 3] : 0.f;
-            bad = __any_sync(full, over) || bad;
+                for (int o = 16; o > 0; o >>= 1) dp[r] += __shfl_xor_sync(full, dp[r], o);
             __syncwarp();
-            if (bad) break;
-            for (int q = 0; q < na; ++q) {
-                for (int t = lane; t < kWBins * DD; t += 32) {
-                    const int b = t / DD, rs = t - b * DD;
-                    const int slot = stslot[q * kWBins + b];
-                    if (slot < 0) continue;
-                    acc[slot * DD + rs] += stcl[q * 3 + rs / D] * stval[(q * kWBins + b) * 3 + rs % D];
-                }
-                __syncwarp();
+            const int si = slot_packed(M, pi, pi);
+            const float in32 = P.inert32[type[i]];
+            if (lane == 0 && !bad) {
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) acc[si * DD + r * D + c] += tv[r * D + c] + (r == c ? in32 : 0.f);
             }
+            __syncwarp();
+            // C Lambda C^T: P-neighbours in order; the bins of one W_k are distinct cells
+            for (int a0 = 0; a0 < np && !bad; a0 += kPartStage) {
+                const int na = min(kPartStage, np - a0);
+                bool over = false;
+                for (int t = lane; t < kPartStage * kWBins; t += 32) {   // stage the bins (slot, W) of na P-neighbours
+                    const int q = t / kWBins, b = t % kWBins;
+                    int slot = -1;
+                    if (q < na) {
+                        const int k = nindP[pb + a0 + q];
+                        const int wk = wkey[(size_t)k * kWBins + b];
+                        if (wk == -2) over = true;
+                        if (wk >= 0) {
+                            slot = slot_packed(M, pi, wk);
+#pragma unroll
+                            for (int d = 0; d < 3; ++d) stval[t * 3 + d] = wval[((size_t)k * kWBins + b) * 3 + d];
+                        }
+                    }
+                    stslot[t] = slot;
+                }
+                for (int t = lane; t < na * 3; t += 32) stcl[t] = t % 3 < D ? cvl32[(pb + a0 + t / 3) * D + t % 3] : 0.f;
+                bad = __any_sync(full, over) || bad;
+                __syncwarp();
+                if (bad) break;
+                for (int q = 0; q < na; ++q) {
+                    for (int t = lane; t < kWBins * DD; t += 32) {
+                        const int b = t / DD, rs = t - b * DD;
+                        const int slot = stslot[q * kWBins + b];
+                        if (slot < 0) continue;
+                        acc[slot * DD + rs] += stcl[q * 3 + rs / D] * stval[(q * kWBins + b) * 3 + rs % D];
+                    }
+                    __syncwarp();
+                }
+            }
+            if (bad) {
+                cellbad = true;
+                break;
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    const float dg = in32 + tv[r * D + r] + dp[r];
+                    invDiag[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
+                }
+            }
+            __syncwarp();
         }
-        if (bad) {
-            if (lane == 0) cell_flags[ki] = 1;   // the per-row kernel assembles this cell
+        if (cellbad) {   // the per-row kernel assembles this cell's rows, k_mg_level0 its level-0 rows
+            if (lane == 0) cell_flags[icell] = 1;
             __syncwarp();
             continue;
         }
-        double* prow = part + (size_t)i * M.S * DD;
-        for (int t = lane; t < SMAX * DD; t += 32) prow[t] = (double)acc[t];
-        if (lane == 0) {
-#pragma unroll
-            for (int r = 0; r < D; ++r) {
-                const float dg = in32 + tv[r * D + r] + dp[r];
-                invDiag[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
-            }
+        // the cell's level-0 rows (entry-major: entry e = slot * D + column component)
+        for (int t = lane; t < SMAX * DD; t += 32) {
+            const int slot = t / DD, rs = t - slot * DD;
+            cof0[(size_t)(slot * D + rs % D) * rows0 + (size_t)g0 * D + rs / D] = (double)acc[t];
         }
         __syncwarp();
     }
@@ -979,8 +1024,9 @@ int launch_part_pairs(mph_case* c, const Level0Map& M, bool* done)
     const DevParams& P = c->dp;
     const int D = c->dim;
     for (int a = 0; a < D; ++a)
-        if (P.cc[a] < 3 || M.cnt[a] < 3) return MPH_OK;
+        if (P.cc[a] < 3 || M.cnt[a] < 3 || P.cc[a] > 1024) return MPH_OK;
     if (!d.wkey) {
+        MPH_CUDA(cudaMalloc((void**)&d.ccell, (size_t)P.N * sizeof(int)));
         MPH_CUDA(cudaMalloc((void**)&d.wkey, (size_t)P.N * kWBins * sizeof(int)));
         MPH_CUDA(cudaMalloc((void**)&d.wval, (size_t)P.N * kWBins * 3 * sizeof(float)));
     }
@@ -993,18 +1039,23 @@ int launch_part_pairs(mph_case* c, const Level0Map& M, bool* done)
         d.cap_cell_flags = fbytes + fbytes / 8 + 1024;
     }
     MPH_CUDA(cudaMemsetAsync(d.cell_flags, 0, (size_t)(P.T + 1) * sizeof(int), c->stream));
-    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
+    MPH_TRY(ensure_mg_cof(c));
+    double* cof0 = d.mg_cof + c->lv[0].off_cof;
+    const long long cells0 = (long long)M.cnt[0] * M.cnt[1] * M.cnt[2];
+    const unsigned g = std::min<long long>((cells0 + kPairWarps - 1) / kPairWarps, 152LL * 16);
+    { k_pack_cells<<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, P, d.key, d.ccell); MPH_COUNT_LAUNCH(); }
     if (D == 2) {
-        { k_ct_cells<2><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.key, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
-        { k_part_pairs<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.part, d.invDiag,
+        { k_ct_cells<2><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.ccell, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
+        { k_part_pairs<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.ccell, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.bucket, cof0, d.invDiag,
                                                                d.cell_flags); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_cells<3><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.key, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
-        { k_part_pairs<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.part, d.invDiag,
+        { k_ct_cells<3><<<grid_for(P.N, 256), 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v32, d.ccell, d.wkey, d.wval); MPH_COUNT_LAUNCH(); }
+        { k_part_pairs<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, M, d.key, d.ccell, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
+                                                               d.nindP, d.cval32, d.cvl32, d.wkey, d.wval, d.bucket, cof0, d.invDiag,
                                                                d.cell_flags); MPH_COUNT_LAUNCH(); }
     }
+    c->level0_done = true;
     *done = true;
     return MPH_OK;
 }

@@ -86,7 +86,7 @@ __device__ __forceinline__ void child_range(const LevelK& S_, const LevelK& L, c
 // ---- build -------------------------------------------------------------------
 template <int D>
 __global__ void k_mg_level0(DevParams P, LevelK L, const int* __restrict__ bucket, const double* __restrict__ part,
-                            double* __restrict__ cofT)
+                            double* __restrict__ cofT, const int* __restrict__ only_cells)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)L.rows * L.width) return;
@@ -100,7 +100,10 @@ __global__ void k_mg_level0(DevParams P, LevelK L, const int* __restrict__ bucke
     double sum = 0.0;
     if (cx < P.cc[0] && cy < P.cc[1] && cz < P.cc[2]) {
         const int ic = cell_id(P, cx, cy, cz);
+        if (only_cells && !only_cells[ic]) return;   // written by the assembly
         for (int i = bucket[ic]; i < bucket[ic + 1]; ++i) sum += part[((size_t)i * S + slot) * D * D + rD * D + sD];
+    } else if (only_cells) {
+        return;
     }
     cofT[t] = sum;
 }
@@ -153,13 +156,15 @@ __global__ void k_mg_invd(int rows, int width, const double* __restrict__ cofT, 
     invd[row] = s != 0.0 ? 2.0 / s : 0.0;
 }
 
-void launch_mg_level0(mph_case* c)
+// only_cells (cell flags by key, or null for every cell): the level-0 rows of
+// those cells only, the others having been written by the assembly
+void launch_mg_level0(mph_case* c, const int* only_cells)
 {
     const LevelK L = level_k(c, 0);
     const long long n = (long long)L.rows * L.width;
     double* cof = c->d.mg_cof + c->lv[0].off_cof;
-    if (c->dim == 2) { k_mg_level0<2><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof); MPH_COUNT_LAUNCH(); }
-    else { k_mg_level0<3><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof); MPH_COUNT_LAUNCH(); }
+    if (c->dim == 2) { k_mg_level0<2><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof, only_cells); MPH_COUNT_LAUNCH(); }
+    else { k_mg_level0<3><<<grid_for(n, 256), 256, 0, c->stream>>>(c->dp, L, c->d.bucket, c->d.part, cof, only_cells); MPH_COUNT_LAUNCH(); }
 }
 
 void launch_mg_coarse(mph_case* c, int lvl)

@@ -539,12 +539,18 @@ int stage_assemble(mph_case* c)
     return MPH_OK;
 }
 
-int stage_mg_build(mph_case* c)
+int ensure_mg_cof(mph_case* c)
 {
-    if (c->stage < 5) return fail(MPH_ERR_STATE, "multigrid build before assembly");
     void* p = c->d.mg_cof;
     MPH_TRY(grow(&p, &c->d.cap_mg_cof, c->mg_cof_total, sizeof(double)));
     c->d.mg_cof = (double*)p;
+    return MPH_OK;
+}
+
+int stage_mg_build(mph_case* c)
+{
+    if (c->stage < 5) return fail(MPH_ERR_STATE, "multigrid build before assembly");
+    MPH_TRY(ensure_mg_cof(c));
     if (c->mg_rows_total > c->d.cap_mg_vec) {
         for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r, &c->d.mg_res}) {
             if (*b) cudaFree(*b);
@@ -554,7 +560,9 @@ int stage_mg_build(mph_case* c)
         for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r, &c->d.mg_res}) MPH_CUDA(cudaMalloc((void**)b, n * sizeof(double)));
         c->d.cap_mg_vec = n;
     }
-    launch_mg_level0(c);
+    // the pair path wrote the level-0 stencils already, except for the cells
+    // it flagged for the per-row kernel
+    launch_mg_level0(c, c->level0_done ? c->d.cell_flags : nullptr);
     for (int L = 1; L < c->depth; ++L) launch_mg_coarse(c, L);
     launch_mg_invd(c);
     MPH_CUDA(cudaGetLastError());
@@ -646,7 +654,8 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
                     (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
                     (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
-                    (void*)d.pes16, (void*)d.pscale, (void*)d.wkey, (void*)d.wval, d.scan_tmp})
+                    (void*)d.pes16, (void*)d.pscale, (void*)d.wkey, (void*)d.wval, (void*)d.ccell,
+                    (void*)d.io3, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

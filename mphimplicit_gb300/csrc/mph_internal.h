@@ -138,6 +138,8 @@ struct DeviceState {
     unsigned short* pes16 = nullptr;   // the inner operator's copy of g: FP16, scaled per slice
     long long cap_pes16 = 0;
     float* pscale = nullptr;           // per slice: g = pes16 * pscale
+    int* ccell = nullptr;              // packed cell coordinates of every particle (pair path)
+    double* io3 = nullptr;             // host-layout staging, 2 x N x 3 doubles (state upload, field download)
     int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
     float* wval = nullptr;             // the sums of C_jk over each (level-0 stencils of the pair path)
     float* sdiag32 = nullptr;
@@ -224,6 +226,7 @@ struct mph_case {
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
+    bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
@@ -320,7 +323,8 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap);
 int launch_pairs_to_slices(mph_case* c);
 int launch_ct_slices(mph_case* c);
 int launch_part_pairs(mph_case* c, const struct Level0Map& M, bool* done);
-void launch_mg_level0(mph_case* c);
+void launch_mg_level0(mph_case* c, const int* only_cells);
+int ensure_mg_cof(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);
 int run_cr_solve(mph_case* c);
