@@ -14,9 +14,9 @@ physics, assembly, multigrid build, CR solve).
           matrix alone is ~7 GB, far above L2); the line also carries the
           plain FP64 form's value on the same workload and the velocity
           difference of one step of each form from the same state
-  e2e   : the same metric through the public API with host buffers: every
-          step uploads the particle state (mph_case_set_state) and reads back
-          positions and velocities (mph_get_fields)
+  e2e   : the same metric through the public API with pinned host buffers:
+          every step uploads the particle state (mph_case_set_state) and reads
+          back ids, types, positions and velocities (mph_get_fields)
   --impl reference : the CPU restatement of the reference (the oracle,
           OpenMP over all host cores) on a bounded sample of the workload
 """
@@ -503,8 +503,12 @@ def main():
     scal = case.scalars()
     value, total_s = replica_throughput(N * args.steps, total_s, dist, "cuda")
 
-    # end to end through the public API with host buffers
-    fields = case.fields(("id", "type", "pos", "vel"))
+    # end to end through the public API with host buffers (pinned)
+    def pinned(shape, dt):
+        return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    fields = {"id": pinned((N,), torch.int32), "type": pinned((N,), torch.int32), "pos": pinned((N, 3), torch.float64),
+              "vel": pinned((N, 3), torch.float64)}
+    case.fields(out=fields)
     host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
                              fields["vel"])
     ids = fields["id"]
@@ -519,9 +523,9 @@ def main():
     for _ in range(args.e2e_steps):
         case.set_state(host, ids, wc)
         case.step(1)
-        f = case.fields(("id", "type", "pos", "vel"))
-        host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, f["type"], f["pos"], f["vel"])
-        ids = f["id"]
+        case.fields(out=fields)   # read back into the same pinned buffers
+        host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
+                                 fields["vel"])
         wc = case.export("WallCenter")
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0

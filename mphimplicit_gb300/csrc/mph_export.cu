@@ -254,10 +254,78 @@ int case_scalars(mph_case* c, double* out, int n)
     return MPH_OK;
 }
 
+// ---- host-layout particle records: N x 3 doubles <-> the device's N x VS ----------
+template <int D>
+__global__ void k_pack3(int N, const double* __restrict__ src, double zfill, double* __restrict__ dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double v[3];
+    load_vec<D>(src, i, v);
+    dst[3 * (size_t)i] = v[0];
+    dst[3 * (size_t)i + 1] = v[1];
+    dst[3 * (size_t)i + 2] = D == 3 ? v[2] : zfill;
+}
+
+template <int D>
+__global__ void k_unpack3(int N, const double* __restrict__ src, double* __restrict__ dst)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double v[3] = {src[3 * (size_t)i], src[3 * (size_t)i + 1], D == 3 ? src[3 * (size_t)i + 2] : 0.0};
+    store_vec<D>(dst, i, v);
+}
+
+__global__ void k_iota(int N, int* __restrict__ a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) a[i] = i;
+}
+
+static int ensure_io3(mph_case* c)
+{
+    if (!c->d.io3) MPH_CUDA(cudaMalloc((void**)&c->d.io3, (size_t)c->dp.N * 6 * sizeof(double)));
+    return MPH_OK;
+}
+
+// stage the N x 3 host layout of a device vector array in io3 slot `slot`
+static void pack3(mph_case* c, const double* src, double zfill, int slot)
+{
+    const int N = c->dp.N;
+    double* dst = c->d.io3 + (size_t)slot * N * 3;
+    if (c->dim == 2) { k_pack3<2><<<grid_for(N, 256), 256, 0, c->stream>>>(N, src, zfill, dst); MPH_COUNT_LAUNCH(); }
+    else { k_pack3<3><<<grid_for(N, 256), 256, 0, c->stream>>>(N, src, zfill, dst); MPH_COUNT_LAUNCH(); }
+}
+
+// The fields go straight from device memory to the caller's buffers: the
+// per-particle arrays by one copy each, the vector arrays after a kernel puts
+// them in the N x 3 host layout (a pinned caller buffer takes the copies at
+// link speed).  Fields that need the output-step computations go through
+// build_export.
 int case_get_fields(mph_case* c, mph_fields* f)
 {
     if (!c || !f) return fail(MPH_ERR_ARG, "null argument");
     const int N = c->dp.N;
+    DeviceState& d = c->d;
+    MPH_TRY(ensure_io3(c));
+    const size_t b3 = (size_t)N * 3 * sizeof(double);
+    if (f->id) MPH_CUDA(cudaMemcpyAsync(f->id, d.id, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (f->type) MPH_CUDA(cudaMemcpyAsync(f->type, d.type, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (f->neighbor_count) MPH_CUDA(cudaMemcpyAsync(f->neighbor_count, d.nc, (size_t)N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (f->pos) {
+        pack3(c, d.pos, c->z_plane, 0);
+        MPH_CUDA(cudaMemcpyAsync(f->pos, d.io3, b3, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (f->vel) {
+        pack3(c, d.vel, 0.0, 1);
+        MPH_CUDA(cudaMemcpyAsync(f->vel, d.io3 + (size_t)N * 3, b3, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (f->force) {
+        MPH_CUDA(cudaStreamSynchronize(c->stream));   // slot 0 is free again
+        pack3(c, d.force, 0.0, 0);
+        MPH_CUDA(cudaMemcpyAsync(f->force, d.io3, b3, cudaMemcpyDeviceToHost, c->stream));
+    }
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
     Out o;
     auto take_i = [&](const char* nm, int* dst) -> int {
         if (!dst) return MPH_OK;
@@ -271,12 +339,7 @@ int case_get_fields(mph_case* c, mph_fields* f)
         std::memcpy(dst, o.f64.data(), n * sizeof(double));
         return MPH_OK;
     };
-    MPH_TRY(take_i("ParticleIndex", f->id));
-    MPH_TRY(take_i("Property", f->type));
-    MPH_TRY(take_i("NeighborCount", f->neighbor_count));
-    MPH_TRY(take_d("Position", f->pos, (size_t)N * 3));
-    MPH_TRY(take_d("Velocity", f->vel, (size_t)N * 3));
-    MPH_TRY(take_d("Force", f->force, (size_t)N * 3));
+    (void)take_i;
     MPH_TRY(take_d("VolStrainP", f->vol_strain_p, N));
     MPH_TRY(take_d("DivergenceP", f->divergence_p, N));
     MPH_TRY(take_d("PressureP", f->pressure_p, N));
@@ -302,20 +365,24 @@ int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_c
         }
     }
     if (nf != c->dp.Nf) return fail(MPH_ERR_INPUT, "fluid particle count differs from the case");
-    const int VSn = vs_of(c->dim);
-    std::vector<double> pos((size_t)N * VSn, 0.0), vel((size_t)N * VSn, 0.0);
-    std::vector<int> id(N);
-    for (int i = 0; i < N; ++i) {
-        for (int k = 0; k < c->dim; ++k) {
-            pos[(size_t)i * VSn + k] = parts->pos[3 * i + k];
-            vel[(size_t)i * VSn + k] = parts->vel[3 * i + k];
-        }
-        id[i] = parts->id ? parts->id[i] : i;
+    // the caller's N x 3 arrays go to device staging as they are (a pinned
+    // caller buffer copies at link speed); a kernel lays them out as N x VS
+    MPH_TRY(ensure_io3(c));
+    DeviceState& d = c->d;
+    const size_t b3 = (size_t)N * 3 * sizeof(double);
+    MPH_CUDA(cudaMemcpyAsync(d.io3, parts->pos, b3, cudaMemcpyHostToDevice, c->stream));
+    MPH_CUDA(cudaMemcpyAsync(d.io3 + (size_t)N * 3, parts->vel, b3, cudaMemcpyHostToDevice, c->stream));
+    MPH_CUDA(cudaMemcpyAsync(d.type, parts->type, (size_t)N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    if (parts->id) MPH_CUDA(cudaMemcpyAsync(d.id, parts->id, (size_t)N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    else { k_iota<<<grid_for(N, 256), 256, 0, c->stream>>>(N, d.id); MPH_COUNT_LAUNCH(); }
+    const unsigned g = grid_for(N, 256);
+    if (c->dim == 2) {
+        { k_unpack3<2><<<g, 256, 0, c->stream>>>(N, d.io3, d.pos); MPH_COUNT_LAUNCH(); }
+        { k_unpack3<2><<<g, 256, 0, c->stream>>>(N, d.io3 + (size_t)N * 3, d.vel); MPH_COUNT_LAUNCH(); }
+    } else {
+        { k_unpack3<3><<<g, 256, 0, c->stream>>>(N, d.io3, d.pos); MPH_COUNT_LAUNCH(); }
+        { k_unpack3<3><<<g, 256, 0, c->stream>>>(N, d.io3 + (size_t)N * 3, d.vel); MPH_COUNT_LAUNCH(); }
     }
-    MPH_CUDA(cudaMemcpyAsync(c->d.pos, pos.data(), pos.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    MPH_CUDA(cudaMemcpyAsync(c->d.vel, vel.data(), vel.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    MPH_CUDA(cudaMemcpyAsync(c->d.type, parts->type, (size_t)N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    MPH_CUDA(cudaMemcpyAsync(c->d.id, id.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     if (wall_center) std::memcpy(&c->wallC[0][0], wall_center, sizeof(c->wallC));
     c->time = parts->time;

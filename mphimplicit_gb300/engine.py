@@ -209,16 +209,25 @@ class Case:
         _check(self.lib.mph_case_time(self.h, ctypes.byref(t)))
         return t.value
 
-    def fields(self, which=None) -> Dict[str, np.ndarray]:
+    def fields(self, which=None, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
         """Per-particle fields (cell order) copied to host; `which` selects a
         subset of id, type, pos, vel, force, vol_strain_p, divergence_p,
-        pressure_p, virial_p, neighbor_count."""
+        pressure_p, virial_p, neighbor_count.  `out` supplies the buffers
+        (contiguous, int32 / float64 of the field's shape; pinned host memory
+        takes the copies at link speed)."""
         n = self.count
-        out = {"id": np.empty(n, np.int32), "type": np.empty(n, np.int32), "pos": np.empty((n, 3)), "vel": np.empty((n, 3)),
-               "force": np.empty((n, 3)), "vol_strain_p": np.empty(n), "divergence_p": np.empty(n),
-               "pressure_p": np.empty(n), "virial_p": np.empty(n), "neighbor_count": np.empty(n, np.int32)}
-        if which is not None:
-            out = {k: v for k, v in out.items() if k in which}
+        if out is None:
+            out = {"id": np.empty(n, np.int32), "type": np.empty(n, np.int32), "pos": np.empty((n, 3)), "vel": np.empty((n, 3)),
+                   "force": np.empty((n, 3)), "vol_strain_p": np.empty(n), "divergence_p": np.empty(n),
+                   "pressure_p": np.empty(n), "virial_p": np.empty(n), "neighbor_count": np.empty(n, np.int32)}
+            if which is not None:
+                out = {k: v for k, v in out.items() if k in which}
+        else:
+            for k, a in out.items():
+                want = (n,) if k in ("id", "type", "neighbor_count", "vol_strain_p", "divergence_p", "pressure_p", "virial_p") else (n, 3)
+                dt = np.int32 if k in ("id", "type", "neighbor_count") else np.float64
+                if a.shape != want or a.dtype != dt or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"fields: buffer {k} must be a contiguous {np.dtype(dt).name} array of shape {want}")
         f = MphFields()
         for k, a in out.items():
             setattr(f, k, np_ptr(a, ctypes.c_int if a.dtype == np.int32 else ctypes.c_double))
