@@ -40,6 +40,14 @@ constexpr int kPairWarps = 8;
 #ifndef MPH_PAIR_MINB
 #define MPH_PAIR_MINB 1
 #endif
+// threads per block of k_visc_pen32 (rows of a block share L1 for their x gathers)
+#ifndef MPH_PAIR_BLOCK
+#define MPH_PAIR_BLOCK 512
+#endif
+// threads per block of k_ct_apply32
+#ifndef MPH_CT_BLOCK
+#define MPH_CT_BLOCK 256
+#endif
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
@@ -276,7 +284,7 @@ constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 
 template <int D>
-__global__ void __launch_bounds__(256) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
+__global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
                                                     const int* __restrict__ ctscol, const float* __restrict__ ctsval,
                                                     const float* __restrict__ x, float* __restrict__ t,
                                                     const double* __restrict__ scal, int* __restrict__ flags, int cap)
@@ -352,7 +360,7 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
 }
 
 template <int D>
-__global__ void __launch_bounds__(128, MPH_PAIR_MINB)
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ pes16, const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
@@ -530,15 +538,15 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
     unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
-    const unsigned gt = grid_for(P.N, 256);
-    const unsigned gv = grid_for(P.Nf, 128);
+    const unsigned gt = grid_for(P.N, MPH_CT_BLOCK);
+    const unsigned gv = grid_for(P.Nf, MPH_PAIR_BLOCK);
     if (c->dim == 2) {
-        { k_ct_apply32<2><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<2><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+        { k_ct_apply32<2><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
+        { k_visc_pen32<2><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
                                                      d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_apply32<3><<<gt, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<3><<<gv, 128, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
+        { k_ct_apply32<3><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
+        { k_visc_pen32<3><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
                                                      d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
     }
 }
