@@ -40,7 +40,8 @@ constexpr int kPairWarps = 8;
 #ifndef MPH_PAIR_MINB
 #define MPH_PAIR_MINB 1
 #endif
-// threads per block of k_visc_pen32 (rows of a block share L1 for their x gathers)
+// threads per block of k_visc_pen32 and k_resid_pairs (rows of a block share
+// L1 for their x gathers)
 #ifndef MPH_PAIR_BLOCK
 #define MPH_PAIR_BLOCK 512
 #endif
@@ -496,7 +497,7 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
 // FP32 on x32 from the sliced pair terms (as the inner operator), inertia and
 // C Lambda t (t = C^T x) in FP64; (r, r) -> *out.
 template <int D>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK)
 k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __restrict__ nfc, const long long* __restrict__ sptr,
               const int* __restrict__ acol, const float* __restrict__ pes, const float* __restrict__ sdiag,
               const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
@@ -996,14 +997,14 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     const long long nv = (long long)P.Nf * c->dim;
     { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
     if (c->step_pairs) {
-        const unsigned gr = grid_for(P.Nf, 128);
+        const unsigned gr = grid_for(P.Nf, MPH_PAIR_BLOCK);
         if (c->dim == 2) {
             { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<2><<<gr, 128, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+            { k_resid_pairs<2><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         } else {
             { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<3><<<gr, 128, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+            { k_resid_pairs<3><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         }
         return;
