@@ -31,6 +31,12 @@
 namespace mph {
 
 constexpr int kPairWarps = 8;
+// warps per block of k_pair_terms (consecutive rows of a block share L1 for
+// their position gathers)
+#ifndef MPH_PT_WARPS
+#define MPH_PT_WARPS 16
+#endif
+constexpr int kPtWarps = MPH_PT_WARPS;
 
 // Tuning of the inner operator's viscous loop: slots unrolled per step and
 // the minimum resident blocks of k_visc_pen32 (register cap).
@@ -61,7 +67,7 @@ constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 // keeps the factored form off when that bound would reach 1e-2 of the outer
 // tolerance).  Inertia and C p stay FP64.
 template <int D>
-__global__ void __launch_bounds__(kPairWarps * 32)
+__global__ void __launch_bounds__(kPtWarps * 32)
 k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const float* __restrict__ pos32,
              const float* __restrict__ poslo32, const double* __restrict__ vel,
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
@@ -570,6 +576,7 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 // cell; the per-row FP64 kernel then assembles that cell's rows and
 // k_mg_level0 that cell's level-0 rows.
 constexpr int kWBins = 8;
+static_assert(kWBins * 3 <= 32, "one lane per bin and row component");
 
 // Neighbour-grid cell coordinates packed 10 bits an axis (grids of at most
 // 1024 cells an axis), so the stencil slot of one cell seen from another is
@@ -794,12 +801,17 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
                 bad = __any_sync(full, over) || bad;
                 __syncwarp();
                 if (bad) break;
-                for (int q = 0; q < na; ++q) {
-                    for (int t = lane; t < kWBins * DD; t += 32) {
-                        const int b = t / DD, rs = t - b * DD;
+                for (int q = 0; q < na; ++q) {   // lane (bin, row component): a block row of one bin
+                    if (lane < kWBins * D) {
+                        const int b = lane / D, r = lane - b * D;
                         const int slot = stslot[q * kWBins + b];
-                        if (slot < 0) continue;
-                        acc[slot * DD + rs] += stcl[q * 3 + rs / D] * stval[(q * kWBins + b) * 3 + rs % D];
+                        if (slot >= 0) {
+                            const float cr = stcl[q * 3 + r];
+                            const float* w = stval + (q * kWBins + b) * 3;
+                            float* a = acc + slot * DD + r * D;
+#pragma unroll
+                            for (int c2 = 0; c2 < D; ++c2) a[c2] += cr * w[c2];
+                        }
                     }
                     __syncwarp();
                 }
@@ -909,12 +921,12 @@ int launch_pair_terms(mph_case* c)
         sdiag = d.sdiag32;
         cvl = d.cvl32;
     }
-    const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, 152LL * 16);
+    const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
     if (c->dim == 2) {
-        { k_pair_terms<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+        { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
                                                                d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_pair_terms<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+        { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
                                                                d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
