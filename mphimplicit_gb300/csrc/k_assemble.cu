@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
     const int lane = i & 31;
     const long long sbase = sptr[i >> 5];
     int* colp = acol + sbase + lane;
-    double* valp = aval + sbase * DD + lane;
+    double* valp = aval ? aval + sbase * DD + lane : nullptr;   // null when the FP64 operator is factored
     float* valp32 = aval32 ? aval32 + sbase * DD + lane : nullptr;   // mixed form: FP32 copy
 
     const int ti = type[i];
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
         for (int r = 0; r < D; ++r)
 #pragma unroll
             for (int s = 0; s < D; ++s) {
-                valp[((long long)k * DD + r * D + s) * 32] = blk[r][s];
+                if (aval) valp[((long long)k * DD + r * D + s) * 32] = blk[r][s];
                 if (valp32) valp32[((long long)k * DD + r * D + s) * 32] = (float)blk[r][s];
             }
         // per-cell partial sums of the row (runs of equal stencil slot)
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
         for (int r = 0; r < D; ++r)
 #pragma unroll
             for (int s = 0; s < D; ++s) {
-                valp[((long long)self * DD + r * D + s) * 32] = blk[r][s];
+                if (aval) valp[((long long)self * DD + r * D + s) * 32] = blk[r][s];
                 if (valp32) valp32[((long long)self * DD + r * D + s) * 32] = (float)blk[r][s];
             }
 #pragma unroll
@@ -420,21 +420,41 @@ int launch_assemble(mph_case* c)
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     const int kmax_rows = h_width / 32;   // longest fluid row
     c->nslots = h_slots;
+    // the form of this step's system decides which block arrays exist: FP64
+    // blocks unless the FP64 operator is factored, FP32 blocks for the mixed
+    // form unless its inner operator runs on the pair terms
+    c->step_factored = factored_applies(c);
+    c->step_pairs = c->step_factored && !c->inner_blocks && c->visc_nonneg;
     {
         long long cap = c->d.cap_slots;
         void* p = c->d.acol;
         MPH_TRY(ensure(&p, &cap, h_slots, sizeof(int)));
         c->d.acol = (int*)p;
-        if (cap != c->d.cap_slots) {
+        c->d.cap_slots = cap;
+        const bool need64 = !c->step_factored, need32 = c->precision == MPH_PRECISION_MIXED && !c->step_pairs;
+        if (need64 && cap > c->d.cap_aval) {
             if (c->d.aval) cudaFree(c->d.aval);
             c->d.aval = nullptr;
+            c->d.cap_aval = 0;
             MPH_CUDA(cudaMalloc(&c->d.aval, (size_t)cap * D * D * sizeof(double)));
-            if (c->precision == MPH_PRECISION_MIXED) {
-                if (c->d.aval32) cudaFree(c->d.aval32);
-                c->d.aval32 = nullptr;
-                MPH_CUDA(cudaMalloc(&c->d.aval32, (size_t)cap * D * D * sizeof(float)));
-            }
-            c->d.cap_slots = cap;
+            c->d.cap_aval = cap;
+        }
+        if (need32 && cap > c->d.cap_aval32) {
+            if (c->d.aval32) cudaFree(c->d.aval32);
+            c->d.aval32 = nullptr;
+            c->d.cap_aval32 = 0;
+            MPH_CUDA(cudaMalloc(&c->d.aval32, (size_t)cap * D * D * sizeof(float)));
+            c->d.cap_aval32 = cap;
+        }
+        if (!need64 && c->d.aval) {   // a form change (option) since the last step: release what is unused
+            cudaFree(c->d.aval);
+            c->d.aval = nullptr;
+            c->d.cap_aval = 0;
+        }
+        if (!need32 && c->d.aval32) {
+            cudaFree(c->d.aval32);
+            c->d.aval32 = nullptr;
+            c->d.cap_aval32 = 0;
         }
     }
     // C values for the fluid rows (aligned with the P-list)
@@ -472,8 +492,6 @@ int launch_assemble(mph_case* c)
     const int pon = prof_begin(c, 2, &pe);
     bool cells = false;
     c->ct_ready = false;
-    c->step_factored = factored_applies(c);
-    c->step_pairs = c->step_factored && !c->inner_blocks && c->visc_nonneg;
     c->level0_done = false;
     if (c->step_factored) {
         // mixed form: FP64 pair terms and b, transposed P-lists (the factored
@@ -487,7 +505,7 @@ int launch_assemble(mph_case* c)
         else MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
     }
     const int* only = cells ? c->d.cell_flags : nullptr;
-    float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;
+    float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;   // null on the pair path
     if (D == 2) {
         { k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, only, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc,
                                                  c->d.nptr, c->d.nind, c->d.ncp, c->d.nptrP, c->d.nindP, c->d.cval, c->d.pvec, c->d.sptr,

@@ -57,11 +57,20 @@ int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, i
     double b = 0.0;
     b += (double)N * 400.0;                                   // particle vectors, keys, sort scratch
     b += (double)N * (nb + np) * 4.0 + (double)N * 32.0;      // neighbour lists and row pointers
-    const double blocks = 1.10 * (double)Nf * nb;             // A, with slice padding
-    b += blocks * (DD * 8.0 + 4.0);
-    if (precision == MPH_PRECISION_MIXED) {
-        b += 2.0 * blocks * DD * 4.0;                         // FP32 blocks, sliced and row-contiguous
-        b += (double)Nf * nb * 16.0;                          // FP32 pair terms
+    const double blocks = 1.10 * (double)Nf * nb;             // block slots of A, with slice padding
+    b += blocks * 4.0;                                        // block columns
+    if (precision == MPH_PRECISION_MIXED && pair_path_expected(prm, parts, dim)) {
+        // default options, factored operator, inner operator on pair terms:
+        // no blocks; pair terms, their sliced FP32 / FP16 copies, sliced
+        // P-lists and transposed P-lists, level-0 cell bins
+        b += (double)Nf * nb * 16.0 + blocks * D * 6.0;
+        b += (double)Nf * np * (D * 4.0 + 4.0) * 2.2 + (double)N * (8.0 * 16.0 + 8.0) + (double)Nf * 32.0;
+    } else {
+        b += blocks * DD * 8.0;                               // FP64 blocks
+        if (precision == MPH_PRECISION_MIXED) {
+            b += 2.0 * blocks * DD * 4.0;                     // FP32 blocks, sliced and row-contiguous
+            b += (double)Nf * nb * 16.0;                      // FP32 pair terms
+        }
     }
     b += (double)Nf * np * (D * 8.0) * 2.0;                   // C and its transpose values
     b += (double)Nf * np * 4.0 * 2.0 + (double)N * 24.0;      // transpose indices and pointers

@@ -596,6 +596,19 @@ int stage_output_fields(mph_case* c)
 }
 
 // ---- create / destroy ---------------------------------------------------------
+// Whether a mixed-form case created from these inputs with the default
+// options steps on the pair-term path (no assembled blocks): the parameter
+// derivation of case creation, without device work.
+bool pair_path_expected(const mph_params* prm, const mph_particles* parts, int dim)
+{
+    mph_case c;
+    c.dim = dim;
+    c.precision = MPH_PRECISION_MIXED;
+    c.prm = *prm;
+    if (derive(&c, parts) != MPH_OK) return false;
+    return factored_applies(&c) && c.inner_blocks == false && c.visc_nonneg;
+}
+
 int case_create(const mph_params* prm, const mph_particles* parts, int dim, int precision, void* stream, mph_case** out)
 {
     if (!out) return fail(MPH_ERR_ARG, "null output handle");

@@ -96,7 +96,7 @@ struct DeviceState {
     int* acol = nullptr;           // [slots]
     double* aval = nullptr;        // [slots*D*D]
     float* aval32 = nullptr;       // mixed precision copy
-    long long cap_slots = 0;
+    long long cap_slots = 0, cap_aval = 0, cap_aval32 = 0;
     double *bvec = nullptr, *invDiag = nullptr;
     int* selfk = nullptr;          // position of the self block in each row
     // matrix C and source p
@@ -317,6 +317,7 @@ int launch_assemble(mph_case* c);
 int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done);
 int build_ct(mph_case* c);
 bool factored_applies(const mph_case* c);
+bool pair_path_expected(const mph_params* prm, const mph_particles* parts, int dim);
 int launch_pair_terms(mph_case* c);
 void launch_resid_factored(mph_case* c, const double* x, double* r, double* out);
 void launch_apply32(mph_case* c, const float* x, float* y, int cap);
