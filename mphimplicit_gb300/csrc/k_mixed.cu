@@ -316,7 +316,7 @@ static int mixed_solve_t(mph_case* c)
     // One FP32 CR iteration; its index lives in flags[kFlagIter] (it runs on
     // across refinement steps), so one launch sequence serves every iteration
     // and replays as a graph.  Iterations after a stop return at once.
-    auto iteration = [&, c](cudaEvent_t* e) {
+    auto iteration = [&, c](cudaEvent_t* e, cudaEvent_t ev_end) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
         if (c->step_pairs) {
             launch_apply32(c, s32, y32, cap);   // FP32 pair terms, no assembled blocks
@@ -325,16 +325,26 @@ static int mixed_solve_t(mph_case* c)
                                                   counter);
             MPH_COUNT_LAUNCH();
         }
-        if (e) prof_begin(c, 0, &e[1]);
+        if (ev_end) cudaEventRecordWithFlags(ev_end, st, cudaEventRecordExternal);   // profiled graph: the operator's end
+        else if (e) prof_begin(c, 0, &e[1]);
         { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
         vcycle_mixed(c, q32, u32, scal + kSQU32);
         { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
-    const int chunk = 8;
-    const bool graphs = c->use_graphs && !c->prof.on;
+    const int chunk = kGraphChunk;
+    const bool graphs = c->use_graphs;
+    // with profiling on, the captured chunk records a fixed event pair around
+    // every iteration's operator; the pairs of the iterations that ran are
+    // read after each chunk
+    const bool gprof = graphs && c->prof.on;
+    if (gprof && !c->gev[0])
+        for (int k = 0; k < 2 * kGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
     if (graphs) {
         MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, tol_in2, cap), [&] {
-            for (int k = 0; k < chunk; ++k) iteration(nullptr);
+            for (int k = 0; k < chunk; ++k) {
+                if (gprof) cudaEventRecordWithFlags(c->gev[2 * k], c->stream, cudaEventRecordExternal);   // a record node
+                iteration(nullptr, gprof ? c->gev[2 * k + 1] : nullptr);
+            }
         }, &c->mx_launches));
     }
     const long long chunk_launches = c->mx_launches;
@@ -360,6 +370,7 @@ static int mixed_solve_t(mph_case* c)
         vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
         bool done = false;
         while (!done) {
+            const int it_before = host_flags[kFlagIter];
             if (graphs) {
                 MPH_CUDA(cudaGraphLaunch(c->mx_exec, st));
                 g_launch_count += chunk_launches;
@@ -368,12 +379,21 @@ static int mixed_solve_t(mph_case* c)
                 for (int k = 0; k < chunk; ++k, ++launched) {
                     cudaEvent_t e[2] = {nullptr, nullptr};
                     const bool pon = prof_begin(c, 0, &e[0]) != 0;
-                    iteration(pon ? e : nullptr);
+                    iteration(pon ? e : nullptr, nullptr);
                     if (pon) timed.push_back({launched, {e[0], e[1]}});
                 }
             }
             MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
             MPH_CUDA(cudaStreamSynchronize(st));
+            if (gprof) {   // the operators of the iterations this chunk ran
+                const int ran = std::min(chunk, std::max(0, host_flags[kFlagIter] - it_before));
+                for (int k = 0; k < ran; ++k) {
+                    float ms = 0.f;
+                    MPH_CUDA(cudaEventElapsedTime(&ms, c->gev[2 * k], c->gev[2 * k + 1]));
+                    c->prof.kern_ms[0] += ms;
+                    c->prof.kern_n[0] += 1;
+                }
+            }
             done = host_flags[kFlagDone] != 0 || launched > cap + chunk;
         }
         if (host_flags[kFlagBad]) { bad = true; break; }

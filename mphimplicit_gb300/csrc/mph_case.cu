@@ -657,6 +657,8 @@ int case_destroy(mph_case* c)
     if (c->cr_exec) cudaGraphExecDestroy(c->cr_exec);
     if (c->mx_exec) cudaGraphExecDestroy(c->mx_exec);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    for (cudaEvent_t e : c->gev)
+        if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     for (void* p : c->allocations) cudaFree(p);
     DeviceState& d = c->d;

@@ -226,6 +226,7 @@ struct mph_case {
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
+    cudaEvent_t gev[16] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step

@@ -37,3 +37,26 @@ def test_graph_replay_is_bit_identical(engine_lib, case, precision):
     assert np.array_equal(fa["id"], fb["id"])
     assert np.array_equal(fa["pos"], fb["pos"])
     assert np.array_equal(fa["vel"], fb["vel"])
+
+
+@pytest.mark.parametrize("case", CASES[:2], ids=IDS[:2])
+def test_profiled_mixed_steps_keep_graphs_and_bits(engine_lib, case):
+    """With kernel profiling on, the mixed form still replays its CR chunks as
+    graphs (each chunk records an event pair around every iteration's
+    operator): the operator timings cover exactly the iterations that ran,
+    and the step gives the same bits as an unprofiled one."""
+    name, dim, params, parts = case
+    a = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    a.profile(True)
+    a.step(2)
+    p = a.profile_read()
+    b = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    iters = 0
+    for _ in range(2):
+        b.step(1)
+        iters += b.solve_stats()["iter"]
+    assert p["kern_n_spmv"] == iters
+    assert p["kern_ms_spmv"] > 0.0
+    fa, fb = a.fields(("id", "pos", "vel")), b.fields(("id", "pos", "vel"))
+    for k in ("id", "pos", "vel"):
+        assert np.array_equal(fa[k], fb[k]), k
