@@ -73,7 +73,8 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
-             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ sdiag32, float* __restrict__ cvl32)
+             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ sdiag32, float* __restrict__ cvl32,
+             unsigned* __restrict__ gmax)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -89,6 +90,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         load_f32<D>(poslo32, i, li);
         float sumw[3] = {0.f, 0.f, 0.f};
         float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over the wall slots: xx xy xz yy yz zz
+        float lm = 0.f;                                  // largest |g| component of the fluid slots
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
             float e[3] = {0.f, 0.f, 0.f};
@@ -143,6 +145,12 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                 }
             }
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
+            if (k < nf) lm = fmaxf(lm, sqrtf(f) * fmaxf(fabsf(e[0]), fmaxf(fabsf(e[1]), fabsf(e[2]))));
+        }
+        if (gmax) {   // the slice's largest |g| component, for the FP16 scale (f >= 0: bits order as values)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) lm = fmaxf(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+            if (lane == 0) atomicMax(gmax + (i >> 5), __float_as_uint(lm));
         }
         if (sdiag32) {   // the row's wall part of the viscous diagonal block and its FP32 inertia
 #pragma unroll
@@ -440,24 +448,11 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
     const long long sb = sptr[sl];
     const int w = (int)((sptr[sl + 1] - sb) / 32);   // entries per row of the slice
     float inv16 = 0.f;
-    if (PAIRS) {   // the slice's largest |g| component maps to 2^15 in the FP16 copy
-        __shared__ float wmax[8];
-        float m = 0.f;
-        for (int t = threadIdx.x; t < 32 * w; t += blockDim.x) {
-            const int r = t / w, k = t % w;
-            if (k < rn[r]) {
-                const float4 pv = pe32[rb[r] + k];
-                m = fmaxf(m, sqrtf(pv.w) * fmaxf(fabsf(pv.x), fmaxf(fabsf(pv.y), fabsf(pv.z))));
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
-        __syncthreads();
-        m = 0.f;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) m = fmaxf(m, wmax[k]);
+    if (PAIRS) {   // the slice's largest |g| component (from k_pair_terms, as bits) maps to 2^15
+        const float m = __uint_as_float(reinterpret_cast<const unsigned*>(sscale)[sl]);
         const float sigma = m / 32768.f;
         inv16 = m > 0.f ? 1.f / sigma : 0.f;
+        __syncthreads();   // every thread has read the maximum before it is replaced by the scale
         if (threadIdx.x == 0) sscale[sl] = sigma;
     }
     for (int k0 = 0; k0 < w; k0 += kLtsK) {
@@ -915,19 +910,23 @@ int launch_pair_terms(mph_case* c)
     { k_cval_f32<<<grid_for(ncv, 256), 256, 0, c->stream>>>(ncv, d.cval, d.cval32); MPH_COUNT_LAUNCH(); }
     float* sdiag = nullptr;
     float* cvl = nullptr;
+    unsigned* gmax = nullptr;
     if (c->step_pairs) {   // FP32 inner operator on the pair terms
         if (!d.sdiag32) MPH_CUDA(cudaMalloc((void**)&d.sdiag32, (size_t)P.Nf * 8 * sizeof(float)));
         MPH_TRY(grow_f(&d.cvl32, &d.cap_cvl32, ncv));
         sdiag = d.sdiag32;
         cvl = d.cvl32;
+        if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float)));
+        MPH_CUDA(cudaMemsetAsync(d.pscale, 0, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float), c->stream));
+        gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
     }
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl, gmax); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl, gmax); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }
