@@ -436,7 +436,7 @@ def main():
     ap.add_argument("--outer-tol", type=float, default=1e-6,
                     help="mixed form: FP64 outer relative residual (the reference's tolerance is 1e-6)")
     ap.add_argument("--cases", type=int, default=0, help="ensemble / serve: number of cases (0: 512 / 24)")
-    ap.add_argument("--workers", type=int, default=32, help="ensemble / serve: host worker threads")
+    ap.add_argument("--workers", type=int, default=64, help="ensemble / serve: host worker threads")
     ap.add_argument("--sample", type=int, default=16, help="ensemble: cases timed alone in the FP64 form")
     ap.add_argument("--serve-step-scale", type=float, default=0.1, help="serve: factor on each request's step count")
     args = ap.parse_args()

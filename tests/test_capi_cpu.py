@@ -142,6 +142,9 @@ def test_footprint_bound_scales_with_case(lib):
     # several times a 2D one
     fixed = 64 << 20
     assert (c - fixed) / (s3.types < 2).sum() > 3 * (b - fixed) / (s2.types < 2).sum()
+    # the 3D mixed form steps on pair terms (no assembled blocks) by default,
+    # so its bound is below the FP64 form's, whose FP64 blocks dominate
+    assert serving.footprint(p3, s3, 3, PRECISION_MIXED) < c
 
 
 def test_server_rejects_requests_beyond_budget(lib):
