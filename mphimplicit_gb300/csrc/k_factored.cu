@@ -24,6 +24,7 @@
 // accumulation of the assembled form; in the residual only inertia and
 // C Lambda C^T (about 20 P-slots a row) are FP64.
 #include <cuda_fp16.h>
+#include <climits>
 
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
@@ -55,6 +56,12 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 #ifndef MPH_CT_BLOCK
 #define MPH_CT_BLOCK 256
 #endif
+// Block-local neighbour columns of the inner operator: the fluid neighbours
+// of a block of MPH_PAIR_BLOCK rows, sorted and deduplicated, at most kUMax
+// of them (their x then fits the block's shared memory), found through a
+// bitmap of an index window of at most kWinWords * 32 particles.
+constexpr int kUMax = 8192;
+constexpr int kWinWords = 1 << 14;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
@@ -337,12 +344,13 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
 // The viscous part of row i in FP32 from the sliced pair terms:
 // yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)), with g from the FP32
 // slices (pes32) or from the FP16 slices times the slice scale (HALF).
-template <int D, bool HALF>
+template <int D, bool HALF, bool LOC = false>
 __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, const float* __restrict__ sdiag,
                                            const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                            const int* __restrict__ acol, const float* __restrict__ pes,
                                            const unsigned short* __restrict__ pes16, const float* __restrict__ pscale,
-                                           const float* __restrict__ x, float* yv)
+                                           const float* __restrict__ x, float* yv,
+                                           const unsigned short* __restrict__ lidx = nullptr, const float* xs = nullptr)
 {
     const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
     const float4 s1 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8 + 4);
@@ -351,12 +359,15 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
     const long long base = sptr[i >> 5];
     const int* cp = acol + base + lane;
+    const unsigned short* lp = lidx + base + lane;
     const long long vo = base * D + lane;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
 #pragma unroll (kPairUnroll)
     for (int k = 0; k < n; ++k) {
-        const int col = __ldcs(cp + (long long)k * 32);
+        // LOC: the neighbour's x from the block's shared-memory copy, by its
+        // block-local index; else the global gather by column
+        const float* xj = LOC ? xs + (size_t)__ldcs(lp + (long long)k * 32) * D : x + (size_t)__ldcs(cp + (long long)k * 32) * D;
         float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -365,7 +376,7 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
         }
         float gx = 0.f;
 #pragma unroll
-        for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - x[(size_t)col * D + d]);
+        for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - xj[d]);
 #pragma unroll
         for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
     }
@@ -374,17 +385,32 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     for (int d = 0; d < 3; ++d) yv[d] += ys[d] * s2;
 }
 
-template <int D>
+template <int D, bool LOC>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ pes16, const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
              const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
-             const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
+             const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
+             const unsigned short* __restrict__ lidx, const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
+    extern __shared__ float xs_loc[];   // LOC: x of the block's neighbours, by block-local index
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int U = -1;
+    if (LOC) {   // stage x of the block's distinct neighbours once (block-uniform)
+        U = ucount[blockIdx.x];
+        if (U >= 0) {
+            const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+            for (int k = threadIdx.x; k < U; k += blockDim.x) {
+                const int j = ul[k];
+#pragma unroll
+                for (int d = 0; d < D; ++d) xs_loc[k * D + d] = x[(size_t)j * D + d];
+            }
+            __syncthreads();
+        }
+    }
     double acc = 0.0;
     if (i < Nf) {
         const int lane = i & 31;
@@ -392,7 +418,8 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
         float yv[3];
-        visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv);
+        if (LOC && U >= 0) visc_row32<D, true, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv, lidx, xs_loc);
+        else visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv);
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
@@ -544,12 +571,22 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     const unsigned gv = grid_for(P.Nf, MPH_PAIR_BLOCK);
     if (c->dim == 2) {
         { k_ct_apply32<2><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<2><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
-                                                     d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+        if (c->loc_smem)
+            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.lidx16, d.uniq, d.ucount);
+        else
+            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr, nullptr);
+        MPH_COUNT_LAUNCH();
     } else {
         { k_ct_apply32<3><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        { k_visc_pen32<3><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr, d.pscol, d.psval,
-                                                     d.tct32, x, y, d.scal, d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+        if (c->loc_smem)
+            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.lidx16, d.uniq, d.ucount);
+        else
+            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr, nullptr);
+        MPH_COUNT_LAUNCH();
     }
 }
 
@@ -838,6 +875,112 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
     }
 }
 
+// Block-local columns: for block b of MPH_PAIR_BLOCK rows (thread = row), the
+// sorted distinct fluid neighbours uniq[b][0..U) and, per fluid slot, the
+// neighbour's rank among them (16 bits).  A bitmap over the block's index
+// window [lo, hi] marks the neighbours; word ranks come from a block scan of
+// the word popcounts.  ucount[b] = U, or -1 when the window is wider than
+// kWinWords * 32 or U > kUMax (the operator then gathers by column).
+template <int D>
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const long long* __restrict__ sptr, const int* __restrict__ nfc,
+                                                             const int* __restrict__ acol, unsigned short* __restrict__ lidx,
+                                                             int* __restrict__ uniq, int* __restrict__ ucount)
+{
+    extern __shared__ unsigned lc_smem[];
+    unsigned* bm = lc_smem;                       // kWinWords bitmap words
+    unsigned* rank = lc_smem + kWinWords;         // kWinWords exclusive word ranks
+    __shared__ int red[2][32];
+    __shared__ unsigned wsum[32];
+    const int tid = threadIdx.x, lane = tid & 31, wl = tid >> 5, nwl = blockDim.x >> 5;
+    const int i = blockIdx.x * blockDim.x + tid;
+    const bool row = i < Nf;
+    const long long base = row ? sptr[i >> 5] + (i & 31) : 0;
+    const int n = row ? nfc[i] : 0;
+    // window of the block's columns
+    int lo = INT_MAX, hi = -1;
+    for (int k = 0; k < n; ++k) {
+        const int col = acol[base + (long long)k * 32];
+        lo = min(lo, col);
+        hi = max(hi, col);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) { red[0][wl] = lo; red[1][wl] = hi; }
+    __syncthreads();
+    lo = INT_MAX;
+    hi = -1;
+    for (int w = 0; w < nwl; ++w) { lo = min(lo, red[0][w]); hi = max(hi, red[1][w]); }
+    if (hi < 0) {   // no fluid neighbours in the block
+        if (tid == 0) ucount[blockIdx.x] = 0;
+        return;
+    }
+    const long long span = (long long)hi - lo + 1;
+    if (span > (long long)kWinWords * 32) {
+        if (tid == 0) ucount[blockIdx.x] = -1;
+        return;
+    }
+    const int nw = (int)((span + 31) >> 5);
+    for (int w = tid; w < nw; w += blockDim.x) bm[w] = 0u;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        const int off = acol[base + (long long)k * 32] - lo;
+        atomicOr(&bm[off >> 5], 1u << (off & 31));
+    }
+    __syncthreads();
+    // exclusive ranks of the words: thread chunks, then a block scan of the chunk sums
+    const int per = (nw + blockDim.x - 1) / blockDim.x;
+    const int w0 = min(nw, tid * per), w1 = min(nw, w0 + per);
+    unsigned cs = 0;
+    for (int w = w0; w < w1; ++w) cs += __popc(bm[w]);
+    unsigned inc = cs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[wl] = inc;
+    __syncthreads();
+    unsigned woff = 0, total = 0;
+    for (int w = 0; w < nwl; ++w) {
+        if (w < wl) woff += wsum[w];
+        total += wsum[w];
+    }
+    unsigned r = woff + inc - cs;
+    for (int w = w0; w < w1; ++w) {
+        rank[w] = r;
+        r += __popc(bm[w]);
+    }
+    __syncthreads();
+    const int U = (int)total;
+    if (U > kUMax) {
+        if (tid == 0) ucount[blockIdx.x] = -1;
+        return;
+    }
+    for (int k = 0; k < n; ++k) {
+        const long long e = base + (long long)k * 32;
+        const int off = acol[e] - lo;
+        const unsigned word = bm[off >> 5];
+        lidx[e] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
+    }
+    int* ul = uniq + (size_t)blockIdx.x * kUMax;
+    for (int w = w0; w < w1; ++w) {
+        unsigned word = bm[w];
+        unsigned rr = rank[w];
+        while (word) {
+            const int b = __ffs(word) - 1;
+            ul[rr++] = lo + w * 32 + b;
+            word &= word - 1u;
+        }
+    }
+    if (tid == 0) {
+        ucount[blockIdx.x] = U;
+        atomicMax(ucount + gridDim.x, U);
+    }
+}
+
 // ---- host side ---------------------------------------------------------------------
 static int grow_f(float** p, long long* cap, long long need)
 {
@@ -933,6 +1076,49 @@ int launch_pair_terms(mph_case* c)
 
 // The sliced pair terms g = sqrt(f) e with the block columns, and the sliced
 // lambda-scaled P-lists, of the fluid rows (after k_pair_terms).
+// Block-local neighbour columns of the inner operator (after the fluid
+// columns are sliced) and the shared memory its staged copy of x needs: the
+// largest block's distinct neighbours (read back; 0 when no block fits).
+static int launch_local_cols(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    c->loc_smem = 0;
+    if (P.Nf == 0) return MPH_OK;
+    const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK);
+    if (c->nslots > d.cap_lidx16) {
+        if (d.lidx16) cudaFree(d.lidx16);
+        d.lidx16 = nullptr;
+        d.cap_lidx16 = 0;
+        const long long n = c->nslots + c->nslots / 8 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.lidx16, (size_t)n * sizeof(unsigned short)));
+        d.cap_lidx16 = n;
+    }
+    MPH_TRY(grow_i(&d.uniq, &d.cap_uniq, nb * kUMax));
+    MPH_TRY(grow_i(&d.ucount, &d.cap_ucount, nb + 1));
+    const size_t smem = 2 * kWinWords * sizeof(unsigned);
+    if (c->dim == 2) {
+        MPH_CUDA(cudaFuncSetAttribute(k_local_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+    } else {
+        MPH_CUDA(cudaFuncSetAttribute(k_local_cols<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+    }
+    MPH_CUDA(cudaMemsetAsync(d.ucount + nb, 0, sizeof(int), c->stream));
+    if (c->dim == 2) {
+        k_local_cols<2><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
+    } else {
+        k_local_cols<3><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
+    }
+    MPH_COUNT_LAUNCH();
+    int umax = 0;
+    MPH_CUDA(cudaMemcpyAsync(&umax, d.ucount + nb, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    // a step's size rounded up so that small changes keep the captured graphs
+    if (umax > 0) c->loc_smem = ((umax + 511) / 512) * 512 * c->dim * (int)sizeof(float);
+    return MPH_OK;
+}
+
 int launch_pairs_to_slices(mph_case* c)
 {
     DeviceState& d = c->d;
@@ -968,7 +1154,7 @@ int launch_pairs_to_slices(mph_case* c)
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
                                                                        d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
-    return MPH_OK;
+    return launch_local_cols(c);
 }
 
 // The transposed P-lists (C in FP32) of every particle in the sliced layout

@@ -138,6 +138,15 @@ struct DeviceState {
     unsigned short* pes16 = nullptr;   // the inner operator's copy of g: FP16, scaled per slice
     long long cap_pes16 = 0;
     float* pscale = nullptr;           // per slice: g = pes16 * pscale
+    // block-local neighbour columns of the inner operator (per fluid slot the
+    // neighbour's rank among its row block's distinct neighbours; per block
+    // those neighbours, kUMax a block, and their count or -1; their maximum)
+    unsigned short* lidx16 = nullptr;
+    long long cap_lidx16 = 0;
+    int* uniq = nullptr;
+    long long cap_uniq = 0;
+    int* ucount = nullptr;
+    long long cap_ucount = 0;
     int* ccell = nullptr;              // packed cell coordinates of every particle (pair path)
     double* io3 = nullptr;             // host-layout staging, 2 x N x 3 doubles (state upload, field download)
     int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
@@ -228,6 +237,7 @@ struct mph_case {
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
     cudaEvent_t gev[16] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
+    int loc_smem = 0;                   // shared memory of the inner operator's staged neighbour x (0: gathers by column)
     bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs
