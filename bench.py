@@ -148,22 +148,31 @@ def spmv_bytes(prof, scal, dim, vb=8):
     return blocks * (dim * dim * vb + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * vb
 
 
-def pair_apply_bytes(prof, scal, dim):
+def pair_apply_bytes(prof, scal, dim, st=None):
     """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
     (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
     transposed P-list slot, entry counts and slice pointers, s gathered once,
-    t written.  k_visc_pen32: column + D FP16 values of g = sqrt(f) e per
-    fluid slot, column + D FP32 lambda C per P-slot, the 8-float diagonal /
-    inertia record, row lengths, slice pointers and scales, s read once, t
-    gathered once, y written."""
+    t written.  k_visc_pen32: a column (4 bytes; 2 bytes of block-local index
+    when the row block's neighbours are staged in shared memory, counted so
+    for every slot once any block is staged: a lower bound) + D FP16 values of
+    g = sqrt(f) e per fluid slot, column + D FP32 lambda C per P-slot, the
+    8-float diagonal / inertia record, row lengths, slice pointers and
+    scales, s read once, t gathered once, y written; a staged block also reads
+    its count and its distinct columns (4 bytes each; their s, which the block
+    copies to shared memory, count as part of s read once)."""
     nf = int(scal["FluidParticleEnd"])
     n = int(scal["ParticleCount"])
     slots = scal["NonzeroCountA"] / (dim * dim)
     pslots = scal["NonzeroCountC"] / dim
     nsl, nct = (nf + 31) // 32, (n + 31) // 32
+    st = st or {}
+    staged = st.get("inner_local_blocks", 0) > 0
+    col = 2 if staged else 4
     ct = pslots * (dim * 4 + 4) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
-    vp = slots * (dim * 2 + 4) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
+    vp = slots * (dim * 2 + col) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
         + 2 * dim * nf * 4 + n * 4
+    if staged:
+        vp += st["inner_local_cols"] * 4 + (st["inner_local_blocks"] + st["inner_gather_blocks"]) * 4
     return ct + vp
 
 
@@ -534,8 +543,9 @@ def main():
     # roofline of the dominant kernel (CUDA events on the case stream)
     peak, peak_kind = measured_peaks()
     vb = 4 if prec == PRECISION_MIXED else 8
-    pairs = case.solve_stats().get("inner_form") == 2
-    kern = {"spmv": ("k_ct_apply32+k_visc_pen32", pair_apply_bytes) if pairs else
+    st = case.solve_stats()
+    pairs = st.get("inner_form") == 2
+    kern = {"spmv": ("k_ct_apply32+k_visc_pen32", lambda p_, s_, d_: pair_apply_bytes(p_, s_, d_, st)) if pairs else
                     ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
             "assemble_a": ("k_assemble_cells", assemble_bytes)}
     dom = max(kern, key=lambda k: prof[f"kern_ms_{k}"])
@@ -581,6 +591,9 @@ def main():
                    "l2": "inputs larger than L2 (the block matrix alone exceeds 129 MB by ~100x)",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                    "cr_iterations": iters,
+                   "inner_row_blocks": {"staged": st.get("inner_local_blocks"), "gathering": st.get("inner_gather_blocks"),
+                                        "mean_distinct_cols": (st["inner_local_cols"] / st["inner_local_blocks"]
+                                                               if st.get("inner_local_blocks") else None)},
                    "stage_ms_per_step": {s: prof[f"stage_ms_{s}"] / args.steps for s in
                                          ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve")},
                    "stage_sum_ms_per_step": stage_total / args.steps,

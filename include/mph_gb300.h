@@ -102,6 +102,10 @@ typedef struct mph_solve_stats {
     int outer_iterations;    /* mixed form: FP64 refinement steps (0 for the FP64 form) */
     int inner_form;          /* operator of the CR iterations: 0 FP64 blocks, 1 FP32 blocks,
                                 2 FP32 pair terms (mixed form, factored, option inner_blocks 0) */
+    int inner_local_blocks;  /* inner_form 2: row blocks (512 fluid rows) whose neighbours' values are
+                                staged in shared memory, and the rest, which gather by column */
+    int inner_gather_blocks;
+    long long inner_local_cols;  /* distinct neighbour columns summed over the staged row blocks */
 } mph_solve_stats;
 
 typedef struct mph_case mph_case;

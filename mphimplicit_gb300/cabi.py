@@ -71,7 +71,9 @@ class MphFields(ctypes.Structure):
 class MphSolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("rr0", ctypes.c_double), ("rr", ctypes.c_double),
                 ("rs0", ctypes.c_double), ("rs", ctypes.c_double), ("status", ctypes.c_int),
-                ("outer_iterations", ctypes.c_int), ("inner_form", ctypes.c_int)]
+                ("outer_iterations", ctypes.c_int), ("inner_form", ctypes.c_int),
+                ("inner_local_blocks", ctypes.c_int), ("inner_gather_blocks", ctypes.c_int),
+                ("inner_local_cols", ctypes.c_longlong)]
 
 
 def params_to_c(p: casegen.Params) -> MphParams:

@@ -914,7 +914,10 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
     hi = -1;
     for (int w = 0; w < nwl; ++w) { lo = min(lo, red[0][w]); hi = max(hi, red[1][w]); }
     if (hi < 0) {   // no fluid neighbours in the block
-        if (tid == 0) ucount[blockIdx.x] = 0;
+        if (tid == 0) {
+            ucount[blockIdx.x] = 0;
+            atomicAdd(ucount + gridDim.x + 1, 1);
+        }
         return;
     }
     const long long span = (long long)hi - lo + 1;
@@ -975,9 +978,11 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
             word &= word - 1u;
         }
     }
-    if (tid == 0) {
+    if (tid == 0) {   // after the blocks: the largest count, the staged blocks and their columns
         ucount[blockIdx.x] = U;
         atomicMax(ucount + gridDim.x, U);
+        atomicAdd(ucount + gridDim.x + 1, 1);
+        atomicAdd((unsigned*)ucount + gridDim.x + 2, (unsigned)U);
     }
 }
 
@@ -1084,6 +1089,8 @@ static int launch_local_cols(mph_case* c)
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
     c->loc_smem = 0;
+    c->loc_blocks[0] = c->loc_blocks[1] = 0;
+    c->loc_cols = 0;
     if (P.Nf == 0) return MPH_OK;
     const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK);
     if (c->nslots > d.cap_lidx16) {
@@ -1095,8 +1102,9 @@ static int launch_local_cols(mph_case* c)
         d.cap_lidx16 = n;
     }
     MPH_TRY(grow_i(&d.uniq, &d.cap_uniq, nb * kUMax));
-    MPH_TRY(grow_i(&d.ucount, &d.cap_ucount, nb + 1));
+    MPH_TRY(grow_i(&d.ucount, &d.cap_ucount, nb + 3));
     const size_t smem = 2 * kWinWords * sizeof(unsigned);
+    const int per_col = 4 * c->dim;   // shared memory of a staged neighbour's x
     if (c->dim == 2) {
         MPH_CUDA(cudaFuncSetAttribute(k_local_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
@@ -1104,18 +1112,22 @@ static int launch_local_cols(mph_case* c)
         MPH_CUDA(cudaFuncSetAttribute(k_local_cols<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
     }
-    MPH_CUDA(cudaMemsetAsync(d.ucount + nb, 0, sizeof(int), c->stream));
+    MPH_CUDA(cudaMemsetAsync(d.ucount + nb, 0, 3 * sizeof(int), c->stream));
     if (c->dim == 2) {
         k_local_cols<2><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
     } else {
         k_local_cols<3><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
     }
     MPH_COUNT_LAUNCH();
-    int umax = 0;
-    MPH_CUDA(cudaMemcpyAsync(&umax, d.ucount + nb, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int h[3] = {};
+    MPH_CUDA(cudaMemcpyAsync(h, d.ucount + nb, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     MPH_CUDA(cudaStreamSynchronize(c->stream));
+    const int umax = h[0];
+    c->loc_blocks[0] = umax > 0 ? h[1] : 0;
+    c->loc_blocks[1] = (int)nb - c->loc_blocks[0];
+    c->loc_cols = umax > 0 ? (long long)(unsigned)h[2] : 0;
     // a step's size rounded up so that small changes keep the captured graphs
-    if (umax > 0) c->loc_smem = ((umax + 511) / 512) * 512 * c->dim * (int)sizeof(float);
+    if (umax > 0) c->loc_smem = ((umax + 511) / 512) * 512 * per_col;
     return MPH_OK;
 }
 

@@ -238,6 +238,8 @@ struct mph_case {
     cudaEvent_t gev[16] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     int loc_smem = 0;                   // shared memory of the inner operator's staged neighbour x (0: gathers by column)
+    int loc_blocks[2] = {};             // row blocks staged / gathering by column
+    long long loc_cols = 0;             // distinct neighbour columns over the staged blocks
     bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step
     bool use_graphs = true;             // replay CR iteration chunks as CUDA graphs

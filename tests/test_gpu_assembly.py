@@ -148,6 +148,12 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
         assert rel(x, y) <= 1e-6, L
     sa, sb = a.solve_stats(), b.solve_stats()
     assert (sa["inner_form"], sb["inner_form"]) == (2, 1)
+    # every row block of the pair-term operator is accounted for; compact
+    # particle orderings stage their neighbours in shared memory
+    nblk = (a.fluid_count + 511) // 512
+    assert sa["inner_local_blocks"] + sa["inner_gather_blocks"] == nblk
+    assert sa["inner_local_blocks"] > 0 and sa["inner_local_cols"] >= sa["inner_local_blocks"]
+    assert sb["inner_local_blocks"] == sb["inner_gather_blocks"] == 0
     assert abs(sa["iter"] - sb["iter"]) <= max(2, sb["iter"] // 10), (sa, sb)
     assert abs(sa["outer"] - sb["outer"]) <= 1
     nf = a.fluid_count
