@@ -686,9 +686,10 @@ __global__ void __launch_bounds__(256) k_ct_cells(int N, const long long* __rest
 // next 32 neighbours while a chunk is scanned for runs, and the W_k bins of
 // up to 32 P-neighbours at once into a per-warp stage.
 constexpr int kPartStage = 16;   // P-neighbours staged at a time
+static_assert(kPartStage * kWBins % 32 == 0 && kPartStage * 3 <= 64, "whole staging rounds");
 
 template <int D>
-__global__ void __launch_bounds__(kPairWarps * 32)
+__global__ void __launch_bounds__(kPairWarps * 32, 4)
 k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* __restrict__ ccell, const int* __restrict__ type,
              const int* __restrict__ nc,
              const int* __restrict__ nfc, const long long* __restrict__ nptr, const int* __restrict__ nind,
@@ -731,22 +732,31 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
             const int n = nc[i], nf = nfc[i];
             // runs of equal cell in the fluid part of the neighbour list
             int nrun = 0, last = -1;
-            int kjn = lane < nf ? ccell[nind[nb + lane]] : -1;
-            for (int k0 = 0; k0 < nf; k0 += 32) {
-                const int k = k0 + lane;
-                const int kj = kjn;
-                kjn = k + 32 < nf ? ccell[nind[nb + k + 32]] : -1;   // next chunk, issued ahead
-                int kp = __shfl_up_sync(full, kj, 1);
-                if (lane == 0) kp = last;
-                last = __shfl_sync(full, kj, 31);
-                const bool start = k < nf && kj != kp;
-                const unsigned bal = __ballot_sync(full, start);
-                const int at = nrun + __popc(bal & ((1u << lane) - 1u));
-                if (start && at < SMAX) {
-                    run[at] = k;
-                    rkey[at] = kj;
+            for (int c0 = 0; c0 < nf; c0 += 128) {   // four chunks of 32 slots, their loads issued together
+                int kc[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = c0 + 32 * u + lane;
+                    kc[u] = k < nf ? nind[nb + k] : -1;
                 }
-                nrun += __popc(bal);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) kc[u] = kc[u] >= 0 ? ccell[kc[u]] : -1;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = c0 + 32 * u + lane;
+                    const int kj = kc[u];
+                    int kp = __shfl_up_sync(full, kj, 1);
+                    if (lane == 0) kp = last;
+                    last = __shfl_sync(full, kj, 31);
+                    const bool start = k < nf && kj != kp;
+                    const unsigned bal = __ballot_sync(full, start);
+                    const int at = nrun + __popc(bal & ((1u << lane) - 1u));
+                    if (start && at < SMAX) {
+                        run[at] = k;
+                        rkey[at] = kj;
+                    }
+                    nrun += __popc(bal);
+                }
             }
             bool bad = nrun > SMAX;
             if (lane == 0) run[min(nrun, SMAX)] = nf;
@@ -814,22 +824,40 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
             for (int a0 = 0; a0 < np && !bad; a0 += kPartStage) {
                 const int na = min(kPartStage, np - a0);
                 bool over = false;
-                for (int t = lane; t < kPartStage * kWBins; t += 32) {   // stage the bins (slot, W) of na P-neighbours
-                    const int q = t / kWBins, b = t % kWBins;
-                    int slot = -1;
-                    if (q < na) {
-                        const int k = nindP[pb + a0 + q];
-                        const int wk = wkey[(size_t)k * kWBins + b];
-                        if (wk == -2) over = true;
-                        if (wk >= 0) {
-                            slot = slot_packed(M, pi, wk);
+                // stage the bins (slot, W) of na P-neighbours, kPer a lane: all
+                // loads of one level of the index chain issued together
+                constexpr int kPer = kPartStage * kWBins / 32;
+                int kk[kPer], wk[kPer];
+                float wv[kPer][3];
 #pragma unroll
-                            for (int d = 0; d < 3; ++d) stval[t * 3 + d] = wval[((size_t)k * kWBins + b) * 3 + d];
-                        }
-                    }
-                    stslot[t] = slot;
+                for (int u = 0; u < kPer; ++u) {
+                    const int q = (lane + 32 * u) / kWBins;
+                    kk[u] = q < na ? nindP[pb + a0 + q] : -1;
                 }
-                for (int t = lane; t < na * 3; t += 32) stcl[t] = t % 3 < D ? cvl32[(pb + a0 + t / 3) * D + t % 3] : 0.f;
+#pragma unroll
+                for (int u = 0; u < kPer; ++u) wk[u] = kk[u] >= 0 ? wkey[(size_t)kk[u] * kWBins + (lane + 32 * u) % kWBins] : -1;
+#pragma unroll
+                for (int u = 0; u < kPer; ++u)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        wv[u][d] = wk[u] >= 0 ? wval[((size_t)kk[u] * kWBins + (lane + 32 * u) % kWBins) * 3 + d] : 0.f;
+                float cl[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int t = lane + 32 * u;
+                    cl[u] = t < na * 3 && t % 3 < D ? cvl32[(pb + a0 + t / 3) * D + t % 3] : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kPer; ++u) {
+                    const int t = lane + 32 * u;
+                    if (wk[u] == -2) over = true;
+                    stslot[t] = wk[u] >= 0 ? slot_packed(M, pi, wk[u]) : -1;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) stval[t * 3 + d] = wv[u][d];
+                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+                    if (lane + 32 * u < kPartStage * 3) stcl[lane + 32 * u] = cl[u];
                 bad = __any_sync(full, over) || bad;
                 __syncwarp();
                 if (bad) break;
