@@ -77,16 +77,16 @@ __device__ __forceinline__ void load_xi32(const float* __restrict__ pos32, int i
     }
 }
 
+// The list of particle i by one thread (count pass: nc, nfc, ncp; FILL:
+// nind, nindP at nptr, nptrP).
 template <int D, bool FILL>
-__global__ void __launch_bounds__(128) k_neighbors(DevParams P, int rx, int ry, int rz, int wB, int wE,
-                                                   const int* __restrict__ key, const int* __restrict__ bucket,
-                                                   const double* __restrict__ pos, const float* __restrict__ pos32,
-                                                   int* __restrict__ nc, int* __restrict__ nfc, int* __restrict__ ncp,
-                                                   const long long* __restrict__ nptr, const long long* __restrict__ nptrP,
-                                                   int* __restrict__ nind, int* __restrict__ nindP)
+__device__ void neighbors_one(const DevParams& P, int rx, int ry, int rz, int wB, int wE,
+                              const int* __restrict__ key, const int* __restrict__ bucket,
+                              const double* __restrict__ pos, const float* __restrict__ pos32,
+                              int* __restrict__ nc, int* __restrict__ nfc, int* __restrict__ ncp,
+                              const long long* __restrict__ nptr, const long long* __restrict__ nptrP,
+                              int* __restrict__ nind, int* __restrict__ nindP, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
     const int range[3] = {rx, ry, rz};
     Walk w;
     make_walk(P, range, key[i], w);
@@ -123,6 +123,194 @@ __global__ void __launch_bounds__(128) k_neighbors(DevParams P, int rx, int ry, 
         if (pass == 0 && !FILL) nfc[i] = n;
     }
     if (!FILL) { nc[i] = n; ncp[i] = np; }
+}
+
+template <int D, bool FILL>
+__global__ void __launch_bounds__(128) k_neighbors(DevParams P, int rx, int ry, int rz, int wB, int wE,
+                                                   const int* __restrict__ key, const int* __restrict__ bucket,
+                                                   const double* __restrict__ pos, const float* __restrict__ pos32,
+                                                   int* __restrict__ nc, int* __restrict__ nfc, int* __restrict__ ncp,
+                                                   const long long* __restrict__ nptr, const long long* __restrict__ nptrP,
+                                                   int* __restrict__ nind, int* __restrict__ nindP)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    neighbors_one<D, FILL>(P, rx, ry, rz, wB, wE, key, bucket, pos, pos32, nc, nfc, ncp, nptr, nptrP, nind, nindP, i);
+}
+
+// ---- one block per cell bucket -------------------------------------------------
+// The particles of one bucket (the fluid or the wall particles of one cell)
+// share their walk: the block stages the candidates of each pass (fluid
+// buckets, then wall buckets of the 3^D cells, in the walk's order) in shared
+// memory once, and a warp takes one particle at a time, its lanes on 32
+// consecutive candidates; ballots keep the list order, so a list is the same
+// as the per-thread walk's, written with coalesced stores.  A walk that does
+// not wrap around the periodic grid (and a grid of at least 2 range + 3 cells
+// on every axis) needs no minimum-image correction in FP32.  A bucket with
+// more than kNbMaxP particles, a pass with more than kNbCap candidates, a walk
+// of more than 27 cells or the exact-only mode runs the per-thread walk.
+constexpr int kNbThreads = 256;
+constexpr int kNbCap = 1536;
+constexpr int kNbMaxP = 256;
+
+template <int D>
+__device__ __forceinline__ int classify_staged(const DevParams& P, bool wrap, const float* xi32, const float4 pj,
+                                               const double* __restrict__ pos, int i, int j)
+{
+    float a = pj.x - xi32[0], b = pj.y - xi32[1];
+    float d2;
+    if (D == 2) {
+        if (wrap) {
+            a = a > P.hw32[0] ? a - P.w32[0] : (a < -P.hw32[0] ? a + P.w32[0] : a);
+            b = b > P.hw32[1] ? b - P.w32[1] : (b < -P.hw32[1] ? b + P.w32[1] : b);
+        }
+        d2 = a * a + b * b;
+    } else {
+        float e = pj.z - xi32[2];
+        if (wrap) {
+            a = a > P.hw32[0] ? a - P.w32[0] : (a < -P.hw32[0] ? a + P.w32[0] : a);
+            b = b > P.hw32[1] ? b - P.w32[1] : (b < -P.hw32[1] ? b + P.w32[1] : b);
+            e = e > P.hw32[2] ? e - P.w32[2] : (e < -P.hw32[2] ? e + P.w32[2] : e);
+        }
+        d2 = a * a + b * b + e * e;
+    }
+    if (d2 > P.maxR2_hi) return 0;
+    const bool inM = d2 < P.maxR2_lo;
+    const bool inP = d2 < P.rP2_lo;
+    const bool outP = d2 > P.rP2_hi;
+    if (inM && (inP || outP)) return 1 | (inP ? 2 : 0);
+    double xi[3], xj[3], q[3];
+    load_vec<D>(pos, i, xi);
+    load_vec<D>(pos, j, xj);
+    sep_vec<D>(P, xj, xi, q);
+    const double r2 = norm2_exact<D>(q);
+    if (!(r2 <= P.maxR2)) return 0;
+    return 1 | (r2 <= P.rP2 ? 2 : 0);
+}
+
+template <int D, bool FILL>
+__global__ void __launch_bounds__(kNbThreads) k_neighbors_cells(DevParams P, int rx, int ry, int rz, int wB, int wE,
+                                                                const int* __restrict__ key, const int* __restrict__ bucket,
+                                                                const double* __restrict__ pos, const float* __restrict__ pos32,
+                                                                int* __restrict__ nc, int* __restrict__ nfc, int* __restrict__ ncp,
+                                                                const long long* __restrict__ nptr, const long long* __restrict__ nptrP,
+                                                                int* __restrict__ nind, int* __restrict__ nindP)
+{
+    __shared__ float4 spos[kNbCap];
+    __shared__ int sj[kNbCap];
+    __shared__ int coff[2][28];
+    __shared__ int cbeg[2][27];
+    __shared__ int sn0[kNbMaxP], snp0[kNbMaxP];
+    const int u = blockIdx.x;   // bucket = sort key: cell u (fluid) or u - T (wall)
+    const int r0 = bucket[u], r1 = bucket[u + 1];
+    if (r0 >= r1) return;
+    const int tid = threadIdx.x, lane = tid & 31, wl = tid >> 5, nw = blockDim.x >> 5;
+    const unsigned full = 0xffffffffu;
+    const int range[3] = {rx, ry, rz};
+    Walk w;
+    make_walk(P, range, u, w);
+    const int ncell = w.n[0] * w.n[1] * w.n[2];
+    bool wrap = false;
+    {
+        int ic[3];
+        key_coords(P, u, ic);
+        for (int d = 0; d < D; ++d) {
+            const int c = wrapc(ic[d], P.cc[d]);
+            wrap = wrap || c - range[d] < 0 || c + range[d] >= P.cc[d] || P.cc[d] < 2 * range[d] + 3;
+        }
+    }
+    bool slow = ncell > 27 || r1 - r0 > kNbMaxP;
+    if (!slow) {
+        if (tid < 64) {   // warp 0: the fluid buckets of the walk's cells, warp 1: the wall buckets
+            const int pass = tid >> 5;
+            int beg = 0, cnt = 0;
+            if (lane < ncell) {
+                const int a = lane / (w.n[1] * w.n[2]), b = (lane / w.n[2]) % w.n[1], z = lane % w.n[2];
+                const int jx = w.lo[0] + a, jy = w.lo[1] + b, jz = w.lo[2] + z;
+                const int jc = cell_id(P, w.cells[0][jx % w.n[0]], w.cells[1][jy % w.n[1]], w.cells[2][jz % w.n[2]]);
+                beg = bucket[pass * P.T + jc];
+                cnt = bucket[pass * P.T + jc + 1] - beg;
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane < ncell) {
+                cbeg[pass][lane] = beg;
+                coff[pass][lane + 1] = incl;
+            }
+            if (lane == 0) coff[pass][0] = 0;
+        }
+        __syncthreads();
+        slow = coff[0][ncell] > kNbCap || coff[1][ncell] > kNbCap;
+    }
+    if (slow) {   // the same for every thread of the block
+        for (int i = r0 + tid; i < r1; i += blockDim.x)
+            neighbors_one<D, FILL>(P, rx, ry, rz, wB, wE, key, bucket, pos, pos32, nc, nfc, ncp, nptr, nptrP, nind, nindP, i);
+        return;
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        const int F = coff[pass][ncell];
+        for (int t = wl; t < ncell; t += nw) {
+            const int beg = cbeg[pass][t], off = coff[pass][t], cnt = coff[pass][t + 1] - off;
+            for (int k = lane; k < cnt; k += 32) {
+                const int j = beg + k;
+                float4 pj;
+                if (D == 2) {
+                    const float2 q = reinterpret_cast<const float2*>(pos32)[j];
+                    pj = make_float4(q.x, q.y, 0.f, 0.f);
+                } else {
+                    pj = reinterpret_cast<const float4*>(pos32)[j];
+                }
+                spos[off + k] = pj;
+                sj[off + k] = j;
+            }
+        }
+        __syncthreads();
+        for (int pi = wl; pi < r1 - r0; pi += nw) {
+            const int i = r0 + pi;
+            int n = 0, np = 0;
+            if (pass == 1) {
+                n = sn0[pi];
+                np = snp0[pi];
+                if (wB <= i && i < wE && n == 0) {   // wall particle without fluid neighbours
+                    if (!FILL && lane == 0) { nc[i] = 0; ncp[i] = 0; }
+                    continue;
+                }
+            }
+            long long o = 0, op = 0;
+            if (FILL) { o = nptr[i] + n; op = nptrP[i] + np; }
+            float xi32[3] = {0.f, 0.f, 0.f};
+            load_xi32<D>(pos32, i, xi32);
+            for (int c0 = 0; c0 < F; c0 += 32) {
+                const int c = c0 + lane;
+                const int cl = c < F ? classify_staged<D>(P, wrap, xi32, spos[c], pos, i, sj[c]) : 0;
+                const unsigned bm = __ballot_sync(full, cl & 1), bp = __ballot_sync(full, (cl & 2) != 0);
+                if (FILL) {
+                    const unsigned lt = (1u << lane) - 1u;
+                    if (cl & 1) nind[o + __popc(bm & lt)] = sj[c];
+                    if (cl & 2) nindP[op + __popc(bp & lt)] = sj[c];
+                    o += __popc(bm);
+                    op += __popc(bp);
+                }
+                n += __popc(bm);
+                np += __popc(bp);
+            }
+            if (lane == 0) {
+                if (pass == 0) {
+                    sn0[pi] = n;
+                    snp0[pi] = np;
+                    if (!FILL) nfc[i] = n;
+                } else if (!FILL) {
+                    nc[i] = n;
+                    ncp[i] = np;
+                }
+            }
+        }
+        __syncthreads();   // the staged candidates are replaced; sn0 is read by the same warp
+    }
 }
 
 // ---- scan: out[0] = 0, out[k+1] = in[0] + ... + in[k] (int32 -> int64) ----
@@ -240,10 +428,29 @@ static void neighbor_ranges(const mph_case* c, int* r)
     }
 }
 
+// one block per bucket (2 T of them), or the per-thread walk in the exact-only mode
+template <bool FILL>
+static void launch_neighbors_cells(mph_case* c, const int* r)
+{
+    const unsigned g = (unsigned)(2 * c->dp.T);
+    DeviceState& d = c->d;
+    if (c->dim == 2)
+        k_neighbors_cells<2, FILL><<<g, kNbThreads, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, d.key, d.bucket, d.pos, d.pos32,
+                                                                    d.nc, d.nfc, d.ncp, d.nptr, d.nptrP, d.nind, d.nindP);
+    else
+        k_neighbors_cells<3, FILL><<<g, kNbThreads, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, d.key, d.bucket, d.pos, d.pos32,
+                                                                    d.nc, d.nfc, d.ncp, d.nptr, d.nptrP, d.nind, d.nindP);
+    MPH_COUNT_LAUNCH();
+}
+
 void launch_neighbor_count(mph_case* c)
 {
     int r[3];
     neighbor_ranges(c, r);
+    if (!c->dp.exact_only && c->dp.T > 0) {
+        launch_neighbors_cells<false>(c, r);
+        return;
+    }
     const unsigned g = grid_for(c->dp.N, 128);
     if (c->dim == 2)
         { k_neighbors<2, false><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
@@ -257,6 +464,10 @@ void launch_neighbor_fill(mph_case* c)
 {
     int r[3];
     neighbor_ranges(c, r);
+    if (!c->dp.exact_only && c->dp.T > 0) {
+        launch_neighbors_cells<true>(c, r);
+        return;
+    }
     const unsigned g = grid_for(c->dp.N, 128);
     if (c->dim == 2)
         { k_neighbors<2, true><<<g, 128, 0, c->stream>>>(c->dp, r[0], r[1], r[2], c->wB, c->wE, c->d.key, c->d.bucket, c->d.pos,
