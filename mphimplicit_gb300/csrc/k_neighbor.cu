@@ -153,32 +153,32 @@ constexpr int kNbThreads = 256;
 constexpr int kNbCap = 1536;
 constexpr int kNbMaxP = 256;
 
+// The FP32 squared distance of a staged candidate (the minimum image only
+// for a walk that wraps), as classify computes it.
 template <int D>
-__device__ __forceinline__ int classify_staged(const DevParams& P, bool wrap, const float* xi32, const float4 pj,
-                                               const double* __restrict__ pos, int i, int j)
+__device__ __forceinline__ float d2_staged(const DevParams& P, bool wrap, const float* xi32, const float4 pj)
 {
     float a = pj.x - xi32[0], b = pj.y - xi32[1];
-    float d2;
     if (D == 2) {
         if (wrap) {
             a = a > P.hw32[0] ? a - P.w32[0] : (a < -P.hw32[0] ? a + P.w32[0] : a);
             b = b > P.hw32[1] ? b - P.w32[1] : (b < -P.hw32[1] ? b + P.w32[1] : b);
         }
-        d2 = a * a + b * b;
-    } else {
-        float e = pj.z - xi32[2];
-        if (wrap) {
-            a = a > P.hw32[0] ? a - P.w32[0] : (a < -P.hw32[0] ? a + P.w32[0] : a);
-            b = b > P.hw32[1] ? b - P.w32[1] : (b < -P.hw32[1] ? b + P.w32[1] : b);
-            e = e > P.hw32[2] ? e - P.w32[2] : (e < -P.hw32[2] ? e + P.w32[2] : e);
-        }
-        d2 = a * a + b * b + e * e;
+        return a * a + b * b;
     }
-    if (d2 > P.maxR2_hi) return 0;
-    const bool inM = d2 < P.maxR2_lo;
-    const bool inP = d2 < P.rP2_lo;
-    const bool outP = d2 > P.rP2_hi;
-    if (inM && (inP || outP)) return 1 | (inP ? 2 : 0);
+    float e = pj.z - xi32[2];
+    if (wrap) {
+        a = a > P.hw32[0] ? a - P.w32[0] : (a < -P.hw32[0] ? a + P.w32[0] : a);
+        b = b > P.hw32[1] ? b - P.w32[1] : (b < -P.hw32[1] ? b + P.w32[1] : b);
+        e = e > P.hw32[2] ? e - P.w32[2] : (e < -P.hw32[2] ? e + P.w32[2] : e);
+    }
+    return a * a + b * b + e * e;
+}
+
+// The reference's FP64 decision for a pair inside the FP32 band.
+template <int D>
+__device__ __forceinline__ int classify_exact(const DevParams& P, const double* __restrict__ pos, int i, int j)
+{
     double xi[3], xj[3], q[3];
     load_vec<D>(pos, i, xi);
     load_vec<D>(pos, j, xj);
@@ -253,6 +253,11 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbors_cells(DevParams P, int
     }
     for (int pass = 0; pass < 2; ++pass) {
         const int F = coff[pass][ncell];
+        // candidates F.. up to a multiple of 32: far away, never neighbours
+        for (int k = F + tid; k < ((F + 31) & ~31); k += blockDim.x) {
+            spos[k] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+            sj[k] = -1;
+        }
         for (int t = wl; t < ncell; t += nw) {
             const int beg = cbeg[pass][t], off = coff[pass][t], cnt = coff[pass][t + 1] - off;
             for (int k = lane; k < cnt; k += 32) {
@@ -280,20 +285,34 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbors_cells(DevParams P, int
                     continue;
                 }
             }
-            long long o = 0, op = 0;
-            if (FILL) { o = nptr[i] + n; op = nptrP[i] + np; }
+            int* outM = nullptr;
+            int* outP = nullptr;
+            if (FILL) { outM = nind + nptr[i]; outP = nindP + nptrP[i]; }
             float xi32[3] = {0.f, 0.f, 0.f};
             load_xi32<D>(pos32, i, xi32);
+            const unsigned lt = (1u << lane) - 1u;
             for (int c0 = 0; c0 < F; c0 += 32) {
                 const int c = c0 + lane;
-                const int cl = c < F ? classify_staged<D>(P, wrap, xi32, spos[c], pos, i, sj[c]) : 0;
-                const unsigned bm = __ballot_sync(full, cl & 1), bp = __ballot_sync(full, (cl & 2) != 0);
+                // FP32 first: far (> the band above MaxRadius^2), or inside
+                // MaxRadius and clear of the RadiusP band; the rest exactly
+                const float d2 = d2_staged<D>(P, wrap, xi32, spos[c]);
+                const bool inM = d2 < P.maxR2_lo, inP = d2 < P.rP2_lo;
+                const bool sure = d2 > P.maxR2_hi || (inM && (inP || d2 > P.rP2_hi));
+                bool m = sure && inM, pp = sure && inP;
+                if (__any_sync(full, !sure)) {
+                    if (!sure) {
+                        const int cl = classify_exact<D>(P, pos, i, sj[c]);
+                        m = cl & 1;
+                        pp = (cl & 2) != 0;
+                    }
+                }
+                const unsigned bm = __ballot_sync(full, m), bp = __ballot_sync(full, pp);
                 if (FILL) {
-                    const unsigned lt = (1u << lane) - 1u;
-                    if (cl & 1) nind[o + __popc(bm & lt)] = sj[c];
-                    if (cl & 2) nindP[op + __popc(bp & lt)] = sj[c];
-                    o += __popc(bm);
-                    op += __popc(bp);
+                    if (bm) {
+                        const int j = sj[c];
+                        if (m) outM[n + __popc(bm & lt)] = j;
+                        if (pp) outP[np + __popc(bp & lt)] = j;
+                    }
                 }
                 n += __popc(bm);
                 np += __popc(bp);
