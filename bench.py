@@ -152,10 +152,11 @@ def pair_apply_bytes(prof, scal, dim, st=None):
     """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
     (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
     transposed P-list slot, entry counts and slice pointers, s gathered once,
-    t written.  k_visc_pen32: a column (4 bytes; 2 bytes of block-local index
-    when the row block's neighbours are staged in shared memory, counted so
-    for every slot once any block is staged: a lower bound) + D FP16 values of
-    g = sqrt(f) e per fluid slot, column + D FP32 lambda C per P-slot, the
+    t written.  k_visc_pen32: an 8-byte record per fluid slot (g = sqrt(f) e
+    in FP16 and the neighbour's block-local index) and, unless the row
+    block's neighbours are staged in shared memory, a 4-byte column (counted
+    for no slot once any block is staged: a lower bound), column + D FP32
+    lambda C per P-slot, the
     8-float diagonal / inertia record, row lengths, slice pointers and
     scales, s read once, t gathered once, y written; a staged block also reads
     its count and its distinct columns (4 bytes each; their s, which the block
@@ -167,9 +168,9 @@ def pair_apply_bytes(prof, scal, dim, st=None):
     nsl, nct = (nf + 31) // 32, (n + 31) // 32
     st = st or {}
     staged = st.get("inner_local_blocks", 0) > 0
-    col = 2 if staged else 4
+    col = 0 if staged else 4
     ct = pslots * (dim * 4 + 4) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
-    vp = slots * (dim * 2 + col) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
+    vp = slots * (8 + col) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
         + 2 * dim * nf * 4 + n * 4
     if staged:
         vp += st["inner_local_cols"] * 4 + (st["inner_local_blocks"] + st["inner_gather_blocks"]) * 4

@@ -343,14 +343,15 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
 
 // The viscous part of row i in FP32 from the sliced pair terms:
 // yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)), with g from the FP32
-// slices (pes32) or from the FP16 slices times the slice scale (HALF).
+// slices (pes32) or (HALF) from the slot records: 8 bytes a fluid slot, in
+// the slot order of the sliced layout, g in FP16 (scaled per slice) in the
+// first D halves and the neighbour's block-local index in the fourth.
 template <int D, bool HALF, bool LOC = false>
 __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, const float* __restrict__ sdiag,
                                            const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                            const int* __restrict__ acol, const float* __restrict__ pes,
-                                           const unsigned short* __restrict__ pes16, const float* __restrict__ pscale,
-                                           const float* __restrict__ x, float* yv,
-                                           const unsigned short* __restrict__ lidx = nullptr, const float* xs = nullptr)
+                                           const unsigned short* __restrict__ grec, const float* __restrict__ pscale,
+                                           const float* __restrict__ x, float* yv, const float* xs = nullptr)
 {
     const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
     const float4 s1 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8 + 4);
@@ -359,20 +360,26 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
     const long long base = sptr[i >> 5];
     const int* cp = acol + base + lane;
-    const unsigned short* lp = lidx + base + lane;
+    const uint2* rp = reinterpret_cast<const uint2*>(grec) + base + lane;
     const long long vo = base * D + lane;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
 #pragma unroll (kPairUnroll)
     for (int k = 0; k < n; ++k) {
-        // LOC: the neighbour's x from the block's shared-memory copy, by its
-        // block-local index; else the global gather by column
-        const float* xj = LOC ? xs + (size_t)__ldcs(lp + (long long)k * 32) * D : x + (size_t)__ldcs(cp + (long long)k * 32) * D;
         float g[3] = {0.f, 0.f, 0.f};
+        const float* xj;
+        if (HALF) {
+            const uint2 r = __ldcs(rp + (long long)k * 32);
+            g[0] = __half2float(__ushort_as_half((unsigned short)(r.x & 0xffffu)));
+            g[1] = __half2float(__ushort_as_half((unsigned short)(r.x >> 16)));
+            if (D == 3) g[2] = __half2float(__ushort_as_half((unsigned short)(r.y & 0xffffu)));
+            // LOC: the neighbour's x from the block's shared-memory copy, by
+            // its block-local index; else the global gather by column
+            xj = LOC ? xs + (size_t)(r.y >> 16) * D : x + (size_t)__ldcs(cp + (long long)k * 32) * D;
+        } else {
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const long long o = vo + ((long long)k * D + d) * 32;
-            g[d] = HALF ? __half2float(__ushort_as_half(__ldcs(pes16 + o))) : __ldcs(pes + o);
+            for (int d = 0; d < D; ++d) g[d] = __ldcs(pes + vo + ((long long)k * D + d) * 32);
+            xj = x + (size_t)__ldcs(cp + (long long)k * 32) * D;
         }
         float gx = 0.f;
 #pragma unroll
@@ -388,11 +395,11 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
 template <int D, bool LOC>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
-             const unsigned short* __restrict__ pes16, const float* __restrict__ pscale, const float* __restrict__ sdiag,
+             const unsigned short* __restrict__ grec, const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
              const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
-             const unsigned short* __restrict__ lidx, const int* __restrict__ uniq, const int* __restrict__ ucount)
+             const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
     extern __shared__ float xs_loc[];   // LOC: x of the block's neighbours, by block-local index
     if (flags[kFlagDone]) return;
@@ -418,8 +425,8 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
         float yv[3];
-        if (LOC && U >= 0) visc_row32<D, true, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv, lidx, xs_loc);
-        else visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, pes16, pscale, x, yv);
+        if (LOC && U >= 0) visc_row32<D, true, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, grec, pscale, x, yv, xs_loc);
+        else visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, grec, pscale, x, yv);
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
@@ -450,7 +457,8 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 // slice-wise (coalesced), padding slots as zeros.  PAIRS: the values are the
 // pair terms (e, f), stored as g = sqrt(f) e in FP32 and, for the inner
 // operator, in FP16 scaled per slice (g / sigma, sigma = the slice's largest
-// |g| component / 2^15: relative rounding 2^-11, no overflow).
+// |g| component / 2^15: relative rounding 2^-11, no overflow) into the first
+// D halves of the slot records (4 halves a slot).
 constexpr int kLtsK = 32;
 
 template <int D, bool PAIRS>
@@ -509,9 +517,16 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
         __syncthreads();
         for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
             const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
-            const float v = tile[ln * W + ec];
-            sval[sb * D + (long long)k0 * D * 32 + o] = v;
-            if (PAIRS) sval16[sb * D + (long long)k0 * D * 32 + o] = __half_as_ushort(__float2half_rn(v * inv16));
+            sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+        }
+        if (PAIRS) {   // whole slot records (the index half is written later)
+            for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+                const int ln = o & 31, kl = o >> 5;
+                unsigned h[3] = {0u, 0u, 0u};
+#pragma unroll
+                for (int d = 0; d < D; ++d) h[d] = __half_as_ushort(__float2half_rn(tile[ln * W + kl * D + d] * inv16));
+                reinterpret_cast<uint2*>(sval16)[sb + (long long)(k0 + kl) * 32 + ln] = make_uint2(h[0] | (h[1] << 16), h[2]);
+            }
         }
         for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
             const int ln = o & 31, kl = o >> 5;
@@ -572,20 +587,20 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     if (c->dim == 2) {
         { k_ct_apply32<2><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
         if (c->loc_smem)
-            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.lidx16, d.uniq, d.ucount);
+            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
-            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr, nullptr);
+            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     } else {
         { k_ct_apply32<3><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
         if (c->loc_smem)
-            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.lidx16, d.uniq, d.ucount);
+            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
-            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.pes16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr, nullptr);
+            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
+                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     }
 }
@@ -905,13 +920,13 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
 
 // Block-local columns: for block b of MPH_PAIR_BLOCK rows (thread = row), the
 // sorted distinct fluid neighbours uniq[b][0..U) and, per fluid slot, the
-// neighbour's rank among them (16 bits).  A bitmap over the block's index
+// neighbour's rank among them (the fourth half of the slot record).  A bitmap over the block's index
 // window [lo, hi] marks the neighbours; word ranks come from a block scan of
 // the word popcounts.  ucount[b] = U, or -1 when the window is wider than
 // kWinWords * 32 or U > kUMax (the operator then gathers by column).
 template <int D>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const long long* __restrict__ sptr, const int* __restrict__ nfc,
-                                                             const int* __restrict__ acol, unsigned short* __restrict__ lidx,
+                                                             const int* __restrict__ acol, unsigned short* __restrict__ grec,
                                                              int* __restrict__ uniq, int* __restrict__ ucount)
 {
     extern __shared__ unsigned lc_smem[];
@@ -994,7 +1009,7 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
         const long long e = base + (long long)k * 32;
         const int off = acol[e] - lo;
         const unsigned word = bm[off >> 5];
-        lidx[e] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
+        grec[e * 4 + 3] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
     }
     int* ul = uniq + (size_t)blockIdx.x * kUMax;
     for (int w = w0; w < w1; ++w) {
@@ -1121,14 +1136,6 @@ static int launch_local_cols(mph_case* c)
     c->loc_cols = 0;
     if (P.Nf == 0) return MPH_OK;
     const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK);
-    if (c->nslots > d.cap_lidx16) {
-        if (d.lidx16) cudaFree(d.lidx16);
-        d.lidx16 = nullptr;
-        d.cap_lidx16 = 0;
-        const long long n = c->nslots + c->nslots / 8 + 1024;
-        MPH_CUDA(cudaMalloc((void**)&d.lidx16, (size_t)n * sizeof(unsigned short)));
-        d.cap_lidx16 = n;
-    }
     MPH_TRY(grow_i(&d.uniq, &d.cap_uniq, nb * kUMax));
     MPH_TRY(grow_i(&d.ucount, &d.cap_ucount, nb + 3));
     const size_t smem = 2 * kWinWords * sizeof(unsigned);
@@ -1142,9 +1149,9 @@ static int launch_local_cols(mph_case* c)
     }
     MPH_CUDA(cudaMemsetAsync(d.ucount + nb, 0, 3 * sizeof(int), c->stream));
     if (c->dim == 2) {
-        k_local_cols<2><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
+        k_local_cols<2><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.grec16, d.uniq, d.ucount);
     } else {
-        k_local_cols<3><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.lidx16, d.uniq, d.ucount);
+        k_local_cols<3><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.grec16, d.uniq, d.ucount);
     }
     MPH_COUNT_LAUNCH();
     int h[3] = {};
@@ -1166,13 +1173,13 @@ int launch_pairs_to_slices(mph_case* c)
     const int D = c->dim;
     if (c->nslices == 0) return MPH_OK;
     MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
-    if (c->nslots * D > d.cap_pes16) {
-        if (d.pes16) cudaFree(d.pes16);
-        d.pes16 = nullptr;
-        d.cap_pes16 = 0;
-        const long long n = c->nslots * D + c->nslots * D / 8 + 1024;
-        MPH_CUDA(cudaMalloc((void**)&d.pes16, (size_t)n * sizeof(unsigned short)));
-        d.cap_pes16 = n;
+    if (c->nslots * 4 > d.cap_grec16) {   // slot records, 4 halves a slot
+        if (d.grec16) cudaFree(d.grec16);
+        d.grec16 = nullptr;
+        d.cap_grec16 = 0;
+        const long long n = c->nslots * 4 + c->nslots / 2 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.grec16, (size_t)n * sizeof(unsigned short)));
+        d.cap_grec16 = n;
     }
     if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)(c->nslices + 1) * sizeof(float)));
     if (!d.psptr) {
@@ -1185,12 +1192,12 @@ int launch_pairs_to_slices(mph_case* c)
     MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * D));
     if (D == 2) {
         { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, d.pes16, d.pscale); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
                                                                        d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, d.pes16, d.pscale); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
                                                                        d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }

@@ -63,9 +63,9 @@ int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, i
         // default options, factored operator, inner operator on pair terms:
         // no blocks; pair terms, their sliced FP32 / FP16 copies, sliced
         // P-lists and transposed P-lists, level-0 cell bins
-        b += (double)Nf * nb * 16.0 + blocks * D * 6.0;
+        b += (double)Nf * nb * 16.0 + blocks * (D * 4.0 + 8.0);
         b += (double)Nf * np * (D * 4.0 + 4.0) * 2.2 + (double)N * (8.0 * 16.0 + 8.0) + (double)Nf * 32.0;
-        b += blocks * 2.0 + (double)Nf * 17.0 * 4.0;         // block-local neighbour columns
+        b += (double)Nf * 17.0 * 4.0;                         // block-local neighbour columns
     } else {
         b += blocks * DD * 8.0;                               // FP64 blocks
         if (precision == MPH_PRECISION_MIXED) {

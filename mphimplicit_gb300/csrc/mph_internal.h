@@ -135,14 +135,12 @@ struct DeviceState {
     // columns, D FP32 values a slot
     float* pes32 = nullptr;
     long long cap_pes32 = 0;
-    unsigned short* pes16 = nullptr;   // the inner operator's copy of g: FP16, scaled per slice
-    long long cap_pes16 = 0;
-    float* pscale = nullptr;           // per slice: g = pes16 * pscale
-    // block-local neighbour columns of the inner operator (per fluid slot the
-    // neighbour's rank among its row block's distinct neighbours; per block
-    // those neighbours, kUMax a block, and their count or -1; their maximum)
-    unsigned short* lidx16 = nullptr;
-    long long cap_lidx16 = 0;
+    unsigned short* grec16 = nullptr;  // inner operator slot records: g in FP16 scaled per slice (D halves), block-local index (4th)
+    long long cap_grec16 = 0;
+    float* pscale = nullptr;           // per slice: g = FP16 g * pscale
+    // block-local neighbour columns of the inner operator (per block its
+    // distinct neighbours, kUMax a block, and their count or -1; their
+    // maximum, the staged blocks and their columns after the blocks)
     int* uniq = nullptr;
     long long cap_uniq = 0;
     int* ucount = nullptr;
