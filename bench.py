@@ -169,8 +169,13 @@ def pair_apply_bytes(prof, scal, dim, st=None):
     st = st or {}
     staged = st.get("inner_local_blocks", 0) > 0
     col = 0 if staged else 4
-    ct = pslots * (dim * 4 + 4) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
-    vp = slots * (8 + col) + pslots * (dim * 4 + 4) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
+    # transposed slots of particle blocks that stage s read a 2-byte rank
+    # instead of the 4-byte column: counted so for every slot once any block
+    # stages (a lower bound)
+    pcol = 4
+    ctcol = 2 if st.get("inner_ct_local_blocks", 0) > 0 else 4
+    ct = pslots * (dim * 4 + ctcol) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
+    vp = slots * (8 + col) + pslots * (dim * 4 + pcol) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
         + 2 * dim * nf * 4 + n * 4
     if staged:
         vp += st["inner_local_cols"] * 4 + (st["inner_local_blocks"] + st["inner_gather_blocks"]) * 4
@@ -593,6 +598,7 @@ def main():
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                    "cr_iterations": iters,
                    "inner_row_blocks": {"staged": st.get("inner_local_blocks"), "gathering": st.get("inner_gather_blocks"),
+                                        "ct_blocks_staging_s": st.get("inner_ct_local_blocks"),
                                         "mean_distinct_cols": (st["inner_local_cols"] / st["inner_local_blocks"]
                                                                if st.get("inner_local_blocks") else None)},
                    "stage_ms_per_step": {s: prof[f"stage_ms_{s}"] / args.steps for s in

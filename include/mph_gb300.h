@@ -106,6 +106,8 @@ typedef struct mph_solve_stats {
                                 staged in shared memory, and the rest, which gather by column */
     int inner_gather_blocks;
     long long inner_local_cols;  /* distinct neighbour columns summed over the staged row blocks */
+    int inner_ct_local_blocks;   /* particle blocks (256) of the transposed P-list apply staging s */
+    int inner_reserved;          /* 0 */
 } mph_solve_stats;
 
 typedef struct mph_case mph_case;

@@ -73,7 +73,8 @@ class MphSolveStats(ctypes.Structure):
                 ("rs0", ctypes.c_double), ("rs", ctypes.c_double), ("status", ctypes.c_int),
                 ("outer_iterations", ctypes.c_int), ("inner_form", ctypes.c_int),
                 ("inner_local_blocks", ctypes.c_int), ("inner_gather_blocks", ctypes.c_int),
-                ("inner_local_cols", ctypes.c_longlong)]
+                ("inner_local_cols", ctypes.c_longlong), ("inner_ct_local_blocks", ctypes.c_int),
+                ("inner_reserved", ctypes.c_int)]
 
 
 def params_to_c(p: casegen.Params) -> MphParams:

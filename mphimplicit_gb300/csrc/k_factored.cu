@@ -59,9 +59,10 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 // Block-local neighbour columns of the inner operator: the fluid neighbours
 // of a block of MPH_PAIR_BLOCK rows, sorted and deduplicated, at most kUMax
 // of them (their x then fits the block's shared memory), found through a
-// bitmap of an index window of at most kWinWords * 32 particles.
+// bitmap of an index window of at most kWinWords * 32 particles (2^18: two
+// planes of neighbour cells of a 10^6-particle fluid body fit).
 constexpr int kUMax = 8192;
-constexpr int kWinWords = 1 << 14;
+constexpr int kWinWords = 1 << 13;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
@@ -305,12 +306,18 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 
-template <int D>
+// LOC: a block of MPH_CT_BLOCK particles whose transposed lists hold
+// ucount[b] >= 0 distinct fluid rows stages their s in shared memory and
+// reads each slot's 16-bit rank among them instead of its column.
+template <int D, bool LOC>
 __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
                                                     const int* __restrict__ ctscol, const float* __restrict__ ctsval,
                                                     const float* __restrict__ x, float* __restrict__ t,
-                                                    const double* __restrict__ scal, int* __restrict__ flags, int cap)
+                                                    const double* __restrict__ scal, int* __restrict__ flags, int cap,
+                                                    const unsigned short* __restrict__ lidx, const int* __restrict__ uniq,
+                                                    const int* __restrict__ ucount)
 {
+    extern __shared__ float xs_ct[];
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const double tol2 = scal[kSTol2];
@@ -325,18 +332,41 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
         return;
     }
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int U = -1;
+    if (LOC) {   // block-uniform
+        U = ucount[blockIdx.x];
+        if (U >= 0) {
+            const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+            for (int a = threadIdx.x; a < U; a += blockDim.x) {
+                const int j = ul[a];
+#pragma unroll
+                for (int d = 0; d < D; ++d) xs_ct[a * D + d] = x[(size_t)j * D + d];
+            }
+            __syncthreads();
+        }
+    }
     if (k >= N) return;
     const int lane = k & 31;
     const long long base = ctsptr[k >> 5];
-    const int* cp = ctscol + base + lane;
     const float* vp = ctsval + base * D + lane;
     float s = 0.f;
     const int n = ctcnt[k];
+    if (LOC && U >= 0) {
+        const unsigned short* lp = lidx + base + lane;
 #pragma unroll 4
-    for (int e = 0; e < n; ++e) {
-        const int j = __ldcs(cp + (long long)e * 32);
+        for (int e = 0; e < n; ++e) {
+            const float* xj = xs_ct + (int)__ldcs(lp + (long long)e * 32) * D;
 #pragma unroll
-        for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * x[(size_t)j * D + d];
+            for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * xj[d];
+        }
+    } else {
+        const int* cp = ctscol + base + lane;
+#pragma unroll 4
+        for (int e = 0; e < n; ++e) {
+            const int j = __ldcs(cp + (long long)e * 32);
+#pragma unroll
+            for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * x[(size_t)j * D + d];
+        }
     }
     t[k] = s;
 }
@@ -401,12 +431,12 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
              const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
-    extern __shared__ float xs_loc[];   // LOC: x of the block's neighbours, by block-local index
+    extern __shared__ float xs_loc[];   // LOC: s of the block's distinct fluid neighbours, by block-local index
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int U = -1;
-    if (LOC) {   // stage x of the block's distinct neighbours once (block-uniform)
+    if (LOC) {   // stage s of the block's distinct neighbours once (block-uniform)
         U = ucount[blockIdx.x];
         if (U >= 0) {
             const int* ul = uniq + (size_t)blockIdx.x * kUMax;
@@ -585,22 +615,34 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     const unsigned gt = grid_for(P.N, MPH_CT_BLOCK);
     const unsigned gv = grid_for(P.Nf, MPH_PAIR_BLOCK);
     if (c->dim == 2) {
-        { k_ct_apply32<2><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        if (c->loc_smem)
-            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        if (c->loc_ct_smem)
+            k_ct_apply32<2, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal,
+                                                                                d.flags, cap, d.ctlidx16, d.ctuniq, d.ctucount);
         else
-            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+            k_ct_apply32<2, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags,
+                                                                     cap, nullptr, nullptr, nullptr);
+        MPH_COUNT_LAUNCH();
+        if (c->loc_smem)
+            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        else
+            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     } else {
-        { k_ct_apply32<3><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags, cap); MPH_COUNT_LAUNCH(); }
-        if (c->loc_smem)
-            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        if (c->loc_ct_smem)
+            k_ct_apply32<3, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal,
+                                                                                d.flags, cap, d.ctlidx16, d.ctuniq, d.ctucount);
         else
-            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp, d.psptr,
-                d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+            k_ct_apply32<3, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags,
+                                                                     cap, nullptr, nullptr, nullptr);
+        MPH_COUNT_LAUNCH();
+        if (c->loc_smem)
+            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        else
+            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     }
 }
@@ -918,15 +960,17 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
     }
 }
 
-// Block-local columns: for block b of MPH_PAIR_BLOCK rows (thread = row), the
-// sorted distinct fluid neighbours uniq[b][0..U) and, per fluid slot, the
-// neighbour's rank among them (the fourth half of the slot record).  A bitmap over the block's index
+// Block-local columns of a sliced list: for block b of blockDim rows (thread
+// = row), the sorted distinct columns uniq[b][0..U) and, per slot e, the
+// column's rank among them at out16[e * OS + OO] (the fourth half of the
+// fluid slot records; a plain 16-bit array for the P-lists and transposed
+// P-lists).  A bitmap over the block's index
 // window [lo, hi] marks the neighbours; word ranks come from a block scan of
 // the word popcounts.  ucount[b] = U, or -1 when the window is wider than
 // kWinWords * 32 or U > kUMax (the operator then gathers by column).
-template <int D>
+template <int OS, int OO>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const long long* __restrict__ sptr, const int* __restrict__ nfc,
-                                                             const int* __restrict__ acol, unsigned short* __restrict__ grec,
+                                                             const int* __restrict__ acol, unsigned short* __restrict__ out16,
                                                              int* __restrict__ uniq, int* __restrict__ ucount)
 {
     extern __shared__ unsigned lc_smem[];
@@ -1009,7 +1053,7 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
         const long long e = base + (long long)k * 32;
         const int off = acol[e] - lo;
         const unsigned word = bm[off >> 5];
-        grec[e * 4 + 3] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
+        out16[e * OS + OO] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
     }
     int* ul = uniq + (size_t)blockIdx.x * kUMax;
     for (int w = w0; w < w1; ++w) {
@@ -1124,45 +1168,78 @@ int launch_pair_terms(mph_case* c)
 
 // The sliced pair terms g = sqrt(f) e with the block columns, and the sliced
 // lambda-scaled P-lists, of the fluid rows (after k_pair_terms).
-// Block-local neighbour columns of the inner operator (after the fluid
-// columns are sliced) and the shared memory its staged copy of x needs: the
-// largest block's distinct neighbours (read back; 0 when no block fits).
+// Block-local columns of one sliced list (rows in blocks of `block`), their
+// counts and statistics after the blocks (read back with the other lists').
+template <int OS, int OO>
+static int local_cols(mph_case* c, int rows, int block, const long long* sptr, const int* cnt, const int* cols,
+                      unsigned short* out16, int** uniq, long long* cap_uniq, int** ucount, long long* cap_ucount)
+{
+    const long long nb = grid_for(rows, block);
+    MPH_TRY(grow_i(uniq, cap_uniq, nb * kUMax));
+    MPH_TRY(grow_i(ucount, cap_ucount, nb + 3));
+    const size_t smem = 2 * kWinWords * sizeof(unsigned);
+    MPH_CUDA(cudaFuncSetAttribute(k_local_cols<OS, OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MPH_CUDA(cudaMemsetAsync(*ucount + nb, 0, 3 * sizeof(int), c->stream));
+    k_local_cols<OS, OO><<<(unsigned)nb, block, smem, c->stream>>>(rows, sptr, cnt, cols, out16, *uniq, *ucount);
+    MPH_COUNT_LAUNCH();
+    return MPH_OK;
+}
+
+// a step's count rounded up so that small changes keep the captured graphs
+static int round_cols(int umax) { return umax > 0 ? (umax + 511) / 512 * 512 : 0; }
+
+// Block-local columns of the inner operator's lists (after the slicing):
+// the fluid neighbours of each 512-row block (their s, staged by
+// k_visc_pen32) and the fluid rows of the transposed P-lists of each block of
+// k_ct_apply32 (their s).  The largest counts set the operators' shared
+// memory (0: gather by column).  Staging t for the P-lists the same way
+// measured no faster.
 static int launch_local_cols(mph_case* c)
 {
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
-    c->loc_smem = 0;
+    c->loc_smem = c->loc_ct_smem = 0;
     c->loc_blocks[0] = c->loc_blocks[1] = 0;
+    c->loc_ct_blocks = 0;
     c->loc_cols = 0;
     if (P.Nf == 0) return MPH_OK;
-    const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK);
-    MPH_TRY(grow_i(&d.uniq, &d.cap_uniq, nb * kUMax));
-    MPH_TRY(grow_i(&d.ucount, &d.cap_ucount, nb + 3));
-    const size_t smem = 2 * kWinWords * sizeof(unsigned);
-    const int per_col = 4 * c->dim;   // shared memory of a staged neighbour's x
-    if (c->dim == 2) {
-        MPH_CUDA(cudaFuncSetAttribute(k_local_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
-    } else {
-        MPH_CUDA(cudaFuncSetAttribute(k_local_cols<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
-    }
-    MPH_CUDA(cudaMemsetAsync(d.ucount + nb, 0, 3 * sizeof(int), c->stream));
-    if (c->dim == 2) {
-        k_local_cols<2><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.grec16, d.uniq, d.ucount);
-    } else {
-        k_local_cols<3><<<(unsigned)nb, MPH_PAIR_BLOCK, smem, c->stream>>>(P.Nf, d.sptr, d.nfc, d.acol, d.grec16, d.uniq, d.ucount);
-    }
-    MPH_COUNT_LAUNCH();
-    int h[3] = {};
-    MPH_CUDA(cudaMemcpyAsync(h, d.ucount + nb, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    const int D = c->dim;
+    const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK), nbc = grid_for(P.N, MPH_CT_BLOCK);
+    long long ctslots = 0;
+    MPH_CUDA(cudaMemcpyAsync(&ctslots, d.ctsptr + (P.N + 31) / 32, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     MPH_CUDA(cudaStreamSynchronize(c->stream));
-    const int umax = h[0];
-    c->loc_blocks[0] = umax > 0 ? h[1] : 0;
+    auto grow16 = [](unsigned short** p, long long* cap, long long need) -> int {
+        if (need <= *cap) return MPH_OK;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        *cap = 0;
+        const long long n = need + need / 8 + 1024;
+        MPH_CUDA(cudaMalloc((void**)p, (size_t)n * sizeof(unsigned short)));
+        *cap = n;
+        return MPH_OK;
+    };
+    MPH_TRY(grow16(&d.ctlidx16, &d.cap_ctlidx16, ctslots));
+    MPH_TRY((local_cols<4, 3>(c, P.Nf, MPH_PAIR_BLOCK, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq, &d.ucount, &d.cap_ucount)));
+    MPH_TRY((local_cols<1, 0>(c, P.N, MPH_CT_BLOCK, d.ctsptr, d.ct_cnt, d.ctscol, d.ctlidx16, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
+                              &d.cap_ctucount)));
+    int h[2][3] = {};
+    MPH_CUDA(cudaMemcpyAsync(h[0], d.ucount + nb, sizeof(h[0]), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaMemcpyAsync(h[1], d.ctucount + nbc, sizeof(h[1]), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    const int xcap = round_cols(h[0][0]), ctcap = round_cols(h[1][0]);
+    c->loc_blocks[0] = xcap ? h[0][1] : 0;
     c->loc_blocks[1] = (int)nb - c->loc_blocks[0];
-    c->loc_cols = umax > 0 ? (long long)(unsigned)h[2] : 0;
-    // a step's size rounded up so that small changes keep the captured graphs
-    if (umax > 0) c->loc_smem = ((umax + 511) / 512) * 512 * per_col;
+    c->loc_cols = xcap ? (long long)(unsigned)h[0][2] : 0;
+    c->loc_ct_blocks = ctcap ? h[1][1] : 0;
+    c->loc_smem = xcap * D * (int)sizeof(float);
+    c->loc_ct_smem = ctcap * D * (int)sizeof(float);
+    if (D == 2) {
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+    } else {
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+    }
     return MPH_OK;
 }
 

@@ -422,6 +422,7 @@ static int mixed_solve_t(mph_case* c)
     c->stats.inner_local_blocks = c->step_pairs ? c->loc_blocks[0] : 0;
     c->stats.inner_gather_blocks = c->step_pairs ? c->loc_blocks[1] : 0;
     c->stats.inner_local_cols = c->step_pairs ? c->loc_cols : 0;
+    c->stats.inner_ct_local_blocks = c->step_pairs ? c->loc_ct_blocks : 0;
     c->stats.status = bad ? MPH_ERR_NAN : (hs[kSRR] / hs[kSRR0] < tol_out2 || hs[kSRR] == 0.0 ? MPH_OK : MPH_ERR_NOT_CONVERGED);
     return MPH_OK;
 }

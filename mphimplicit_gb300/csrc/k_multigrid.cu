@@ -420,17 +420,20 @@ __global__ void k_mg_g2p_dot(DevParams P, LevelK L, const int* __restrict__ key,
                              const int* __restrict__ flags)
 {
     if (flags[kFlagDone]) return;
-    const int n = P.Nf * D;
     double acc = 0.0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = k / D, rD = k % D;
+    // a thread per particle: its level-0 cell is decoded from the key once
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.Nf; i += gridDim.x * blockDim.x) {
         int cc3[3];
         key_coords(P, key[i], cc3);
         const int g = grid_index(L, cc3[0] - L.mn[0], cc3[1] - L.mn[1], cc3[2] - L.mn[2]);
-        const TQ qk = q[k];
-        const TQ v = invDiag[k] * qk + (TQ)S0[g * D + rD];
-        u[k] = v;
-        acc += (double)qk * (double)v;
+#pragma unroll
+        for (int rD = 0; rD < D; ++rD) {
+            const size_t k = (size_t)i * D + rD;
+            const TQ qk = q[k];
+            const TQ v = invDiag[k] * qk + (TQ)S0[g * D + rD];
+            u[k] = v;
+            acc += (double)qk * (double)v;
+        }
     }
     reduce_finalize(acc, partials, counter, out);
 }
@@ -632,8 +635,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         prolong(l);
     }
     for (int k = 0; k < 2 + extra0; ++k) jacobi(0);      // level 0 post-smoothing
-    const int n = c->dp.Nf * D;
-    const int blocks = std::min<int>(grid_for(n, 256), kReduceBlocks);
+    const int blocks = std::min<int>(grid_for(c->dp.Nf, 256), kReduceBlocks);
     { k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
                                                      (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags); MPH_COUNT_LAUNCH(); }
 }

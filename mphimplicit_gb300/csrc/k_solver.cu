@@ -245,6 +245,7 @@ static int cr_solve_t(mph_case* c)
     c->stats.inner_form = 0;
     c->stats.inner_local_blocks = c->stats.inner_gather_blocks = 0;
     c->stats.inner_local_cols = 0;
+    c->stats.inner_ct_local_blocks = c->stats.inner_reserved = 0;
     c->stats.status = host_flags[kFlagBad] ? MPH_ERR_NAN : (host_flags[kFlagDone] && host_flags[kFlagIter] < cap ? MPH_OK : MPH_ERR_NOT_CONVERGED);
     for (auto& t : timed) {
         const int iter = t.first & ((1 << 30) - 1);

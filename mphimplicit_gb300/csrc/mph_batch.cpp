@@ -66,6 +66,7 @@ int case_footprint(const mph_params* prm, const mph_particles* parts, int dim, i
         b += (double)Nf * nb * 16.0 + blocks * (D * 4.0 + 8.0);
         b += (double)Nf * np * (D * 4.0 + 4.0) * 2.2 + (double)N * (8.0 * 16.0 + 8.0) + (double)Nf * 32.0;
         b += (double)Nf * 17.0 * 4.0;                         // block-local neighbour columns
+        b += (double)N * 33.0 * 4.0 + (double)Nf * np * 2.0;   // the same for the transposed P-lists (blocks of 256)
     } else {
         b += blocks * DD * 8.0;                               // FP64 blocks
         if (precision == MPH_PRECISION_MIXED) {

@@ -145,6 +145,14 @@ struct DeviceState {
     long long cap_uniq = 0;
     int* ucount = nullptr;
     long long cap_ucount = 0;
+    // the same for the transposed P-lists of k_ct_apply32's particle blocks
+    // (16-bit rank per slot)
+    unsigned short* ctlidx16 = nullptr;
+    long long cap_ctlidx16 = 0;
+    int* ctuniq = nullptr;
+    long long cap_ctuniq = 0;
+    int* ctucount = nullptr;
+    long long cap_ctucount = 0;
     int* ccell = nullptr;              // packed cell coordinates of every particle (pair path)
     double* io3 = nullptr;             // host-layout staging, 2 x N x 3 doubles (state upload, field download)
     int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
@@ -235,8 +243,10 @@ struct mph_case {
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
     cudaEvent_t gev[16] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
-    int loc_smem = 0;                   // shared memory of the inner operator's staged neighbour x (0: gathers by column)
+    int loc_smem = 0;                   // shared memory of k_visc_pen32's staged s (0: gathers by column)
+    int loc_ct_smem = 0;                // shared memory of k_ct_apply32's staged s (0: gathers by column)
     int loc_blocks[2] = {};             // row blocks staged / gathering by column
+    int loc_ct_blocks = 0;              // particle blocks of k_ct_apply32 staging s
     long long loc_cols = 0;             // distinct neighbour columns over the staged blocks
     bool visc_nonneg = true;            // every viscous pair coefficient f is >= 0
     bool ct_ready = false;              // transposed P-lists built for this step

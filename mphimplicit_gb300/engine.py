@@ -198,7 +198,7 @@ class Case:
         return {"iter": s.iterations, "rr0": s.rr0, "rr": s.rr, "rs0": s.rs0, "rs": s.rs, "status": s.status,
                 "outer": s.outer_iterations, "inner_form": s.inner_form,
                 "inner_local_blocks": s.inner_local_blocks, "inner_gather_blocks": s.inner_gather_blocks,
-                "inner_local_cols": s.inner_local_cols}
+                "inner_local_cols": s.inner_local_cols, "inner_ct_local_blocks": s.inner_ct_local_blocks}
 
     def set_solver(self, outer_rel_residual: float = 1e-6, inner_rel_residual: float = 1e-3, max_outer: int = 50):
         _check(self.lib.mph_case_set_solver(self.h, outer_rel_residual, inner_rel_residual, max_outer))

@@ -154,6 +154,7 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
     assert sa["inner_local_blocks"] + sa["inner_gather_blocks"] == nblk
     assert sa["inner_local_blocks"] > 0 and sa["inner_local_cols"] >= sa["inner_local_blocks"]
     assert sb["inner_local_blocks"] == sb["inner_gather_blocks"] == 0
+    assert sa["inner_ct_local_blocks"] > 0
     assert abs(sa["iter"] - sb["iter"]) <= max(2, sb["iter"] // 10), (sa, sb)
     assert abs(sa["outer"] - sb["outer"]) <= 1
     nf = a.fluid_count
