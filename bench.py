@@ -169,11 +169,9 @@ def pair_apply_bytes(prof, scal, dim, st=None):
     st = st or {}
     staged = st.get("inner_local_blocks", 0) > 0
     col = 0 if staged else 4
-    # transposed slots of particle blocks that stage s read a 2-byte rank
-    # instead of the 4-byte column: counted so for every slot once any block
-    # stages (a lower bound)
-    pcol = 4
-    ctcol = 2 if st.get("inner_ct_local_blocks", 0) > 0 else 4
+    # P-slots and transposed slots: 16-byte records (D values, zero-padded in
+    # 2-D, and the column or the block-local rank), counted as D * 4 + 4
+    pcol = ctcol = 4
     ct = pslots * (dim * 4 + ctcol) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
     vp = slots * (8 + col) + pslots * (dim * 4 + pcol) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
         + 2 * dim * nf * 4 + n * 4

@@ -306,16 +306,15 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 constexpr int kSIn0 = 16, kSIn = 17, kSTol2 = 23;
 __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 
-// LOC: a block of MPH_CT_BLOCK particles whose transposed lists hold
-// ucount[b] >= 0 distinct fluid rows stages their s in shared memory and
-// reads each slot's 16-bit rank among them instead of its column.
+// A transposed slot is one 16-byte record: C (D floats, zero-padded) and the
+// fluid row's column.  LOC: a block of MPH_CT_BLOCK particles whose lists
+// hold ucount[b] >= 0 distinct fluid rows stages their s in shared memory;
+// its records carry each row's rank among them in place of the column.
 template <int D, bool LOC>
 __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
-                                                    const int* __restrict__ ctscol, const float* __restrict__ ctsval,
-                                                    const float* __restrict__ x, float* __restrict__ t,
+                                                    const float4* __restrict__ ctrec, const float* __restrict__ x, float* __restrict__ t,
                                                     const double* __restrict__ scal, int* __restrict__ flags, int cap,
-                                                    const unsigned short* __restrict__ lidx, const int* __restrict__ uniq,
-                                                    const int* __restrict__ ucount)
+                                                    const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
     extern __shared__ float xs_ct[];
     if (flags[kFlagDone]) return;
@@ -347,26 +346,17 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
     }
     if (k >= N) return;
     const int lane = k & 31;
-    const long long base = ctsptr[k >> 5];
-    const float* vp = ctsval + base * D + lane;
+    const float4* rp = ctrec + ctsptr[k >> 5] + lane;
+    const float* xb = (LOC && U >= 0) ? xs_ct : x;   // by rank from shared memory, or by column
     float s = 0.f;
     const int n = ctcnt[k];
-    if (LOC && U >= 0) {
-        const unsigned short* lp = lidx + base + lane;
 #pragma unroll 4
-        for (int e = 0; e < n; ++e) {
-            const float* xj = xs_ct + (int)__ldcs(lp + (long long)e * 32) * D;
-#pragma unroll
-            for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * xj[d];
-        }
-    } else {
-        const int* cp = ctscol + base + lane;
-#pragma unroll 4
-        for (int e = 0; e < n; ++e) {
-            const int j = __ldcs(cp + (long long)e * 32);
-#pragma unroll
-            for (int d = 0; d < D; ++d) s += __ldcs(vp + ((long long)e * D + d) * 32) * x[(size_t)j * D + d];
-        }
+    for (int e = 0; e < n; ++e) {
+        const float4 r = __ldcs(rp + (long long)e * 32);
+        const float* xj = xb + (size_t)__float_as_int(r.w) * D;
+        s += r.x * xj[0];
+        s += r.y * xj[1];
+        if (D == 3) s += r.z * xj[2];
     }
     t[k] = s;
 }
@@ -426,7 +416,7 @@ template <int D, bool LOC>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ grec, const float* __restrict__ pscale, const float* __restrict__ sdiag,
-             const int* __restrict__ ncp, const long long* __restrict__ psptr, const int* __restrict__ pscol, const float* __restrict__ psval,
+             const int* __restrict__ ncp, const long long* __restrict__ psptr, const float4* __restrict__ psrec,
              const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
              const int* __restrict__ uniq, const int* __restrict__ ucount)
@@ -460,16 +450,16 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
-        {   // C Lambda t over the row's P-neighbours
-            const long long base = psptr[i >> 5];
-            const int* cp = pscol + base + lane;
-            const float* vp = psval + base * D + lane;
+        {   // C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
+            const float4* rp = psrec + psptr[i >> 5] + lane;
             const int np = ncp[i];
 #pragma unroll 4
             for (int a = 0; a < np; ++a) {
-                const float tk = t[__ldcs(cp + (long long)a * 32)];
-#pragma unroll
-                for (int d = 0; d < D; ++d) yv[d] += __ldcs(vp + ((long long)a * D + d) * 32) * tk;
+                const float4 r = __ldcs(rp + (long long)a * 32);
+                const float tk = t[__float_as_int(r.w)];
+                yv[0] += r.x * tk;
+                yv[1] += r.y * tk;
+                if (D == 3) yv[2] += r.z * tk;
             }
         }
 #pragma unroll
@@ -545,9 +535,18 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
             ctile[r * (kLtsK + 1) + kl] = col;
         }
         __syncthreads();
-        for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
-            const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
-            sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+        if (PAIRS) {
+            for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
+                const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
+                sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+            }
+        } else {   // 16-byte records: D values (zero-padded), the column
+            for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+                const int ln = o & 31, kl = o >> 5;
+                const float* v = tile + ln * W + kl * D;
+                reinterpret_cast<float4*>(sval)[sb + (long long)(k0 + kl) * 32 + ln] =
+                    make_float4(v[0], v[1], D == 3 ? v[2] : 0.f, __int_as_float(ctile[ln * (kLtsK + 1) + kl]));
+            }
         }
         if (PAIRS) {   // whole slot records (the index half is written later)
             for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
@@ -558,10 +557,11 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
                 reinterpret_cast<uint2*>(sval16)[sb + (long long)(k0 + kl) * 32 + ln] = make_uint2(h[0] | (h[1] << 16), h[2]);
             }
         }
-        for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
-            const int ln = o & 31, kl = o >> 5;
-            scol[sb + (long long)(k0 + kl) * 32 + ln] = ctile[ln * (kLtsK + 1) + kl];
-        }
+        if (PAIRS)
+            for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+                const int ln = o & 31, kl = o >> 5;
+                scol[sb + (long long)(k0 + kl) * 32 + ln] = ctile[ln * (kLtsK + 1) + kl];
+            }
         __syncthreads();
     }
 }
@@ -616,33 +616,33 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     const unsigned gv = grid_for(P.Nf, MPH_PAIR_BLOCK);
     if (c->dim == 2) {
         if (c->loc_ct_smem)
-            k_ct_apply32<2, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal,
-                                                                                d.flags, cap, d.ctlidx16, d.ctuniq, d.ctucount);
+            k_ct_apply32<2, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
+                                                                                d.scal, d.flags, cap, d.ctuniq, d.ctucount);
         else
-            k_ct_apply32<2, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags,
-                                                                     cap, nullptr, nullptr, nullptr);
+            k_ct_apply32<2, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
+                                                                     d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
         if (c->loc_smem)
             k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
             k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     } else {
         if (c->loc_ct_smem)
-            k_ct_apply32<3, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal,
-                                                                                d.flags, cap, d.ctlidx16, d.ctuniq, d.ctucount);
+            k_ct_apply32<3, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
+                                                                                d.scal, d.flags, cap, d.ctuniq, d.ctucount);
         else
-            k_ct_apply32<3, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ctscol, d.ctsval, x, d.tct32, d.scal, d.flags,
-                                                                     cap, nullptr, nullptr, nullptr);
+            k_ct_apply32<3, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
+                                                                     d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
         if (c->loc_smem)
             k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
             k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, d.pscol, d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     }
 }
@@ -961,17 +961,18 @@ k_part_pairs(DevParams P, Level0Map M, const int* __restrict__ key, const int* _
 }
 
 // Block-local columns of a sliced list: for block b of blockDim rows (thread
-// = row), the sorted distinct columns uniq[b][0..U) and, per slot e, the
-// column's rank among them at out16[e * OS + OO] (the fourth half of the
-// fluid slot records; a plain 16-bit array for the P-lists and transposed
-// P-lists).  A bitmap over the block's index
+// = row), the sorted distinct columns uniq[b][0..U) (slot e's column at
+// acol[e * IS + IO]) and, per slot e, the column's rank among them at
+// out16[e * OS + OO]: the fourth half of the fluid slot records, or the
+// column word of the transposed P-list records itself (each slot's column
+// is read before its rank replaces it, by the same thread).  A bitmap over the block's index
 // window [lo, hi] marks the neighbours; word ranks come from a block scan of
 // the word popcounts.  ucount[b] = U, or -1 when the window is wider than
 // kWinWords * 32 or U > kUMax (the operator then gathers by column).
-template <int OS, int OO>
+template <int IS, int IO, typename OutT, int OS, int OO>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const long long* __restrict__ sptr, const int* __restrict__ nfc,
-                                                             const int* __restrict__ acol, unsigned short* __restrict__ out16,
-                                                             int* __restrict__ uniq, int* __restrict__ ucount)
+                                                             const int* acol, OutT* out16, int* __restrict__ uniq,
+                                                             int* __restrict__ ucount)
 {
     extern __shared__ unsigned lc_smem[];
     unsigned* bm = lc_smem;                       // kWinWords bitmap words
@@ -986,7 +987,7 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
     // window of the block's columns
     int lo = INT_MAX, hi = -1;
     for (int k = 0; k < n; ++k) {
-        const int col = acol[base + (long long)k * 32];
+        const int col = acol[(base + (long long)k * 32) * IS + IO];
         lo = min(lo, col);
         hi = max(hi, col);
     }
@@ -1016,7 +1017,7 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
     for (int w = tid; w < nw; w += blockDim.x) bm[w] = 0u;
     __syncthreads();
     for (int k = 0; k < n; ++k) {
-        const int off = acol[base + (long long)k * 32] - lo;
+        const int off = acol[(base + (long long)k * 32) * IS + IO] - lo;
         atomicOr(&bm[off >> 5], 1u << (off & 31));
     }
     __syncthreads();
@@ -1051,9 +1052,9 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
     }
     for (int k = 0; k < n; ++k) {
         const long long e = base + (long long)k * 32;
-        const int off = acol[e] - lo;
+        const int off = acol[e * IS + IO] - lo;
         const unsigned word = bm[off >> 5];
-        out16[e * OS + OO] = (unsigned short)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
+        out16[e * OS + OO] = (OutT)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
     }
     int* ul = uniq + (size_t)blockIdx.x * kUMax;
     for (int w = w0; w < w1; ++w) {
@@ -1170,17 +1171,17 @@ int launch_pair_terms(mph_case* c)
 // lambda-scaled P-lists, of the fluid rows (after k_pair_terms).
 // Block-local columns of one sliced list (rows in blocks of `block`), their
 // counts and statistics after the blocks (read back with the other lists').
-template <int OS, int OO>
+template <int IS, int IO, typename OutT, int OS, int OO>
 static int local_cols(mph_case* c, int rows, int block, const long long* sptr, const int* cnt, const int* cols,
-                      unsigned short* out16, int** uniq, long long* cap_uniq, int** ucount, long long* cap_ucount)
+                      OutT* out16, int** uniq, long long* cap_uniq, int** ucount, long long* cap_ucount)
 {
     const long long nb = grid_for(rows, block);
     MPH_TRY(grow_i(uniq, cap_uniq, nb * kUMax));
     MPH_TRY(grow_i(ucount, cap_ucount, nb + 3));
     const size_t smem = 2 * kWinWords * sizeof(unsigned);
-    MPH_CUDA(cudaFuncSetAttribute(k_local_cols<OS, OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MPH_CUDA(cudaFuncSetAttribute(k_local_cols<IS, IO, OutT, OS, OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MPH_CUDA(cudaMemsetAsync(*ucount + nb, 0, 3 * sizeof(int), c->stream));
-    k_local_cols<OS, OO><<<(unsigned)nb, block, smem, c->stream>>>(rows, sptr, cnt, cols, out16, *uniq, *ucount);
+    k_local_cols<IS, IO, OutT, OS, OO><<<(unsigned)nb, block, smem, c->stream>>>(rows, sptr, cnt, cols, out16, *uniq, *ucount);
     MPH_COUNT_LAUNCH();
     return MPH_OK;
 }
@@ -1205,23 +1206,11 @@ static int launch_local_cols(mph_case* c)
     if (P.Nf == 0) return MPH_OK;
     const int D = c->dim;
     const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK), nbc = grid_for(P.N, MPH_CT_BLOCK);
-    long long ctslots = 0;
-    MPH_CUDA(cudaMemcpyAsync(&ctslots, d.ctsptr + (P.N + 31) / 32, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    MPH_CUDA(cudaStreamSynchronize(c->stream));
-    auto grow16 = [](unsigned short** p, long long* cap, long long need) -> int {
-        if (need <= *cap) return MPH_OK;
-        if (*p) cudaFree(*p);
-        *p = nullptr;
-        *cap = 0;
-        const long long n = need + need / 8 + 1024;
-        MPH_CUDA(cudaMalloc((void**)p, (size_t)n * sizeof(unsigned short)));
-        *cap = n;
-        return MPH_OK;
-    };
-    MPH_TRY(grow16(&d.ctlidx16, &d.cap_ctlidx16, ctslots));
-    MPH_TRY((local_cols<4, 3>(c, P.Nf, MPH_PAIR_BLOCK, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq, &d.ucount, &d.cap_ucount)));
-    MPH_TRY((local_cols<1, 0>(c, P.N, MPH_CT_BLOCK, d.ctsptr, d.ct_cnt, d.ctscol, d.ctlidx16, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
-                              &d.cap_ctucount)));
+    MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, MPH_PAIR_BLOCK, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,
+                                                    &d.ucount, &d.cap_ucount)));
+    int* ctw = reinterpret_cast<int*>(d.ctsval);   // the column words of the transposed records
+    MPH_TRY((local_cols<4, 3, int, 4, 3>(c, P.N, MPH_CT_BLOCK, d.ctsptr, d.ct_cnt, ctw, ctw, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
+                                         &d.cap_ctucount)));
     int h[2][3] = {};
     MPH_CUDA(cudaMemcpyAsync(h[0], d.ucount + nb, sizeof(h[0]), cudaMemcpyDeviceToHost, c->stream));
     MPH_CUDA(cudaMemcpyAsync(h[1], d.ctucount + nbc, sizeof(h[1]), cudaMemcpyDeviceToHost, c->stream));
@@ -1265,18 +1254,17 @@ int launch_pairs_to_slices(mph_case* c)
     }
     long long pslots = 0;
     MPH_TRY(launch_slice_ptr(c, P.Nf, d.ncp, d.pswidth, d.psptr, &pslots));
-    MPH_TRY(grow_i(&d.pscol, &d.cap_pscol, pslots));
-    MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * D));
+    MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * 4));   // 16-byte records
     if (D == 2) {
         { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
                                                                       d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                                       nullptr, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
                                                                       d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       d.pscol, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                                       nullptr, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return launch_local_cols(c);
 }
@@ -1296,13 +1284,12 @@ int launch_ct_slices(mph_case* c)
     }
     long long slots = 0;
     MPH_TRY(launch_slice_ptr(c, P.N, d.ct_cnt, d.ctswidth, d.ctsptr, &slots));
-    MPH_TRY(grow_i(&d.ctscol, &d.cap_ctscol, slots));
-    MPH_TRY(grow_f(&d.ctsval, &d.cap_ctsval, slots * D));
+    MPH_TRY(grow_f(&d.ctsval, &d.cap_ctsval, slots * 4));   // 16-byte records
     if (D == 2) {
-        { k_list_to_slices<2, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
+        { k_list_to_slices<2, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, nullptr,
                                                                d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_list_to_slices<3, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, d.ctscol,
+        { k_list_to_slices<3, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, nullptr,
                                                                d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;

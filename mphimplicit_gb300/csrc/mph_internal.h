@@ -146,9 +146,7 @@ struct DeviceState {
     int* ucount = nullptr;
     long long cap_ucount = 0;
     // the same for the transposed P-lists of k_ct_apply32's particle blocks
-    // (16-bit rank per slot)
-    unsigned short* ctlidx16 = nullptr;
-    long long cap_ctlidx16 = 0;
+    // (the rank replaces the column in the slot's record)
     int* ctuniq = nullptr;
     long long cap_ctuniq = 0;
     int* ctucount = nullptr;
@@ -162,8 +160,8 @@ struct DeviceState {
     long long cap_cvl32 = 0;
     long long *psptr = nullptr, *ctsptr = nullptr;
     int *pswidth = nullptr, *ctswidth = nullptr;
-    int *pscol = nullptr, *ctscol = nullptr;
-    float *psval = nullptr, *ctsval = nullptr;
+    int *pscol = nullptr, *ctscol = nullptr;   // (unused: the columns live in the records)
+    float *psval = nullptr, *ctsval = nullptr; // 16-byte slot records: D values (zero-padded), the column
     long long cap_pscol = 0, cap_psval = 0, cap_ctscol = 0, cap_ctsval = 0;
     // multigrid
     double *mg_cof = nullptr, *mg_invd = nullptr;
