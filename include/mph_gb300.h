@@ -232,7 +232,11 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
  *   FP32 operator runs on the sliced FP32 pair terms and P-lists and no
  *   blocks are written (CsrCofA export then fails with MPH_ERR_STATE; the
  *   block columns CsrIndA still export).  1: FP32 blocks are assembled and
- *   the inner SpMV runs on them. */
+ *   the inner SpMV runs on them.
+ *   "inner_local" 1 (default) / 0: pair-term inner operator only.  1: each
+ *   block of rows (particles, for the transposed P-lists) whose distinct
+ *   neighbours fit stages their s in shared memory; 0: every block gathers s
+ *   by column.  Both give the same bits. */
 int mph_case_set_option(mph_case* c, const char* name, double value);
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);

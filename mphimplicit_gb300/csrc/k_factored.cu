@@ -1203,7 +1203,7 @@ static int launch_local_cols(mph_case* c)
     c->loc_blocks[0] = c->loc_blocks[1] = 0;
     c->loc_ct_blocks = 0;
     c->loc_cols = 0;
-    if (P.Nf == 0) return MPH_OK;
+    if (P.Nf == 0 || !c->inner_local) return MPH_OK;
     const int D = c->dim;
     const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK), nbc = grid_for(P.N, MPH_CT_BLOCK);
     MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, MPH_PAIR_BLOCK, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,

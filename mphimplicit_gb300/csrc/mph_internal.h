@@ -236,6 +236,7 @@ struct mph_case {
     bool cell_assembly = true;          // cell-block assembly kernel (else per-row kernel only)
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
+    bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms

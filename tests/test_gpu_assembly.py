@@ -161,3 +161,24 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
     va = vec_proj(a.export("Velocity"), dim)[:nf]
     vb = vec_proj(b.export("Velocity"), dim)[:nf]
     assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 1e-5
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_staged_and_gathered_operator_give_the_same_bits(engine_lib, case):
+    """The pair-term operator sums the same terms in the same order whether a
+    block reads its neighbours' s from its shared-memory copy or gathers it
+    by column (option inner_local 0), so whole mixed steps agree bit for
+    bit."""
+    name, dim, params, parts = case
+    out = {}
+    for local in (1, 0):
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_option("inner_local", local)
+        g.step(2)
+        st = g.solve_stats()
+        assert st["inner_form"] == 2
+        out[local] = (g.export("Velocity"), g.export("Position"), st)
+    (va, pa, sa), (vb, pb, sb) = out[1], out[0]
+    assert sa["inner_local_blocks"] > 0 and sb["inner_local_blocks"] == 0 and sb["inner_ct_local_blocks"] == 0
+    assert sa["iter"] == sb["iter"]
+    assert np.array_equal(va, vb) and np.array_equal(pa, pb)
