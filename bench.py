@@ -9,16 +9,21 @@ files.  One step = the full reference step (sort, neighbours, explicit
 physics, assembly, multigrid build, CR solve).
 
   value : particle-steps/s of the mixed form (FP32 CR + V-cycle, FP64 outer
-          residual; --precision fp64 for the plain form) with the state
-          resident in HBM, CUDA events on the case stream around K steps (the
-          matrix alone is ~7 GB, far above L2); the line also carries the
-          plain FP64 form's value on the same workload and the velocity
-          difference of one step of each form from the same state
+          refinement to ||b - A x|| / ||b|| < 1e-10; --precision fp64 for the
+          plain form) with the state resident in HBM, CUDA events on the case
+          stream around K steps (the pair terms alone are ~7 GB, far above
+          L2).  The line also carries the plain FP64 form's value on the same
+          workload (the reference algorithm, stop test 1e-6) and the velocity
+          error of one mixed step against the FP64 form solved to 1e-12 from
+          the same state (the accuracy the metric names), plus the mixed form
+          at the reference's 1e-6 as a labelled secondary
   e2e   : the same metric through the public API with pinned host buffers:
-          every step uploads the particle state (mph_case_set_state) and reads
-          back ids, types, positions and velocities (mph_get_fields)
+          every one of K steps uploads the particle state
+          (mph_case_set_state) and reads back ids, types, positions and
+          velocities (mph_get_fields)
   --impl reference : the CPU restatement of the reference (the oracle,
-          OpenMP over all host cores) on a bounded sample of the workload
+          OpenMP over all host cores) on the same workload, one full step
+          per timed step
 """
 from __future__ import annotations
 
@@ -188,10 +193,30 @@ def assemble_bytes(prof, scal, dim):
             + dim * 8 * scal["NonzeroCountC"] / dim)
 
 
-def cpu_sample(threads: int, steps: int = 1, fluid: int = 60, check_gpu: bool = False):
+def assemble_pair_bytes(prof, scal, dim, case):
+    """Algorithmic bytes of the mixed form's assembly stage on the pair path
+    (no blocks): the neighbour and P-neighbour lists and the particle state
+    read once, and once written what the solve consumes: per fluid slot an
+    8-byte inner record, D FP32 g and a 4-byte column (outer residual); per
+    P-slot of a fluid row a 16-byte lambda-C record and a 16-byte transposed
+    record; per fluid row b (D doubles) and a 32-byte diagonal / inertia
+    record; the level-0 multigrid stencils (doubles)."""
+    nf = int(scal["FluidParticleEnd"])
+    n = int(scal["ParticleCount"])
+    slots = scal["NonzeroCountA"] / (dim * dim)
+    pslots = scal["NonzeroCountC"] / dim
+    lv0 = case.export("MultiGridCsrCofA:0").size
+    return (4 * prof["nnb"] + 4 * prof["nnbP"] + 64 * n + slots * (12 + 4 * dim) + pslots * 32
+            + nf * (dim * 8 + 32) + lv0 * 8)
+
+
+def cpu_sample(threads: int, steps: int = 1, fluid: int = 100, check_gpu: bool = False):
     """Time the oracle (OpenMP, `threads` threads) on the config-1 geometry
-    scaled to `fluid`^3 fluid particles; optionally run the GPU engine on the
-    same sample and report its velocity error against the oracle."""
+    at `fluid`^3 fluid particles (100: the workload itself), `steps` full
+    steps after the untimed initial pass; optionally run the GPU engine's
+    FP64 form on the same case and report the integer parity (sort
+    permutation, cell ranges, both neighbour lists) and the velocity error
+    against the oracle."""
     import oracle as orc
     orc.build_oracle()
     p, parts = casegen.cube_collapse_3d(fluid, seed=0)
@@ -201,16 +226,20 @@ def cpu_sample(threads: int, steps: int = 1, fluid: int = 60, check_gpu: bool = 
     o.step(steps)
     dt = time.perf_counter() - t0
     out = {"value": parts.count * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": f"3D cube collapse {fluid}^3 fluid ({parts.count} particles), {steps} step(s) after the initial pass, "
-                     f"{dt:.1f} s wall"}
+           "sample": f"3D cube collapse {fluid}^3 fluid ({parts.count} particles), {steps} full step(s) after the "
+                     f"initial pass, {dt:.1f} s wall"}
     if check_gpu:
         from mphimplicit_gb300 import engine
         g = engine.Case(p, parts, 3)
         g.step(steps)
-        vo = o.array("Velocity").reshape(-1, 3)[:g.fluid_count]
-        vg = g.export("Velocity").reshape(-1, 3)[:g.fluid_count]
-        ido, idg = o.array("ParticleIndex")[:g.fluid_count], g.export("ParticleIndex")[:g.fluid_count]
-        vo, vg = vo[np.argsort(ido)], vg[np.argsort(idg)]
+        nf = g.fluid_count
+        exact = {}
+        for name in ("ParticleIndex", "CellFluidParticleBegin", "CellFluidParticleEnd", "CellWallParticleBegin",
+                     "CellWallParticleEnd", "NeighborPtr", "NeighborInd", "NeighborPtrP", "NeighborIndP"):
+            exact[name] = bool(np.array_equal(g.export(name), o.array(name)))
+        out["gpu_bit_exact"] = exact
+        vo = o.array("Velocity").reshape(-1, 3)[:nf]
+        vg = g.export("Velocity").reshape(-1, 3)[:nf]
         out["gpu_err_vs_oracle"] = float(np.linalg.norm(vg - vo) / np.linalg.norm(vo))
         out["iters_oracle_gpu"] = [o.solve_stats()["iter"], g.solve_stats()["iter"]]
         g.close()
@@ -218,55 +247,85 @@ def cpu_sample(threads: int, steps: int = 1, fluid: int = 60, check_gpu: bool = 
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference's OpenMP path
+    (the oracle, all host threads) on the same workload as the GPU arm, W
+    untimed and K timed full steps after the initial pass.  The oracle's CR
+    iteration count of every timed step is reported beside the value."""
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     import oracle as orc
     orc.build_oracle()
-    fluid = args.ref_fluid
-    p, parts = casegen.cube_collapse_3d(fluid, seed=0)
-    o = orc.Oracle(p, parts, 3, threads=threads)
+    if args.workload in ("ensemble2d", "serve"):
+        dim, p, parts, desc = workload("dam2d_100")
+        desc += " (one case of the batched workloads' 2D family)"
+    elif args.ref_fluid > 0:
+        dim = 3
+        p, parts = casegen.cube_collapse_3d(args.ref_fluid, seed=0)
+        desc = f"3D cube collapse {args.ref_fluid}^3 fluid (config-1 geometry scaled)"
+    else:
+        dim, p, parts, desc = workload(args.workload)
+    t_init = time.perf_counter()
+    o = orc.Oracle(p, parts, dim, threads=threads)
     o.init()
+    t_init = time.perf_counter() - t_init
     for _ in range(args.warmup):
         o.step(1)
-    times = []
+    times, iters = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
+        iters.append(o.solve_stats()["iter"])
     tot = sum(times)
     value = parts.count * args.steps / tot
-    sample = (f"3D cube collapse {fluid}^3 fluid ({parts.count} particles; config-1 geometry scaled down), "
-              f"{args.steps} timed steps after {args.warmup} warm-up steps")
+    same = args.workload not in ("ensemble2d", "serve") and args.ref_fluid <= 0
+    sample = (f"{desc}: {parts.count} particles, the full workload; {args.steps} timed steps after {args.warmup} "
+              f"warm-up steps and the initial pass ({t_init:.1f} s, untimed); CR stop test 1e-6 (the reference's)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "sample": sample, "threads": threads},
+            "config": {"workload": args.workload if same else f"{args.workload} (sampled: {desc})", "description": desc,
+                       "dim": dim, "particles": parts.count, "sample": sample, "threads": threads,
+                       "cr_iterations": iters, "p50_step_ms": float(np.percentile(times, 50)) * 1000,
+                       "p99_step_ms": float(np.percentile(times, 99)) * 1000},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def _vel_error_vs_fp64(engine, cases, prec_mixed, prec_fp64, tol_outer):
-    """One step of each (params, parts, dim) in the mixed and the FP64 form
-    from the same state: relative velocity error of the mixed result over the
-    fluid particles (both forms keep the same particle order)."""
-    errs = []
+def _vel_error_vs_fp64(engine, cases, prec_mixed, prec_fp64, tol_outer, tol_ref=1e-12, extra=False):
+    """One step of each (params, parts, dim) in the mixed form (outer
+    tolerance tol_outer) and in the FP64 form solved to tol_ref (the
+    reference's CR with only its stop-test constant changed) from the same
+    state: relative velocity error of the mixed result over the fluid
+    particles (both forms keep the same particle order).  extra: also the
+    mixed form at the reference's 1e-6 and the FP64 form at 1e-6 against the
+    same tight solve (returned as a dict of lists)."""
+    errs, e_m6, e_f6 = [], [], []
     for params, parts, dim in cases:
+        runs = [(prec_fp64, tol_ref), (prec_mixed, tol_outer)]
+        if extra:
+            runs += [(prec_mixed, 1e-6), (prec_fp64, 1e-6)]
         out = []
-        for prec in (prec_mixed, prec_fp64):
+        for prec, tol in runs:
             g = engine.Case(params, parts, dim, precision=prec)
-            if prec == prec_mixed:
-                g.set_solver(tol_outer, 1e-3, 50)
+            g.set_solver(tol, 1e-3, 50)
             g.step(1)
-            f = g.fields(("id", "type", "vel"))
+            out.append(g.fields(("id", "type", "vel")))
             g.close()
-            out.append(f)
-        a, b = out
-        assert np.array_equal(a["id"], b["id"])
-        fl = b["type"] < 2
-        errs.append(float(np.linalg.norm(a["vel"][fl] - b["vel"][fl]) / max(np.linalg.norm(b["vel"][fl]), 1e-300)))
+        ref = out[0]
+        fl = ref["type"] < 2
+        nv = max(np.linalg.norm(ref["vel"][fl]), 1e-300)
+        for f in out[1:]:
+            assert np.array_equal(f["id"], ref["id"])
+        errs.append(float(np.linalg.norm(out[1]["vel"][fl] - ref["vel"][fl]) / nv))
+        if extra:
+            e_m6.append(float(np.linalg.norm(out[2]["vel"][fl] - ref["vel"][fl]) / nv))
+            e_f6.append(float(np.linalg.norm(out[3]["vel"][fl] - ref["vel"][fl]) / nv))
+    if extra:
+        return {"mixed": errs, "mixed_1e-6": e_m6, "fp64_1e-6": e_f6}
     return errs
 
 
@@ -436,7 +495,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--inner-tol", type=float, default=1e-3,
                     help="mixed form: relative residual reduction of each FP32 inner solve")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=-1, help="end-to-end steps (-1: the same K as the timed region)")
     ap.add_argument("--no-factored", action="store_true",
                     help="mixed form: assemble FP64 blocks instead of the factored FP64 operator")
     ap.add_argument("--extra-sweeps", type=int, default=0, help="mixed form: extra level-0 smoothing sweeps")
@@ -444,10 +503,13 @@ def main():
                     help="mixed form: inner operator on FP32 blocks (1) or sliced pair terms (0); -1 keeps the engine default")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-fluid", type=int, default=60)
-    ap.add_argument("--ref-fluid", type=int, default=50)
-    ap.add_argument("--outer-tol", type=float, default=1e-6,
-                    help="mixed form: FP64 outer relative residual (the reference's tolerance is 1e-6)")
+    ap.add_argument("--cpu-fluid", type=int, default=100,
+                    help="CPU baseline sample: the config-1 geometry at this fluid edge (100: the workload itself)")
+    ap.add_argument("--ref-fluid", type=int, default=0,
+                    help="reference arm: time the config-1 geometry scaled to this fluid edge instead of the workload (0)")
+    ap.add_argument("--outer-tol", type=float, default=1e-10,
+                    help="mixed form: FP64 outer relative residual (1e-10: iterative refinement of the mixed-precision "
+                         "configuration; the reference's own tolerance is 1e-6)")
     ap.add_argument("--cases", type=int, default=0, help="ensemble / serve: number of cases (0: 512 / 24)")
     ap.add_argument("--workers", type=int, default=64, help="ensemble / serve: host worker threads")
     ap.add_argument("--sample", type=int, default=16, help="ensemble: cases timed alone in the FP64 form")
@@ -478,45 +540,69 @@ def main():
         base = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "data": "synthetic", "roofline": None, "cpu_baseline": None}
         return run_ensemble(args, base) if args.workload == "ensemble2d" else run_serve(args, base)
+    return run_single(args, dist, rank, world, local)
+
+
+def run_single(args, dist, rank, world, local):
+    """One case of the named workload, resident on the GPU (the headline)."""
+    import torch
+    from mphimplicit_gb300 import engine
+    from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
     dim, params, parts, desc = workload(args.workload)
     stream = torch.cuda.Stream()
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
-    case = engine.Case(params, parts, dim, precision=prec, stream=stream.cuda_stream)
-    if prec == PRECISION_MIXED:
-        case.set_solver(args.outer_tol, args.inner_tol, 50)
-        case.set_option("factored", 0 if args.no_factored else 1)
-        case.set_option("mixed_extra_sweeps", args.extra_sweeps)
-        if args.inner_blocks >= 0:
-            case.set_option("inner_blocks", args.inner_blocks)
+    tol = args.outer_tol if prec == PRECISION_MIXED else 1e-6
+
+    def make(prec_, tol_):
+        c = engine.Case(params, parts, dim, precision=prec_, stream=stream.cuda_stream)
+        c.set_solver(tol_, args.inner_tol, 50)
+        if prec_ == PRECISION_MIXED:
+            c.set_option("factored", 0 if args.no_factored else 1)
+            c.set_option("mixed_extra_sweeps", args.extra_sweeps)
+            if args.inner_blocks >= 0:
+                c.set_option("inner_blocks", args.inner_blocks)
+        return c
+
+    def timed(c, steps, warmup, clocks=None, profile=False):
+        """Per-step CUDA-event milliseconds (case stream) and CR iterations
+        of `steps` steps after `warmup` untimed ones."""
+        for _ in range(warmup):
+            c.step(1)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        if profile:
+            c.profile(True)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        its = []
+        l0 = engine.launch_count()
+        with (clocks if clocks is not None else _Null()):
+            torch.cuda.synchronize()
+            evs[0].record(stream)
+            for k in range(steps):
+                c.step(1)
+                evs[k + 1].record(stream)
+                its.append(c.solve_stats()["iter"])
+            torch.cuda.synchronize()
+        launches = engine.launch_count() - l0
+        if dist:
+            dist.barrier()
+        return [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)], its, launches
+
+    case = make(prec, tol)
     N, Nf = case.count, case.fluid_count
-    for _ in range(args.warmup):
-        case.step(1)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    case.profile(True)
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    iters = []
-    l0 = engine.launch_count()
-    with Clocks(local) as clk:
-        torch.cuda.synchronize()
-        evs[0].record(stream)
-        for k in range(args.steps):
-            case.step(1)
-            evs[k + 1].record(stream)
-            iters.append(case.solve_stats()["iter"])
-        torch.cuda.synchronize()
-    launches = engine.launch_count() - l0
-    if dist:
-        dist.barrier()
-    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    clk = Clocks(local)
+    step_ms, iters, launches = timed(case, args.steps, args.warmup, clk, profile=True)
     total_s = sum(step_ms) / 1000.0
     prof = case.profile_read()
     case.profile(False)
     scal = case.scalars()
+    st = case.solve_stats()
     value, total_s = replica_throughput(N * args.steps, total_s, dist, "cuda")
 
-    # end to end through the public API with host buffers (pinned)
+    # end to end through the public API with host buffers (pinned): every
+    # step uploads the state and reads it back (the wall centres stay on the
+    # case: mph_case_set_state keeps them when given none)
     def pinned(shape, dt):
         return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
     fields = {"id": pinned((N,), torch.int32), "type": pinned((N,), torch.int32), "pos": pinned((N, 3), torch.float64),
@@ -525,29 +611,29 @@ def main():
     host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
                              fields["vel"])
     ids = fields["id"]
-    wc = case.export("WallCenter")
-    vs = 2 if dim == 2 else 4
-    h2d = N * (vs * 8 * 2 + 4 + 4)
-    d2h = N * (vs * 8 * 2 + 4 + 4)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    if args.e2e_steps <= 0:
-        t0 -= 1.0   # no end-to-end sample requested (profiling runs)
-    for _ in range(args.e2e_steps):
-        case.set_state(host, ids, wc)
-        case.step(1)
-        case.fields(out=fields)   # read back into the same pinned buffers
-        host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
-                                 fields["vel"])
-        wc = case.export("WallCenter")
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = N * args.e2e_steps * world / e2e_s if args.e2e_steps > 0 else None
+    h2d = N * (3 * 8 * 2 + 4 + 4)
+    d2h = N * (3 * 8 * 2 + 4 + 4)
+    e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
+    e2e_value = None
+    if e2e_steps > 0:
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            case.set_state(host, ids)
+            case.step(1)
+            case.fields(out=fields)   # read back into the same pinned buffers
+            host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"],
+                                     fields["pos"], fields["vel"])
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e_value, _ = replica_throughput(N * e2e_steps, e2e_s, dist, "cuda")
 
-    # roofline of the dominant kernel (CUDA events on the case stream)
+    # roofline of the dominant kernel (CUDA events on the case stream) and of
+    # the assembly stage
     peak, peak_kind = measured_peaks()
     vb = 4 if prec == PRECISION_MIXED else 8
-    st = case.solve_stats()
     pairs = st.get("inner_form") == 2
     kern = {"spmv": ("k_ct_apply32+k_visc_pen32", lambda p_, s_, d_: pair_apply_bytes(p_, s_, d_, st)) if pairs else
                     ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
@@ -558,43 +644,56 @@ def main():
     bytes_per = kern[dom][1](prof, scal, dim)
     achieved = bytes_per / avg_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(kern[dom][0]), "kernel": kern[dom][0], "peak_source": peak_kind,
+                "traffic": ncu_traffic(kern[dom][0]) if args.workload == "cube3d_100" else None,
+                "kernel": kern[dom][0], "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_per, "avg_launch_ms": avg_s * 1000.0, "launches": nlaunch}
+    asm_ms = prof["stage_ms_assemble"] / args.steps
+    asm_bytes = (assemble_pair_bytes(prof, scal, dim, case) if pairs else assemble_bytes(prof, scal, dim))
+    roofline_asm = {"bound": "hbm", "achieved": asm_bytes / (asm_ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": asm_bytes / (asm_ms / 1000.0) / 1e9 / peak, "stage": "assemble",
+                    "algorithmic_bytes_per_step": asm_bytes, "ms_per_step": asm_ms, "peak_source": peak_kind,
+                    "form": "pair terms (mixed)" if pairs else "sliced-ELL blocks"}
+    case.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample(os.cpu_count() or 1, 1, args.cpu_fluid, check_gpu=True)
 
-    # the plain FP64 form on the same workload (for the mixed form's speed-up),
-    # and one step of each form from the same state (velocity error)
+    # the plain FP64 form on the same workload (for the mixed form's
+    # speed-up), the mixed form at the reference's 1e-6 (secondary), and one
+    # step of each form from the same state against the FP64 form solved to
+    # 1e-12 (the accuracy of the metric)
     plain = None
-    errs = []
+    errs = {}
+    secondary = None
     if prec == PRECISION_MIXED and not args.no_fp64_leg:
-        case.close()
-        f = engine.Case(params, parts, dim, precision=PRECISION_FP64, stream=stream.cuda_stream)
-        for _ in range(args.warmup):
-            f.step(1)
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        torch.cuda.synchronize()
-        ev[0].record(stream)
-        for _ in range(args.steps):
-            f.step(1)
-        ev[1].record(stream)
-        torch.cuda.synchronize()
-        plain = N * args.steps / (ev[0].elapsed_time(ev[1]) / 1000.0)
+        f = make(PRECISION_FP64, 1e-6)
+        ms, its, _ = timed(f, args.steps, args.warmup)
+        plain = N * args.steps / (sum(ms) / 1000.0)
+        plain_iters = its
         f.close()
-        errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol)
+        m6 = make(PRECISION_MIXED, 1e-6)
+        ms6, its6, _ = timed(m6, args.steps, args.warmup)
+        m6.close()
+        secondary = {"outer_tol": 1e-6, "value": N * args.steps / (sum(ms6) / 1000.0), "cr_iterations": its6,
+                     "note": "mixed form stopped at the reference's own 1e-6; its velocity differs from the 1e-12 FP64 "
+                             "solve by vel_rel_err_vs_fp64_1e-12.mixed_1e-6 (not the headline)"}
+        errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,
+                                  extra=True)
+    max_err = max(errs["mixed"]) if errs else None
 
     stage_total = sum(prof[f"stage_ms_{s}"] for s in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == PRECISION_FP64 else "f32-inner/f64-outer", "data": "synthetic",
+        "dtype": "f64" if prec == PRECISION_FP64 else
+                 ("f32-inner(fp16 pair-term storage)/f64-outer" if pairs else "f32-inner/f64-outer"),
+        "data": "synthetic",
         "config": {"workload": args.workload, "description": desc, "dim": dim, "particles": N, "fluid": Nf,
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (the block matrix alone exceeds 129 MB by ~100x)",
+                   "l2": "inputs larger than L2 (the pair terms alone exceed 129 MB by ~50x)",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-                   "cr_iterations": iters,
+                   "outer_tol": tol, "cr_iterations": iters,
                    "inner_row_blocks": {"staged": st.get("inner_local_blocks"), "gathering": st.get("inner_gather_blocks"),
                                         "ct_blocks_staging_s": st.get("inner_ct_local_blocks"),
                                         "mean_distinct_cols": (st["inner_local_cols"] / st["inner_local_blocks"]
@@ -605,24 +704,34 @@ def main():
                    "kernel_avg_ms": {k: (prof[f"kern_ms_{k}"] / prof[f"kern_n_{k}"] if prof[f"kern_n_{k}"] else None)
                                      for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
                    "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
-                   "outer_tol": args.outer_tol if prec == PRECISION_MIXED else 1e-6,
                    "plain_fp64_value": plain,
+                   "plain_fp64_cr_iterations": plain_iters if plain else None,
                    "speedup_vs_plain_fp64": (value / plain) if plain else None,
-                   "vel_rel_err_vs_fp64_per_step": errs},
+                   "vel_rel_err_vs_fp64_1e-12": errs or None,
+                   "max_vel_rel_err": max_err,
+                   "meets_1e-6": (max_err <= 1e-6) if max_err is not None else None,
+                   "secondary_mixed_1e-6": secondary},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": args.e2e_steps},
+                "steps": e2e_steps},
         "gpu_launches": launches,
         "roofline": roofline,
+        "roofline_assembly": roofline_asm,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if prec != PRECISION_MIXED or args.no_fp64_leg:
-        case.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
 
 
 if __name__ == "__main__":

@@ -207,9 +207,11 @@ int mph_server_destroy(mph_server* s);
 
 /* Solver tolerances.  outer_rel_residual: stop when ||b - A x|| / ||b|| is
  * below it (the reference stops at 1e-6: rr/rr0 < 1e-12, main.cpp:4346; this
- * is the default and the only value the FP64 form uses).  Mixed form only:
- * inner_rel_residual (relative reduction of each FP32 inner solve, default
- * 1e-3) and max_outer (refinement steps, default 50).  No counterpart in the
+ * is the default of both forms).  In the FP64 form it replaces only that
+ * constant of the CR stop test (e.g. 1e-12 for a reference solution of a
+ * tighter mixed solve).  Mixed form only: inner_rel_residual (relative
+ * reduction of each FP32 inner solve, default 1e-3) and max_outer (refinement
+ * steps, default 50; the FP64 form ignores both).  No counterpart in the
  * reference, whose tolerance is a constant. */
 int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel_residual, int max_outer);
 

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(128) k_vector_p(DevParams P, const int* __rest
     const int ti = type[i];
     const double v0 = vsp[i];
     double p = 0.0;
-    if (v0 > 0.0) p = (v0 < 0.0 ? 0.0 : P.bulk[ti]) * v0;
+    if (v0 > 0.0) p = P.bulk[ti] * v0;   // Kappa is 0 where VolStrainP < 0 (main.cpp:1704-1735)
     const bool wi = is_wall(ti);
     const double lam = P.lambda[ti];
     double xi[3], vi[3];

@@ -13,19 +13,26 @@
 // memory is committed has no room for a per-call buffer, so an allocation
 // can fail exactly when the check is wanted (for instance right after another
 // case ran out of memory); and cudaFree waits for the whole device, so a
-// per-call buffer would stall the streams of every other resident case.  The
-// array below is reserved when the module is loaded, so these callers can run
-// the check at any time.
+// per-call buffer would stall the streams of every other resident case.
+//
+// When the array exists: this file is its own CUDA module, and with CUDA's
+// default lazy module loading a module (with its __device__ arrays) is loaded
+// on a device only when something in it is first used there.  So
+// noalloc_prepare, called by mph_case_create on the case's device before the
+// case allocates anything, looks up the array's address (which loads the
+// module and reserves the array) and loads the kernel code; every later check
+// on that device then needs no device memory at all, and no check has to
+// come before a stream capture.
 //
 // Limits and rules:
 //   - at most kNoAllocMaxBlocks blocks of 128 rows, i.e. 2,097,152 fluid
 //     particles; larger cases are rejected with MPH_ERR_CAPACITY;
-//   - the array's device address is looked up once per device, on the first
-//     call made for a case on that device (with that device current); make
-//     that first call before any stream capture;
 //   - one array per device serves every case: calls that overlap on the GPU
 //     (other streams, other host threads) race on it and must be serialised
-//     by the caller.
+//     by the caller;
+//   - the address is cached per device for the life of the process: the
+//     check must not be used across a cudaDeviceReset (or any reset of the
+//     device's primary context), which frees the array.
 #include <mutex>
 
 #include "mph_internal.h"
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(kNoAllocRows) k_resid_norms(int Nf, const int*
 }
 
 // Device address of the scratch array for device `dev` (which is current);
-// looked up on the first call for that device.
+// looked up once per device (first case creation on it).
 int scratch_for_device(int dev, double** out)
 {
     if (dev < 0 || dev >= kMaxDevices) return fail(MPH_ERR_CAPACITY, "device ordinal beyond the allocation-free residual's table");
@@ -166,6 +173,20 @@ int residual_noalloc(mph_case* c, double* out)
 }
 
 }  // namespace
+
+// Called by case creation with the case's device current, before the case
+// allocates: resolves the array's address and loads both kernel variants, so
+// the module's memory is taken while memory is still free.
+int noalloc_prepare(int dev)
+{
+    double* p = nullptr;
+    MPH_TRY(scratch_for_device(dev, &p));
+    cudaFuncAttributes a;
+    MPH_CUDA(cudaFuncGetAttributes(&a, k_resid_norms<2>));
+    MPH_CUDA(cudaFuncGetAttributes(&a, k_resid_norms<3>));
+    return MPH_OK;
+}
+
 }  // namespace mph
 
 extern "C" int mph_residual_noalloc(mph_case* c, double* out)

@@ -41,14 +41,15 @@ __global__ void k_cr_init(int Nf, const int* __restrict__ type, const double* __
 
 // MODE 0: r = b - A x with (r,r) -> out.   MODE 1: y = A s with (s,y) ->
 // the rho slot of iteration it = flags[kFlagIter], after the convergence test
-// of that iteration (out is unused).
+// of that iteration, rr/rr0 < tol2 (out is unused).  The reference's test is
+// rr/rr0 < 1e-12 (main.cpp:4346), i.e. tol2 = (1e-6)^2.
 template <int D, int MODE>
 __global__ void __launch_bounds__(128) k_spmv(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
                                               const int* __restrict__ acol, const double* __restrict__ aval,
                                               const double* __restrict__ xin, const double* __restrict__ b,
                                               double* __restrict__ yout, double* __restrict__ scal, int* __restrict__ flags,
-                                              int cap, double* __restrict__ partials, unsigned* __restrict__ counter,
-                                              double* __restrict__ out)
+                                              int cap, double tol2, double* __restrict__ partials,
+                                              unsigned* __restrict__ counter, double* __restrict__ out)
 {
     constexpr int DD = D * D;
     if (MODE == 1) {
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(128) k_spmv(int Nf, const int* __restrict__ nf
         const int it = flags[kFlagIter];
         const double rr = scal[kSRR], rr0 = scal[kSRR0];
         const bool bad = !(rr == rr);   // NaN residual
-        if (it >= cap || rr / rr0 < 1.0e-12 || bad) {
+        if (it >= cap || rr / rr0 < tol2 || bad) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 flags[kFlagDone] = 1;
                 if (bad) flags[kFlagBad] = 1;
@@ -170,6 +171,9 @@ static int cr_solve_t(mph_case* c)
     double* part = c->d.partials;
     const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
     const unsigned gs = grid_for(Nf, 128);
+    // stop test ||r||/||b|| < tol_outer on squared norms (1e-6 by default, the
+    // reference's constant; mph_case_set_solver tightens it)
+    const double tol2 = c->tol_outer == 1.0e-6 ? 1.0e-12 : c->tol_outer * c->tol_outer;
     MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
 
@@ -177,7 +181,7 @@ static int cr_solve_t(mph_case* c)
                                                 c->dp.density[1], c->dp.vol, c->dp.dt, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.bvec, c->d.s, scal + kSRS0);
     { k_spmv<D, 0><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.x, c->d.bvec, c->d.r, scal, flags, 0,
-                                     part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
+                                     tol2, part, counter, scal + kSRR); MPH_COUNT_LAUNCH(); }
     vcycle_fp64(c, c->d.r, c->d.s, scal + kSQU);
 
     // One CR iteration; the iteration index lives in flags[kFlagIter], so the
@@ -187,7 +191,7 @@ static int cr_solve_t(mph_case* c)
     auto iteration = [&, c](cudaEvent_t* e) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
         { k_spmv<D, 1><<<gs, 128, 0, st>>>(Nf, c->d.nfc, c->d.sptr, c->d.acol, c->d.aval, c->d.s, nullptr, c->d.y, scal, flags,
-                                         cap, part, counter, nullptr); MPH_COUNT_LAUNCH(); }
+                                         cap, tol2, part, counter, nullptr); MPH_COUNT_LAUNCH(); }
         if (e) prof_begin(c, 0, &e[1]);
         { k_update_pq<<<rb, kReduceThreads, 0, st>>>(n, c->d.s, c->d.y, c->d.p, c->d.q, scal, flags); MPH_COUNT_LAUNCH(); }
         if (e) prof_begin(c, 1, &e[2]);
@@ -205,7 +209,7 @@ static int cr_solve_t(mph_case* c)
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
     const bool graphs = c->use_graphs && !c->prof.on;
     if (graphs) {
-        MPH_TRY(capture_graph(c, &c->cr_exec, &c->cr_sig, graph_signature(c, 1.0e-12, cap), [&] {
+        MPH_TRY(capture_graph(c, &c->cr_exec, &c->cr_sig, graph_signature(c, tol2, cap), [&] {
             for (int k = 0; k < chunk; ++k) iteration(nullptr);
         }, &c->cr_launches));
     }

@@ -96,8 +96,6 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
     NEED(c);
     if (!(outer_rel_residual > 0.0) || !(inner_rel_residual > 0.0) || inner_rel_residual >= 1.0 || max_outer < 1)
         return mph::fail(MPH_ERR_ARG, "solver tolerances must be positive (inner < 1) and max_outer >= 1");
-    if (c->precision == MPH_PRECISION_FP64 && outer_rel_residual != 1.0e-6)
-        return mph::fail(MPH_ERR_ARG, "the FP64 form keeps the reference's tolerance 1e-6");
     c->tol_outer = outer_rel_residual;
     c->tol_inner = inner_rel_residual;
     c->max_outer = max_outer;

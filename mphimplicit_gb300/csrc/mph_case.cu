@@ -622,7 +622,10 @@ int case_create(const mph_params* prm, const mph_particles* parts, int dim, int 
     c->stream = (cudaStream_t)stream;
     c->prm = *prm;
     cudaGetDevice(&c->device);
-    int st = derive(c, parts);
+    // the allocation-free residual check's fixed array is reserved on this
+    // device before the case takes its memory
+    int st = noalloc_prepare(c->device);
+    if (st == MPH_OK) st = derive(c, parts);
     if (st == MPH_OK) {
         int nf = 0;
         for (int i = 0; i < parts->count; ++i) nf += parts->type[i] < 2;

@@ -349,6 +349,7 @@ int ensure_mg_cof(mph_case* c);
 void launch_mg_coarse(mph_case* c, int L);
 void launch_mg_invd(mph_case* c);
 int run_cr_solve(mph_case* c);
+int noalloc_prepare(int dev);   // k_resid_noalloc.cu: reserve the allocation-free check's array on this device
 int run_mixed_solve(mph_case* c);
 bool mixed_available();
 

@@ -65,6 +65,7 @@ struct Case {
     std::vector<Level> lv;
     int iters = 0;
     double rr0 = 0, rr = 0, rs0 = 0, rs = 0;
+    double tol2 = 1.0e-12;   // CR stop test rr/rr0 < tol2 (main.cpp:4346 has the constant 1e-12)
     std::vector<double> tmpd;
 };
 
@@ -968,7 +969,7 @@ int solve(Case& c)   // solveWithConjugatedGradient main.cpp:4270-4421
     int it;
     for (it = 0; it < n; ++it) {
         c.rr = dot(n, r.data(), r.data());
-        if (c.rr / c.rr0 < 1.0e-12) break;
+        if (c.rr / c.rr0 < c.tol2) break;
         spmv_a(c, 1.0, s.data(), 0.0, y.data());
         rho = dot(n, s.data(), y.data());
         if (it == 0) {
@@ -1278,6 +1279,11 @@ int mpho_scalars(mpho_case* h, double* out)
     const int n = (int)(sizeof(v) / sizeof(v[0]));
     for (int i = 0; i < n; ++i) out[i] = v[i];
     return n;
+}
+
+void mpho_set_tolerance(mpho_case* h, double rel)
+{
+    h->c.tol2 = rel == 1.0e-6 ? 1.0e-12 : rel * rel;
 }
 
 int mpho_solve_stats(mpho_case* h, double* out5)

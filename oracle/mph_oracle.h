@@ -35,6 +35,9 @@ int  mpho_solve(mpho_case* c);         /* returns CR iteration count            
 void mpho_step_end(mpho_case* c);
 void mpho_output_fields(mpho_case* c);
 int  mpho_step(mpho_case* c, int nsteps);
+/* CR stop test ||r||/||b|| < rel (the reference's constant, main.cpp:4346, is
+ * rel = 1e-6, i.e. rr/rr0 < 1e-12; only that constant changes). */
+void mpho_set_tolerance(mpho_case* c, double rel);
 
 /* Named arrays (same names and layouts as the reference globals). */
 long mpho_array(mpho_case* c, const char* name, void** ptr, int* kind);

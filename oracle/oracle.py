@@ -34,8 +34,10 @@ REF_SO = {2: os.path.join(HERE, "_ref", "libmphref2d.so"), 3: os.path.join(HERE,
 _KIND = {0: np.int32, 1: np.int64, 2: np.float64}
 
 
-def build_oracle(ref: bool = False) -> None:
-    targets = ["oracle"] + (["ref"] if ref else [])
+def build_oracle(ref=False) -> None:
+    """Build the oracle; ref=True also the reference harness (needs the
+    reference checkout), ref="if-present" only where the checkout exists."""
+    targets = ["oracle"] + (["ref-if-present"] if ref == "if-present" else ["ref"] if ref else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
@@ -69,6 +71,8 @@ def oracle_lib():
                                              ctypes.POINTER(ctypes.c_int)]
         lib.mpho_set_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.mpho_set_threads.argtypes = [ctypes.c_int]
+        lib.mpho_set_tolerance.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        lib.mpho_set_tolerance.restype = None
         _lib = lib
     return _lib
 
@@ -110,6 +114,10 @@ class Oracle:
     def step_end(self): self.lib.mpho_step_end(self.h)
     def output_fields(self): self.lib.mpho_output_fields(self.h)
     def step(self, n=1): return self.lib.mpho_step(self.h, n)
+
+    def set_tolerance(self, rel: float):
+        """CR stop test ||r||/||b|| < rel; the reference's constant is 1e-6."""
+        self.lib.mpho_set_tolerance(self.h, rel)
 
     def array(self, name: str) -> np.ndarray:
         p = ctypes.c_void_p()

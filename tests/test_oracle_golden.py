@@ -133,3 +133,28 @@ def test_generator_reproduces_reference_sample():
     parts = casegen.boid_to_particles(h["ParticleDistance"][0], h["LowerDomain"], h["UpperDomain"], b["cuboids"])
     assert hashlib.sha256(casegen.generator_text(parts).encode()).hexdigest() == str(z["grid_sha256"])
     assert np.array_equal(parts.types, z["types"]) and np.array_equal(parts.pos, z["pos"])
+
+
+def test_oracle_tolerance_only_moves_the_stop_test(oracle_built):
+    """The oracle's stop-test constant (main.cpp:4346, rr/rr0 < 1e-12) is a
+    parameter: 1e-6 (the default) gives the reference's iterates; 1e-12
+    continues the same iteration further, so its solution solves the same
+    system to a relative residual below 1e-12."""
+    p, parts = casegen.square_drop_2d(scale=0.1, seed=0)
+    runs = {}
+    for tol in (None, 1e-6, 1e-12):
+        o = orc.Oracle(p, parts, 2, threads=1)
+        o.init()
+        if tol is not None:
+            o.set_tolerance(tol)
+        o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build(); o.solve()
+        x = o.array("Velocity").reshape(-1, 3)
+        nf = int(o.scalars()["FluidParticleEnd"])
+        ptr, ind, val, b = o.array("CsrPtrA"), o.array("CsrIndA"), o.array("CsrCofA"), o.array("VectorB")
+        r = b - csr_mul(ptr, ind, val, x[:nf].ravel())
+        runs[tol] = (o.solve_stats(), x, float(np.linalg.norm(r) / np.linalg.norm(b)))
+    assert runs[None][0] == runs[1e-6][0]
+    assert np.array_equal(runs[None][1], runs[1e-6][1])
+    assert runs[1e-12][0]["iter"] > runs[1e-6][0]["iter"]
+    assert runs[1e-12][0]["rr"] / runs[1e-12][0]["rr0"] < 1e-24
+    assert runs[1e-12][2] < 1e-12 < runs[1e-6][2] * 1e-3
