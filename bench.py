@@ -295,23 +295,44 @@ def run_reference(args, rank, world):
     return 0
 
 
-def _vel_error_vs_fp64(engine, cases, prec_mixed, prec_fp64, tol_outer, tol_ref=1e-12, extra=False):
+def _vel_error_vs_fp64(engine, cases, prec_mixed, prec_fp64, tol_outer, tol_ref=1e-12, extra=False, pre=0, setup=None):
     """One step of each (params, parts, dim) in the mixed form (outer
     tolerance tol_outer) and in the FP64 form solved to tol_ref (the
     reference's CR with only its stop-test constant changed) from the same
     state: relative velocity error of the mixed result over the fluid
-    particles (both forms keep the same particle order).  extra: also the
-    mixed form at the reference's 1e-6 and the FP64 form at 1e-6 against the
-    same tight solve (returned as a dict of lists)."""
+    particles (both forms keep the same particle order).  pre > 0: the mixed
+    case first takes `pre` steps (so that a step with solver history is
+    measured) and every form starts from its state.  setup(case) sets the
+    mixed form's options.  extra: also the mixed form at the reference's
+    1e-6 and the FP64 form at 1e-6 against the same tight solve (returned as
+    a dict of lists)."""
     errs, e_m6, e_f6 = [], [], []
     for params, parts, dim in cases:
         runs = [(prec_fp64, tol_ref), (prec_mixed, tol_outer)]
         if extra:
             runs += [(prec_mixed, 1e-6), (prec_fp64, 1e-6)]
+        start = None
+        if pre > 0:
+            m = engine.Case(params, parts, dim, precision=prec_mixed)
+            m.set_solver(tol_outer, 1e-3, 50)
+            if setup:
+                setup(m)
+            m.step(pre)
+            f = m.fields(("id", "type", "pos", "vel"))
+            import mphimplicit_gb300.casegen as cg
+            start = (cg.Particles(m.time(), parts.spacing, parts.domain_min, parts.domain_max, f["type"], f["pos"], f["vel"]),
+                     f["id"], m.export("WallCenter"), m)
         out = []
         for prec, tol in runs:
-            g = engine.Case(params, parts, dim, precision=prec)
+            if start is not None and prec == prec_mixed and tol == tol_outer:
+                g = start[3]                     # the case with its history
+            else:
+                g = engine.Case(params, parts, dim, precision=prec)
+                if start is not None:
+                    g.set_state(start[0], start[1], start[2])
             g.set_solver(tol, 1e-3, 50)
+            if prec == prec_mixed and setup and g is not (start[3] if start else None):
+                setup(g)
             g.step(1)
             out.append(g.fields(("id", "type", "vel")))
             g.close()
@@ -501,6 +522,8 @@ def main():
     ap.add_argument("--extra-sweeps", type=int, default=0, help="mixed form: extra level-0 smoothing sweeps")
     ap.add_argument("--inner-blocks", type=int, default=-1, choices=[-1, 0, 1],
                     help="mixed form: inner operator on FP32 blocks (1) or sliced pair terms (0); -1 keeps the engine default")
+    ap.add_argument("--extrapolate", type=int, default=0, choices=[0, 1],
+                    help="mixed form: start each CR solve from 2 v_n - v_(n-1) instead of v_n")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -561,6 +584,7 @@ def run_single(args, dist, rank, world, local):
             c.set_option("mixed_extra_sweeps", args.extra_sweeps)
             if args.inner_blocks >= 0:
                 c.set_option("inner_blocks", args.inner_blocks)
+            c.set_option("extrapolate", args.extrapolate)
         return c
 
     def timed(c, steps, warmup, clocks=None, profile=False):
@@ -678,8 +702,14 @@ def run_single(args, dist, rank, world, local):
         secondary = {"outer_tol": 1e-6, "value": N * args.steps / (sum(ms6) / 1000.0), "cr_iterations": its6,
                      "note": "mixed form stopped at the reference's own 1e-6; its velocity differs from the 1e-12 FP64 "
                              "solve by vel_rel_err_vs_fp64_1e-12.mixed_1e-6 (not the headline)"}
+        def setup(c):
+            c.set_option("factored", 0 if args.no_factored else 1)
+            c.set_option("mixed_extra_sweeps", args.extra_sweeps)
+            if args.inner_blocks >= 0:
+                c.set_option("inner_blocks", args.inner_blocks)
+            c.set_option("extrapolate", args.extrapolate)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,
-                                  extra=True)
+                                  extra=True, pre=args.warmup, setup=setup)
     max_err = max(errs["mixed"]) if errs else None
 
     stage_total = sum(prof[f"stage_ms_{s}"] for s in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"))

@@ -81,8 +81,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
-             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ sdiag32, float* __restrict__ cvl32,
-             unsigned* __restrict__ gmax)
+             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ cvl32, unsigned* __restrict__ gmax)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -96,8 +95,6 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         float hi[3], li[3];
         load_f32<D>(pos32, i, hi);
         load_f32<D>(poslo32, i, li);
-        float sumw[3] = {0.f, 0.f, 0.f};
-        float sd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // sum of f e (x) e over the wall slots: xx xy xz yy yz zz
         float lm = 0.f;                                  // largest |g| component of the fluid slots
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
@@ -135,21 +132,6 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                     f = P.vm32[ti][type[j]] * wd * inv;
 #pragma unroll
                     for (int d = 0; d < D; ++d) e[d] = q32[d] * inv;
-                    if (k >= nf) {   // wall neighbour: its velocity enters b
-                        double vj[3];
-                        load_vec<D>(vel, j, vj);
-                        float ev = 0.f;
-#pragma unroll
-                        for (int d = 0; d < D; ++d) ev += e[d] * (float)vj[d];
-#pragma unroll
-                        for (int r = 0; r < D; ++r) sumw[r] += f * e[r] * ev;
-                        sd[0] += f * e[0] * e[0];
-                        sd[1] += f * e[0] * e[1];
-                        sd[2] += f * e[0] * e[2];
-                        sd[3] += f * e[1] * e[1];
-                        sd[4] += f * e[1] * e[2];
-                        sd[5] += f * e[2] * e[2];
-                    }
                 }
             }
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
@@ -160,19 +142,9 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
             for (int o = 16; o > 0; o >>= 1) lm = fmaxf(lm, __shfl_xor_sync(0xffffffffu, lm, o));
             if (lane == 0) atomicMax(gmax + (i >> 5), __float_as_uint(lm));
         }
-        if (sdiag32) {   // the row's wall part of the viscous diagonal block and its FP32 inertia
-#pragma unroll
-            for (int t = 0; t < 6; ++t)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) sd[t] += __shfl_xor_sync(0xffffffffu, sd[t], o);
-            if (lane == 0) {
-                float4* o = reinterpret_cast<float4*>(sdiag32 + (size_t)i * 8);
-                o[0] = make_float4(sd[0], sd[1], sd[2], sd[3]);
-                o[1] = make_float4(sd[4], sd[5], P.inert32[ti], 0.f);
-            }
-        }
-        // - C p over the row's P-neighbours (FP64)
-        double sumv[3] = {(double)sumw[0], (double)sumw[1], (double)sumw[2]};
+        // - C p over the row's P-neighbours (FP64); the wall velocities
+        // follow in k_wall_terms64
+        double sumv[3] = {0.0, 0.0, 0.0};
         const long long pb = nptrP[i];
         const int np = ncp[i];
         for (int a = lane; a < np; a += 32) {
@@ -195,6 +167,73 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
 #pragma unroll
             for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
         }
+    }
+}
+
+// The wall neighbours of every fluid row in FP64 (after k_pair_terms), one
+// thread per row: their viscous terms from the exact minimum image as the
+// assembly of A (main.cpp:2274-2303), summed in FP64 into the wall part of
+// the row's viscous diagonal block (sdiag64; an FP32 copy with the FP32
+// inertia in sdiag32 for the inner operator) and, with the wall velocities,
+// into b (main.cpp:2298-2300).  Wall slots are a few percent of a large
+// case's slots, so FP64 costs little here and keeps the wall part of the
+// outer residual and of b free of FP32 rounding.
+template <int D>
+__global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __restrict__ type, const double* __restrict__ pos,
+                                                      const double* __restrict__ vel, const int* __restrict__ nc,
+                                                      const int* __restrict__ nfc, const long long* __restrict__ nptr,
+                                                      const int* __restrict__ nind, double* __restrict__ bvec,
+                                                      float* __restrict__ sdiag32, double* __restrict__ sdiag64)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.Nf) return;
+    const int ti = type[i];
+    const int n = nc[i], nf = nfc[i];
+    double sd[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // xx xy xz yy yz zz
+    double sw[3] = {0.0, 0.0, 0.0};
+    if (n > nf) {
+        const long long nb = nptr[i];
+        const double rV2 = P.rV * P.rV;
+        double xi[3];
+        load_vec<D>(pos, i, xi);
+        for (int k = nf; k < n; ++k) {
+            const int j = nind[nb + k];
+            if (j == i) continue;
+            double xj[3], q[3];
+            load_vec<D>(pos, j, xj);
+            sep_vec<D>(P, xj, xi, q);
+            const double r2 = norm2_exact<D>(q);
+            if (!(r2 != 0.0 && rV2 - r2 > 0)) continue;
+            const double inv = rsqrt(r2);
+            const double wd = -P.kfv * (P.m2h_rv * (1.0 - (r2 * inv) * P.inv_rv));
+            const double f = P.visc * P.muij[ti][type[j]] * wd * inv;
+            double e[3] = {0.0, 0.0, 0.0}, vj[3];
+#pragma unroll
+            for (int d = 0; d < D; ++d) e[d] = q[d] * inv;
+            load_vec<D>(vel, j, vj);
+            double ev = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) ev += e[d] * vj[d];
+#pragma unroll
+            for (int r = 0; r < D; ++r) sw[r] += f * e[r] * ev;
+            sd[0] += f * e[0] * e[0];
+            sd[1] += f * e[0] * e[1];
+            sd[2] += f * e[0] * e[2];
+            sd[3] += f * e[1] * e[1];
+            sd[4] += f * e[1] * e[2];
+            sd[5] += f * e[2] * e[2];
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] += sw[r];
+    }
+    if (sdiag32) {
+        float4* o = reinterpret_cast<float4*>(sdiag32 + (size_t)i * 8);
+        o[0] = make_float4((float)sd[0], (float)sd[1], (float)sd[2], (float)sd[3]);
+        o[1] = make_float4((float)sd[4], (float)sd[5], P.inert32[ti], 0.f);
+        double2* o64 = reinterpret_cast<double2*>(sdiag64 + (size_t)i * 8);
+        o64[0] = make_double2(sd[0], sd[1]);
+        o64[1] = make_double2(sd[2], sd[3]);
+        o64[2] = make_double2(sd[4], sd[5]);
     }
 }
 
@@ -566,13 +605,73 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
     }
 }
 
-// r = b - A x on the pair-term path, one thread per row: the viscous part in
-// FP32 on x32 from the sliced pair terms (as the inner operator), inertia and
-// C Lambda t (t = C^T x) in FP64; (r, r) -> *out.
+// The viscous part of row i of A x for the FP64 outer residual on the pair
+// path.  The wall part of the diagonal block (FP64 sums of FP64 wall-slot
+// terms) multiplies x_i in FP64; the fluid pairs g (g . (x_i - x_j)) take the
+// FP32 g of the sliced pair terms and the difference of the two-float x
+// (hi + lo, x to about 2^-48 relative), so x enters the viscous part without
+// FP32 rounding: only the pair coefficients are FP32, which bounds the
+// operator's perturbation by about 1e-7 of its viscous part.  The pair terms
+// are summed in FP32 per row (they are differences, small against the row's
+// inertia) and added in FP64.
+template <int D>
+__device__ __forceinline__ void visc_row_resid(int i, int lane, const double* __restrict__ sdiag64,
+                                               const int* __restrict__ nfc, const long long* __restrict__ sptr,
+                                               const int* __restrict__ acol, const float* __restrict__ pes,
+                                               const float* __restrict__ xh, const float* __restrict__ xl,
+                                               const double* __restrict__ x, double* y)
+{
+    double xi[3] = {0.0, 0.0, 0.0};
+    float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        xi[d] = x[(size_t)i * D + d];
+        hi[d] = xh[(size_t)i * D + d];
+        lo[d] = xl[(size_t)i * D + d];
+    }
+    const double2* sp = reinterpret_cast<const double2*>(sdiag64 + (size_t)i * 8);
+    const double2 a = sp[0], b = sp[1], e = sp[2];   // (xx, xy), (xz, yy), (yz, zz)
+    y[0] = a.x * xi[0] + a.y * xi[1] + b.x * xi[2];
+    y[1] = a.y * xi[0] + b.y * xi[1] + e.x * xi[2];
+    y[2] = b.x * xi[0] + e.x * xi[1] + e.y * xi[2];
+    const long long base = sptr[i >> 5];
+    const int* cp = acol + base + lane;
+    const long long vo = base * D + lane;
+    const int n = nfc[i];
+    float ys[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int k = 0; k < n; ++k) {
+        float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[d] = __ldcs(pes + vo + ((long long)k * D + d) * 32);
+        const size_t j = (size_t)__ldcs(cp + (long long)k * 32) * D;
+        float gx = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) gx += g[d] * ((hi[d] - xh[j + d]) + (lo[d] - xl[j + d]));
+#pragma unroll
+        for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) y[d] += (double)ys[d];
+}
+
+// x in two floats: hi = FP32 rounding of x, lo = FP32 rounding of x - hi
+__global__ void k_split_f32(long long n, const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double v = x[k];
+    const float h = (float)v;
+    hi[k] = h;
+    lo[k] = (float)(v - (double)h);
+}
+
+// r = b - A x on the pair-term path, one thread per row: the viscous part as
+// visc_row_resid, inertia and C Lambda t (t = C^T x) in FP64; (r, r) -> *out.
 template <int D>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK)
 k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __restrict__ nfc, const long long* __restrict__ sptr,
-              const int* __restrict__ acol, const float* __restrict__ pes, const float* __restrict__ sdiag,
+              const int* __restrict__ acol, const float* __restrict__ pes, const double* __restrict__ sdiag64,
               const int* __restrict__ ncp, const long long* __restrict__ nptrP, const int* __restrict__ nindP,
               const double* __restrict__ cval, const double* __restrict__ t, const double* __restrict__ x,
               const float* __restrict__ x32, const double* __restrict__ b, double* __restrict__ r,
@@ -581,12 +680,8 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if (i < Nf) {
-        float xi[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int d = 0; d < D; ++d) xi[d] = x32[(size_t)i * D + d];
-        float yv[3];
-        visc_row32<D, false>(i, i & 31, xi, sdiag, nfc, sptr, acol, pes, nullptr, nullptr, x32, yv);
-        double y[3] = {(double)yv[0], (double)yv[1], (double)yv[2]};
+        double y[3];
+        visc_row_resid<D>(i, i & 31, sdiag64, nfc, sptr, acol, pes, x32, x32 + (size_t)Nf * D, x, y);
         const long long pb = nptrP[i];
         const int np = ncp[i];
         for (int a = 0; a < np; ++a) {
@@ -1115,10 +1210,20 @@ static int grow_pairs(mph_case* c, long long slots)
 // its FP32 viscous part is accurate enough while FP32 rounding of that part
 // (about 1e-7 of it, the part being visc_ratio of the inertia) stays below
 // 1e-2 of the outer tolerance.
+// The factored form holds its viscous pair coefficients in FP32, which moves
+// A by about 1e-7 of its viscous part (visc_ratio of the inertia): it is used
+// while that stays two orders under the 1e-6 velocity accuracy of the mixed
+// form.  The pair path's residual (FP64 wall terms, two-float x) carries no
+// other FP32 rounding, so it also serves outer tolerances below that bound
+// (refinement to 1e-10); the warp-per-row residual of the FP32-block path
+// rounds x to FP32 and is kept to tolerances above it.
 bool factored_applies(const mph_case* c)
 {
-    return c->precision == MPH_PRECISION_MIXED && c->factored && 2.0 * c->dp.rP < c->dp.maxR &&
-           1.0e-7 * c->visc_ratio < 1.0e-2 * c->tol_outer;
+    if (!(c->precision == MPH_PRECISION_MIXED && c->factored && 2.0 * c->dp.rP < c->dp.maxR)) return false;
+    const double pert = 1.0e-7 * c->visc_ratio;
+    if (!(pert < 1.0e-8)) return false;
+    const bool pair_path = !c->inner_blocks && c->visc_nonneg;
+    return pair_path || pert < 1.0e-2 * c->tol_outer;
 }
 
 int launch_pair_terms(mph_case* c)
@@ -1130,7 +1235,9 @@ int launch_pair_terms(mph_case* c)
     MPH_CUDA(cudaStreamSynchronize(c->stream));
     MPH_TRY(grow_pairs(c, slots));
     if (!d.tct) MPH_CUDA(cudaMalloc((void**)&d.tct, (size_t)(P.N + 1) * sizeof(double)));
-    if (!d.x32) MPH_CUDA(cudaMalloc((void**)&d.x32, (size_t)P.Nf * c->dim * sizeof(float)));
+    // FP32 copy of x and, after it, the FP32 remainders x - hi (two-float x
+    // of the pair-path residual)
+    if (!d.x32) MPH_CUDA(cudaMalloc((void**)&d.x32, (size_t)P.Nf * c->dim * 2 * sizeof(float)));
     if (!d.tct32) MPH_CUDA(cudaMalloc((void**)&d.tct32, (size_t)(P.N + 1) * sizeof(float)));
     long long ncv = 0;   // C values of the fluid rows, FP32 copy for the inner operator
     MPH_CUDA(cudaMemcpyAsync(&ncv, d.nptrP + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
@@ -1145,10 +1252,13 @@ int launch_pair_terms(mph_case* c)
     }
     { k_cval_f32<<<grid_for(ncv, 256), 256, 0, c->stream>>>(ncv, d.cval, d.cval32); MPH_COUNT_LAUNCH(); }
     float* sdiag = nullptr;
+    double* sdiag64 = nullptr;
     float* cvl = nullptr;
     unsigned* gmax = nullptr;
     if (c->step_pairs) {   // FP32 inner operator on the pair terms
         if (!d.sdiag32) MPH_CUDA(cudaMalloc((void**)&d.sdiag32, (size_t)P.Nf * 8 * sizeof(float)));
+        if (!d.sdiag64) MPH_CUDA(cudaMalloc((void**)&d.sdiag64, (size_t)P.Nf * 8 * sizeof(double)));
+        sdiag64 = d.sdiag64;
         MPH_TRY(grow_f(&d.cvl32, &d.cap_cvl32, ncv));
         sdiag = d.sdiag32;
         cvl = d.cvl32;
@@ -1157,12 +1267,15 @@ int launch_pair_terms(mph_case* c)
         gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
     }
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
+    const unsigned gw = grid_for(P.Nf, 256);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl, gmax); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax); MPH_COUNT_LAUNCH(); }
+        { k_wall_terms64<2><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, sdiag, cvl, gmax); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax); MPH_COUNT_LAUNCH(); }
+        { k_wall_terms64<3><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }
@@ -1303,20 +1416,21 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     const unsigned gt = grid_for(P.N, 256);
     const unsigned g = std::min<long long>(((long long)P.Nf + kPairWarps - 1) / kPairWarps, kReduceBlocks);
     const long long nv = (long long)P.Nf * c->dim;
-    { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
     if (c->step_pairs) {
+        { k_split_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32, d.x32 + nv); MPH_COUNT_LAUNCH(); }
         const unsigned gr = grid_for(P.Nf, MPH_PAIR_BLOCK);
         if (c->dim == 2) {
             { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<2><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+            { k_resid_pairs<2><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         } else {
             { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<3><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag32, d.ncp, d.nptrP,
+            { k_resid_pairs<3><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         }
         return;
     }
+    { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
     if (c->dim == 2) {
         { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
         { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,

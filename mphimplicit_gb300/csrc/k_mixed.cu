@@ -213,10 +213,14 @@ __global__ void k_store_velocity_m(int Nf, const double* __restrict__ x, double*
     vel[(size_t)(k / D) * (D == 2 ? 2 : 4) + k % D] = x[k];
 }
 
+// x0 = v* - F/m dt (= v_n, the reference's start, main.cpp:4299-4308) and
+// (b, b) -> *out.  With vprev (option "extrapolate"): x0 = 2 v_n - v_{n-1}
+// where `have` (the history is valid), and v_n is stored as the next step's
+// v_{n-1}.
 template <int D>
 __global__ void k_x0(int Nf, const int* __restrict__ type, const double* __restrict__ vel, const double* __restrict__ force,
-                     const double* __restrict__ b, double* __restrict__ x, DevParams P, double* __restrict__ partials,
-                     unsigned* __restrict__ counter, double* __restrict__ out)
+                     const double* __restrict__ b, double* __restrict__ x, DevParams P, double* __restrict__ vprev, int have,
+                     double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out)
 {
     double acc = 0.0;
     const int n = Nf * D;
@@ -224,7 +228,13 @@ __global__ void k_x0(int Nf, const int* __restrict__ type, const double* __restr
         const int i = k / D, r = k % D;
         const double m = P.density[type[i]] * P.vol;
         const int VSD = D == 2 ? 2 : 4;
-        x[k] = vel[(size_t)i * VSD + r] - force[(size_t)i * VSD + r] / m * P.dt;
+        const double vn = vel[(size_t)i * VSD + r] - force[(size_t)i * VSD + r] / m * P.dt;
+        double x0 = vn;
+        if (vprev) {
+            if (have) x0 = 2.0 * vn - vprev[(size_t)i * VSD + r];
+            vprev[(size_t)i * VSD + r] = vn;
+        }
+        x[k] = x0;
         acc += b[k] * b[k];
     }
     reduce_finalize(acc, partials, counter, out);
@@ -295,7 +305,16 @@ static int mixed_solve_t(mph_case* c)
     V* u32 = vec + 6 * (size_t)n;
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
     MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
-    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
+    if (c->extrapolate && !d.vprev) {
+        const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
+        MPH_CUDA(cudaMalloc((void**)&d.vprev, nvs * sizeof(double)));
+        MPH_CUDA(cudaMalloc((void**)&d.vprev_alt, nvs * sizeof(double)));
+        c->prev_valid = false;
+    }
+    double* vprev = c->extrapolate ? d.vprev : nullptr;
+    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, c->prev_valid ? 1 : 0,
+                                             part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
+    c->prev_valid = vprev != nullptr;
     // FP64 residual: from the assembled FP64 blocks, or in factored form
     auto residual = [&]() {
         if (c->step_factored) {

@@ -183,6 +183,17 @@ __global__ void k_permute(int N, const int* __restrict__ perm, const int* __rest
     }
 }
 
+// the previous step's start velocity follows the particles through the sort
+template <int D>
+__global__ void k_permute_vec(int N, const int* __restrict__ perm, const double* __restrict__ v, double* __restrict__ v2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double a[3];
+    load_vec<D>(v, perm[i], a);
+    store_vec<D>(v2, i, a);
+}
+
 __global__ void k_fluid_bbox(const int* __restrict__ bucket, DevParams P, int* __restrict__ bbox)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,6 +271,11 @@ void launch_cell_ranges_and_permute(mph_case* c)
     std::swap(c->d.type, c->d.type_alt);
     std::swap(c->d.pos, c->d.pos_alt);
     std::swap(c->d.vel, c->d.vel_alt);
+    if (c->prev_valid && c->d.vprev) {
+        if (c->dim == 2) { k_permute_vec<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev, c->d.vprev_alt); MPH_COUNT_LAUNCH(); }
+        else { k_permute_vec<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev, c->d.vprev_alt); MPH_COUNT_LAUNCH(); }
+        std::swap(c->d.vprev, c->d.vprev_alt);
+    }
 }
 
 void launch_fluid_bbox(mph_case* c)

@@ -110,6 +110,13 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->cell_assembly = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "extrapolate") {
+        if (c->precision != MPH_PRECISION_MIXED && value != 0.0)
+            return mph::fail(MPH_ERR_ARG, "option extrapolate: mixed form only (the FP64 form starts from v_n as the reference)");
+        c->extrapolate = value != 0.0;
+        c->prev_valid = false;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

@@ -670,11 +670,11 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags, d.ct_tmp,
                     (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
-                    (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
+                    (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.sdiag64, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
                     (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
                     (void*)d.grec16, (void*)d.pscale, (void*)d.uniq, (void*)d.ucount,
                     (void*)d.ctuniq, (void*)d.ctucount, (void*)d.wkey, (void*)d.wval, (void*)d.ccell,
-                    (void*)d.io3, d.scan_tmp})
+                    (void*)d.io3, (void*)d.vprev, (void*)d.vprev_alt, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

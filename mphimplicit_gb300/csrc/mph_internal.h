@@ -153,9 +153,11 @@ struct DeviceState {
     long long cap_ctucount = 0;
     int* ccell = nullptr;              // packed cell coordinates of every particle (pair path)
     double* io3 = nullptr;             // host-layout staging, 2 x N x 3 doubles (state upload, field download)
+    double *vprev = nullptr, *vprev_alt = nullptr;   // mixed form, option "extrapolate": the previous step's start velocity (N x VS)
     int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
     float* wval = nullptr;             // the sums of C_jk over each (level-0 stencils of the pair path)
     float* sdiag32 = nullptr;
+    double* sdiag64 = nullptr;         // FP64 wall part of the viscous diagonal block per fluid row (8 doubles: 6 used)
     float* cvl32 = nullptr;
     long long cap_cvl32 = 0;
     long long *psptr = nullptr, *ctsptr = nullptr;
@@ -237,6 +239,8 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
+    bool extrapolate = false;           // mixed form: CR start x0 = 2 v_n - v_{n-1} (else the reference's v_n)
+    bool prev_valid = false;            // vprev holds v_{n-1} in the current particle order
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms

@@ -120,6 +120,7 @@ inline unsigned long long graph_signature(const mph_case* c, double tol, int cap
     d.pos = d.vel = d.force = d.pos_alt = d.vel_alt = nullptr;
     d.pos32 = nullptr;
     d.id = d.id_alt = d.type_alt = d.type = nullptr;
+    d.vprev = d.vprev_alt = nullptr;
     h = fnv1a(h, &d, sizeof(d));
     h = fnv1a(h, &c->dp, sizeof(c->dp));
     if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));

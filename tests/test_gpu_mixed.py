@@ -93,7 +93,9 @@ def test_mixed_1e10_within_1e6_of_tight_fp64(engine_lib, oracle_built, case, mod
     o = oracle_built.Oracle(params, parts, dim, threads=1)
     o.init()
     o.set_tolerance(1e-12)
-    o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build(); o.solve()
+    o.step_begin(); o.cellsort(); o.neighbors(); o.explicit(); o.assemble(); o.mg_build()
+    ptr, ind, val, bo = o.array("CsrPtrA"), o.array("CsrIndA"), o.array("CsrCofA"), o.array("VectorB")
+    o.solve()
     nf = int(o.scalars()["FluidParticleEnd"])
     vo = vec_proj(o.array("Velocity"), dim)[:nf]
     g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
@@ -107,8 +109,14 @@ def test_mixed_1e10_within_1e6_of_tight_fp64(engine_lib, oracle_built, case, mod
     assert np.array_equal(g.export("ParticleIndex"), o.array("ParticleIndex"))
     vg = vec_proj(g.export("Velocity"), dim)[:nf]
     err = float(np.linalg.norm(vg - vo) / np.linalg.norm(vo))
-    print(f"{name} {MODE_IDS[MODES.index(mode)]}: mixed 1e-10 vs FP64 oracle 1e-12: {err:.3e}")
+    # residual of the mixed solution in the oracle's assembled FP64 system
+    x = np.zeros((nf, 3))
+    x[:, :dim] = vg
+    res = oracle_residual(ptr, ind, val, bo, x.ravel())
+    print(f"{name} {MODE_IDS[MODES.index(mode)]} (inner form {s['inner_form']}): mixed 1e-10 vs FP64 oracle 1e-12: "
+          f"{err:.3e}; ||b - A x||/||b|| in the oracle's system {res:.3e}")
     assert err <= 1e-6, err
+    assert res <= 2e-9, res
     f = engine.Case(params, parts, dim)
     f.set_solver(1e-12, 1e-3, 50)
     for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"):
