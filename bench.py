@@ -522,8 +522,9 @@ def main():
     ap.add_argument("--extra-sweeps", type=int, default=0, help="mixed form: extra level-0 smoothing sweeps")
     ap.add_argument("--inner-blocks", type=int, default=-1, choices=[-1, 0, 1],
                     help="mixed form: inner operator on FP32 blocks (1) or sliced pair terms (0); -1 keeps the engine default")
-    ap.add_argument("--extrapolate", type=int, default=0, choices=[0, 1],
-                    help="mixed form: start each CR solve from 2 v_n - v_(n-1) instead of v_n")
+    ap.add_argument("--extrapolate", type=int, default=2, choices=[0, 1, 2],
+                    help="mixed form: start each CR solve from the linear (1) or quadratic (2) extrapolation of the "
+                         "last steps' start velocities instead of v_n (0)")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -598,7 +599,7 @@ def run_single(args, dist, rank, world, local):
         if profile:
             c.profile(True)
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-        its = []
+        its, outs = [], []
         l0 = engine.launch_count()
         with (clocks if clocks is not None else _Null()):
             torch.cuda.synchronize()
@@ -606,17 +607,21 @@ def run_single(args, dist, rank, world, local):
             for k in range(steps):
                 c.step(1)
                 evs[k + 1].record(stream)
-                its.append(c.solve_stats()["iter"])
+                ss = c.solve_stats()
+                its.append(ss["iter"])
+                outs.append(ss["outer"])
             torch.cuda.synchronize()
         launches = engine.launch_count() - l0
         if dist:
             dist.barrier()
+        timed.outer = outs
         return [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)], its, launches
 
     case = make(prec, tol)
     N, Nf = case.count, case.fluid_count
     clk = Clocks(local)
     step_ms, iters, launches = timed(case, args.steps, args.warmup, clk, profile=True)
+    outer_main = list(timed.outer)
     total_s = sum(step_ms) / 1000.0
     prof = case.profile_read()
     case.profile(False)
@@ -723,7 +728,10 @@ def run_single(args, dist, rank, world, local):
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (the pair terms alone exceed 129 MB by ~50x)",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-                   "outer_tol": tol, "cr_iterations": iters,
+                   "outer_tol": tol, "cr_iterations": iters, "outer_refinements": outer_main,
+                   "cr_start": {0: "v_n (the reference's)", 1: "linear extrapolation of the last start velocities",
+                                2: "quadratic extrapolation of the last start velocities"}[args.extrapolate]
+                   if prec == PRECISION_MIXED else "v_n (the reference's)",
                    "inner_row_blocks": {"staged": st.get("inner_local_blocks"), "gathering": st.get("inner_gather_blocks"),
                                         "ct_blocks_staging_s": st.get("inner_ct_local_blocks"),
                                         "mean_distinct_cols": (st["inner_local_cols"] / st["inner_local_blocks"]

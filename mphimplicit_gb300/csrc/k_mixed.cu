@@ -214,13 +214,15 @@ __global__ void k_store_velocity_m(int Nf, const double* __restrict__ x, double*
 }
 
 // x0 = v* - F/m dt (= v_n, the reference's start, main.cpp:4299-4308) and
-// (b, b) -> *out.  With vprev (option "extrapolate"): x0 = 2 v_n - v_{n-1}
-// where `have` (the history is valid), and v_n is stored as the next step's
-// v_{n-1}.
+// (b, b) -> *out.  With a history (option "extrapolate", `have` previous
+// start velocities in vprev: v_{n-1} at [0, nvs), v_{n-2} at [nvs, 2 nvs)),
+// x0 extrapolates the start velocities of the last steps: linearly,
+// 2 v_n - v_{n-1}, or quadratically, 3 v_n - 3 v_{n-1} + v_{n-2} (order =
+// min(have, maximum order)); the history then shifts by one step.
 template <int D>
 __global__ void k_x0(int Nf, const int* __restrict__ type, const double* __restrict__ vel, const double* __restrict__ force,
-                     const double* __restrict__ b, double* __restrict__ x, DevParams P, double* __restrict__ vprev, int have,
-                     double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out)
+                     const double* __restrict__ b, double* __restrict__ x, DevParams P, double* __restrict__ vprev, size_t nvs,
+                     int have, int keep, double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out)
 {
     double acc = 0.0;
     const int n = Nf * D;
@@ -228,11 +230,15 @@ __global__ void k_x0(int Nf, const int* __restrict__ type, const double* __restr
         const int i = k / D, r = k % D;
         const double m = P.density[type[i]] * P.vol;
         const int VSD = D == 2 ? 2 : 4;
-        const double vn = vel[(size_t)i * VSD + r] - force[(size_t)i * VSD + r] / m * P.dt;
+        const size_t a = (size_t)i * VSD + r;
+        const double vn = vel[a] - force[a] / m * P.dt;
         double x0 = vn;
         if (vprev) {
-            if (have) x0 = 2.0 * vn - vprev[(size_t)i * VSD + r];
-            vprev[(size_t)i * VSD + r] = vn;
+            const double v1 = have >= 1 ? vprev[a] : 0.0;
+            if (have >= 2) x0 = 3.0 * vn - 3.0 * v1 + vprev[nvs + a];
+            else if (have == 1) x0 = 2.0 * vn - v1;
+            if (keep >= 2) vprev[nvs + a] = v1;
+            vprev[a] = vn;
         }
         x[k] = x0;
         acc += b[k] * b[k];
@@ -305,16 +311,17 @@ static int mixed_solve_t(mph_case* c)
     V* u32 = vec + 6 * (size_t)n;
     MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
     MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
+    const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
     if (c->extrapolate && !d.vprev) {
-        const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
-        MPH_CUDA(cudaMalloc((void**)&d.vprev, nvs * sizeof(double)));
-        MPH_CUDA(cudaMalloc((void**)&d.vprev_alt, nvs * sizeof(double)));
-        c->prev_valid = false;
+        MPH_CUDA(cudaMalloc((void**)&d.vprev, 2 * nvs * sizeof(double)));
+        MPH_CUDA(cudaMalloc((void**)&d.vprev_alt, 2 * nvs * sizeof(double)));
+        c->prev_valid = 0;
     }
     double* vprev = c->extrapolate ? d.vprev : nullptr;
-    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, c->prev_valid ? 1 : 0,
+    const int have = std::min(c->prev_valid, c->extrapolate);
+    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, nvs, have, c->extrapolate,
                                              part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
-    c->prev_valid = vprev != nullptr;
+    c->prev_valid = vprev ? std::min(c->prev_valid + 1, c->extrapolate) : 0;
     // FP64 residual: from the assembled FP64 blocks, or in factored form
     auto residual = [&]() {
         if (c->step_factored) {

@@ -272,8 +272,11 @@ void launch_cell_ranges_and_permute(mph_case* c)
     std::swap(c->d.pos, c->d.pos_alt);
     std::swap(c->d.vel, c->d.vel_alt);
     if (c->prev_valid && c->d.vprev) {
-        if (c->dim == 2) { k_permute_vec<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev, c->d.vprev_alt); MPH_COUNT_LAUNCH(); }
-        else { k_permute_vec<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev, c->d.vprev_alt); MPH_COUNT_LAUNCH(); }
+        const size_t nvs = (size_t)N * vs_of(c->dim);
+        for (int h = 0; h < c->prev_valid; ++h) {
+            if (c->dim == 2) { k_permute_vec<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev + h * nvs, c->d.vprev_alt + h * nvs); MPH_COUNT_LAUNCH(); }
+            else { k_permute_vec<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.vprev + h * nvs, c->d.vprev_alt + h * nvs); MPH_COUNT_LAUNCH(); }
+        }
         std::swap(c->d.vprev, c->d.vprev_alt);
     }
 }

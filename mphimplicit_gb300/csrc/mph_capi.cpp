@@ -113,8 +113,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
     if (std::string(name) == "extrapolate") {
         if (c->precision != MPH_PRECISION_MIXED && value != 0.0)
             return mph::fail(MPH_ERR_ARG, "option extrapolate: mixed form only (the FP64 form starts from v_n as the reference)");
-        c->extrapolate = value != 0.0;
-        c->prev_valid = false;
+        if (!(value == 0.0 || value == 1.0 || value == 2.0))
+            return mph::fail(MPH_ERR_ARG, "option extrapolate: 0 (the reference's start), 1 (linear) or 2 (quadratic)");
+        c->extrapolate = (int)value;
+        c->prev_valid = 0;
         return MPH_OK;
     }
     if (std::string(name) == "graphs") {

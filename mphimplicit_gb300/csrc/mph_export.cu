@@ -387,7 +387,7 @@ int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_c
     if (wall_center) std::memcpy(&c->wallC[0][0], wall_center, sizeof(c->wallC));
     c->time = parts->time;
     c->densa_valid = false;
-    c->prev_valid = false;   // a state from outside has no velocity history
+    c->prev_valid = 0;   // a state from outside has no velocity history
     c->fB = 0;
     c->fE = nf;
     c->wB = nf;

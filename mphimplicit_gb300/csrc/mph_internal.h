@@ -153,7 +153,8 @@ struct DeviceState {
     long long cap_ctucount = 0;
     int* ccell = nullptr;              // packed cell coordinates of every particle (pair path)
     double* io3 = nullptr;             // host-layout staging, 2 x N x 3 doubles (state upload, field download)
-    double *vprev = nullptr, *vprev_alt = nullptr;   // mixed form, option "extrapolate": the previous step's start velocity (N x VS)
+    double *vprev = nullptr, *vprev_alt = nullptr;   // mixed form, option "extrapolate": start velocities of the two previous
+                                                     // steps (2 x N x VS: v_{n-1}, then v_{n-2})
     int* wkey = nullptr;               // per particle k, kWBins cells of its transposed P-list and
     float* wval = nullptr;             // the sums of C_jk over each (level-0 stencils of the pair path)
     float* sdiag32 = nullptr;
@@ -239,8 +240,9 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
-    bool extrapolate = false;           // mixed form: CR start x0 = 2 v_n - v_{n-1} (else the reference's v_n)
-    bool prev_valid = false;            // vprev holds v_{n-1} in the current particle order
+    int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
+                                        // (1: 2 v_n - v_{n-1}; 2: 3 v_n - 3 v_{n-1} + v_{n-2}; 0: the reference's v_n)
+    int prev_valid = 0;                 // start velocities of previous steps held in vprev (current particle order)
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
