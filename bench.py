@@ -525,6 +525,8 @@ def main():
     ap.add_argument("--extrapolate", type=int, default=2, choices=[0, 1, 2],
                     help="mixed form: start each CR solve from the linear (1) or quadratic (2) extrapolation of the "
                          "last steps' start velocities instead of v_n (0)")
+    ap.add_argument("--dense-coarse", type=int, default=1, choices=[0, 1],
+                    help="mixed form: solve the V-cycle's first one-block coarse level (<= 224 rows) exactly")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -586,6 +588,7 @@ def run_single(args, dist, rank, world, local):
             if args.inner_blocks >= 0:
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
+            c.set_option("dense_coarse", args.dense_coarse)
         return c
 
     def timed(c, steps, warmup, clocks=None, profile=False):
@@ -713,6 +716,7 @@ def run_single(args, dist, rank, world, local):
             if args.inner_blocks >= 0:
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
+            c.set_option("dense_coarse", args.dense_coarse)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,
                                   extra=True, pre=args.warmup, setup=setup)
     max_err = max(errs["mixed"]) if errs else None

@@ -281,7 +281,7 @@ int mixed_prepare(mph_case* c)
     { k_convert<double, float><<<grid_for(c->mg_cof_total, 256), 256, 0, st>>>(c->mg_cof_total, d.mg_cof, d.mg_cof32); MPH_COUNT_LAUNCH(); }
     { k_convert<double, float><<<grid_for(c->mg_rows_total, 256), 256, 0, st>>>(c->mg_rows_total, d.mg_invd, d.mg_invd32); MPH_COUNT_LAUNCH(); }
     { k_convert<double, float><<<grid_for(nv, 256), 256, 0, st>>>(nv, d.invDiag, d.v32 + 7 * nv); MPH_COUNT_LAUNCH(); }
-    return MPH_OK;
+    return mixed_dense_coarse(c);
 }
 
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);

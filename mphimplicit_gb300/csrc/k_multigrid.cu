@@ -38,6 +38,7 @@ namespace mph {
 constexpr int kCtaRows = 8192;
 constexpr int kCtaThreads = 1024;
 constexpr int kClusterCtas = 8;
+constexpr int kDenseRows = 224;   // dense coarse level of the mixed form: n x n floats in one block's shared memory
 
 struct LevelK {
     int mn[3], mx[3], cnt[3], st[3];
@@ -450,7 +451,55 @@ struct CoarseArgs {
     T* Sb[kMaxLevels];
     T* R[kMaxLevels];                 // R[first-1] holds the finer level's residual
     T* Sfine;                         // current S of level first-1 (receives the prolongation)
+    int dense;                        // >= 0: this level (one block's size) is solved exactly with dinv
+    const T* dinv;                    // its dense inverse, n x n (symmetric)
 };
+
+// Dense inverse of one coarse level's matrix (mixed form, FP32), one block:
+// the level's stencil rows into an n x n matrix in shared memory (a thread a
+// row, its entries in stencil order, so the duplicated columns of a wrapped
+// axis add up in a fixed order), then Gauss-Jordan elimination in place
+// without pivoting, which is stable for the symmetric positive definite
+// Galerkin level matrices.  n <= kDenseRows.
+template <int D>
+__global__ void __launch_bounds__(1024) k_mg_dense_inv(LevelK L, const float* __restrict__ cofT, float* __restrict__ inv)
+{
+    extern __shared__ float dn_smem[];
+    const int n = L.rows;
+    float* a = dn_smem;          // n x n, row-major
+    float* colk = dn_smem + n * n;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) a[t] = 0.f;
+    __syncthreads();
+    for (int row = threadIdx.x; row < n; row += blockDim.x) {
+        int p[3];
+        grid_coords(L, row / D, p);
+        int e = 0;
+        for (int ix = 0; ix < L.st[0]; ++ix)
+            for (int iy = 0; iy < L.st[1]; ++iy)
+                for (int iz = 0; iz < L.st[2]; ++iz) {
+                    const int jg = stencil_col(L, p, ix, iy, iz);
+                    for (int sD = 0; sD < D; ++sD, ++e) a[(size_t)row * n + jg * D + sD] += cofT[(size_t)e * n + row];
+                }
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        // a cell without fluid particles has a zero row and column: it stays
+        // zero in the inverse (the pseudo-inverse on the occupied cells)
+        const float akk = a[(size_t)k * n + k];
+        const float pk = akk != 0.f ? 1.f / akk : 0.f;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = i == k ? 0.f : a[(size_t)i * n + k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) a[(size_t)k * n + j] = (j == k ? 1.f : a[(size_t)k * n + j]) * pk;
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t - i * n;
+            if (i == k) continue;
+            a[t] = (j == k ? 0.f : a[t]) - colk[i] * a[(size_t)k * n + j];
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) inv[t] = a[t];
+}
 
 template <int D, typename T>
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCtaThreads)
@@ -517,11 +566,27 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
         const LevelK& S_ = A.L[l - 1];
         for (int row = t0; row < S_.rows; row += nt) cur[l - 1][row] = cur[l - 1][row] + cur[l][row_parent<D>(S_, A.L[l], row)];
     };
+    // restriction into the dense level and its exact solve S = A^-1 Q (the
+    // inverse is symmetric: column `row` read across the threads)
+    auto dense_solve = [&](int l, int t0, int nt, auto sync) {
+        const LevelK& L = A.L[l];
+        for (int row = t0; row < L.rows; row += nt) A.Q[l][row] = row_restrict<D, T>(A.L[l - 1], L, A.R[l - 1], row);
+        sync();
+        for (int row = t0; row < L.rows; row += nt) {
+            T v = 0;
+            for (int c = 0; c < L.rows; ++c) v += A.dinv[(size_t)c * L.rows + row] * A.Q[l][c];
+            cur[l][row] = v;
+        }
+        sync();
+    };
     for (int l = A.first; l < narrow; ++l) down(l, tid, nth, csync);
     if (cluster.block_rank() == 0 && narrow < A.depth) {
         const int t0 = threadIdx.x, nt = blockDim.x;
-        for (int l = narrow; l < A.depth; ++l) down(l, t0, nt, bsync);
-        for (int l = A.depth - 1; l > narrow; --l) {
+        // levels narrow .. bottom-1 smoothed; the dense level (if any) solved exactly
+        const int bottom = A.dense >= 0 ? A.dense : A.depth;
+        for (int l = narrow; l < bottom; ++l) down(l, t0, nt, bsync);
+        if (A.dense >= 0) dense_solve(A.dense, t0, nt, bsync);
+        for (int l = bottom < A.depth ? bottom : A.depth - 1; l > narrow; --l) {
             prolong(l, t0, nt);
             bsync();
             for (int k = 0; k < 3; ++k) jacobi(l - 1, t0, nt, bsync);   // post-smoothing (3 updates)
@@ -618,6 +683,14 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
             A.R[l] = Rp + ov(l);
         }
         A.Sfine = cur[first - 1];
+        A.dense = -1;
+        A.dinv = nullptr;
+        if constexpr (std::is_same<T, float>::value) {
+            if (c->dense_level >= first) {
+                A.dense = c->dense_level;
+                A.dinv = c->d.mg_dinv32;
+            }
+        }
         { k_mg_small_levels<D, T><<<kClusterCtas, kCtaThreads, 0, st>>>(A, flags); MPH_COUNT_LAUNCH(); }
     }
     // up, grid-wide levels: the block kernel already prolongated into level
@@ -638,6 +711,45 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     const int blocks = std::min<int>(grid_for(c->dp.Nf, 256), kReduceBlocks);
     { k_mg_g2p_dot<D, T, TQ><<<blocks, 256, 0, st>>>(c->dp, L[0], c->d.key, invDiag, q, cur[0], u, c->d.partials,
                                                      (unsigned*)(c->d.flags + kFlagCounter), dot_out, flags); MPH_COUNT_LAUNCH(); }
+}
+
+// The mixed form's exact coarse solve: the first level handled by one block
+// of the small-level kernel (at most kCtaThreads rows) that also has at most
+// kDenseRows rows is solved with its dense FP32 inverse, built each step
+// after the level stencils, instead of the reference's smoothing of it and
+// the levels below (c->dense_level = -1: none, the reference's V-cycle).
+int mixed_dense_coarse(mph_case* c)
+{
+    c->dense_level = -1;
+    if (!c->dense_coarse) return MPH_OK;
+    int first = c->depth;
+    for (int l = 1; l < c->depth; ++l)
+        if (c->lv[l].rows <= kCtaRows) { first = l; break; }
+    int lev = -1;
+    for (int l = first; l < c->depth; ++l)
+        if (c->lv[l].rows <= kDenseRows) { lev = l; break; }
+    if (lev < 0) return MPH_OK;
+    const int n = c->lv[lev].rows;
+    if ((long long)n * n > c->d.cap_mg_dinv32) {
+        if (c->d.mg_dinv32) cudaFree(c->d.mg_dinv32);
+        c->d.mg_dinv32 = nullptr;
+        c->d.cap_mg_dinv32 = 0;
+        MPH_CUDA(cudaMalloc((void**)&c->d.mg_dinv32, (size_t)kDenseRows * kDenseRows * sizeof(float)));
+        c->d.cap_mg_dinv32 = (long long)kDenseRows * kDenseRows;
+    }
+    const int smem = (n * n + n) * (int)sizeof(float);
+    const LevelK L = level_k(c, lev);
+    const float* cof = c->d.mg_cof32 + c->lv[lev].off_cof;
+    if (c->dim == 2) {
+        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        { k_mg_dense_inv<2><<<1, 1024, smem, c->stream>>>(L, cof, c->d.mg_dinv32); MPH_COUNT_LAUNCH(); }
+    } else {
+        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        { k_mg_dense_inv<3><<<1, 1024, smem, c->stream>>>(L, cof, c->d.mg_dinv32); MPH_COUNT_LAUNCH(); }
+    }
+    MPH_CUDA(cudaGetLastError());
+    c->dense_level = lev;
+    return MPH_OK;
 }
 
 // FP32 V-cycle of the mixed form: the FP32 copies of the level stencils and

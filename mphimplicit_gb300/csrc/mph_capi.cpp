@@ -119,6 +119,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->prev_valid = 0;
         return MPH_OK;
     }
+    if (std::string(name) == "dense_coarse") {
+        c->dense_coarse = value != 0.0;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

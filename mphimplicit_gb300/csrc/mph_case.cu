@@ -669,7 +669,7 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_cof, (void*)d.mg_invd, (void*)d.mg_q, (void*)d.mg_s, (void*)d.mg_r, (void*)d.mg_res, (void*)d.mg_cof32,
                     (void*)d.mg_q32, (void*)d.mg_s32, (void*)d.mg_r32, (void*)d.mg_res32, (void*)d.v32,
                     (void*)d.ct_cnt, (void*)d.ct_ptr, (void*)d.ct_j, (void*)d.ct_v, (void*)d.cell_flags, d.ct_tmp,
-                    (void*)d.mg_invd32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
+                    (void*)d.mg_invd32, (void*)d.mg_dinv32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
                     (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.sdiag64, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
                     (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
                     (void*)d.grec16, (void*)d.pscale, (void*)d.uniq, (void*)d.ucount,

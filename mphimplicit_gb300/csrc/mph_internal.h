@@ -170,6 +170,8 @@ struct DeviceState {
     double *mg_cof = nullptr, *mg_invd = nullptr;
     double *mg_q = nullptr, *mg_s = nullptr, *mg_r = nullptr, *mg_res = nullptr;   // Q, S ping-pong pair, residual
     float *mg_cof32 = nullptr, *mg_invd32 = nullptr;
+    float* mg_dinv32 = nullptr;     // mixed form: dense inverse of the exactly solved coarse level
+    long long cap_mg_dinv32 = 0;
     float *mg_q32 = nullptr, *mg_s32 = nullptr, *mg_r32 = nullptr, *mg_res32 = nullptr;
     float* v32 = nullptr;           // mixed form: 7 FP32 CR vectors + FP32 D^-1, each D*Nf
     long long cap_mg_cof = 0, cap_mg_vec = 0, cap_mg_cof32 = 0, cap_mg_vec32 = 0;
@@ -240,6 +242,8 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
+    bool dense_coarse = true;           // mixed form: solve the first one-block coarse level of <= 224 rows exactly
+    int dense_level = -1;               // this step's exactly solved level (-1: none)
     int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
                                         // (1: 2 v_n - v_{n-1}; 2: 3 v_n - 3 v_{n-1} + v_{n-2}; 0: the reference's v_n)
     int prev_valid = 0;                 // start velocities of previous steps held in vprev (current particle order)
@@ -357,6 +361,7 @@ void launch_mg_invd(mph_case* c);
 int run_cr_solve(mph_case* c);
 int noalloc_prepare(int dev);   // k_resid_noalloc.cu: reserve the allocation-free check's array on this device
 int run_mixed_solve(mph_case* c);
+int mixed_dense_coarse(mph_case* c);   // k_multigrid.cu: this step's dense coarse level of the mixed V-cycle
 bool mixed_available();
 
 }  // namespace mph
