@@ -10,8 +10,15 @@ Also records the reference's own 3D sample case (results3d/.../box.grid,
 box.data) and its generator input (box.boid), so the case generator can be
 checked against the reference pre-processor byte for byte.
 
+Also runs the reference executables themselves (main() and its time loop,
+compiled into oracle/_ref/Mph_gcc and Mph_gcc3d) on a short 2D and 3D case
+with chosen output intervals, and stores their input files, every .prof and
+.vtk frame they write (output.vtk included) and the output lines of their
+log: the fixtures of the command-line and frame-writer parity tests.
+
 Run in the development container (needs the reference checkout):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py cli        # the executable fixtures only
 """
 from __future__ import annotations
 
@@ -143,8 +150,56 @@ def parse_boid(path):
     return head, cubs
 
 
+def cli_cases():
+    """(name, dim, params, particles) of the executable fixtures: the 2D dam
+    and the 3D cube parity cases, 10 steps, a .prof frame every 3 steps and a
+    .vtk frame every 4."""
+    import dataclasses
+    out = []
+    for name, dim, p, parts in small_cases():
+        if name not in ("dam2d", "cube3d"):
+            continue
+        q = dataclasses.replace(p, end_time=9 * p.dt, output_interval=3 * p.dt, vtk_output_interval=4 * p.dt)
+        out.append((name, dim, q, parts))
+    return out
+
+
+def run_cli(name, dim, params, parts):
+    """Run the reference executable (one thread) in a scratch directory and
+    collect its inputs, frames and log output lines."""
+    import subprocess
+    import tempfile
+    exe = os.path.join(REPO, "oracle", "_ref", "Mph_gcc" if dim == 2 else "Mph_gcc3d")
+    with tempfile.TemporaryDirectory() as tmp:
+        data, grid = casegen.write_case(os.path.join(tmp, "case"), params, parts)
+        subprocess.run([exe, data, grid, "prof%03d.prof", "vtk%03d.vtk", "case.log", "1"], cwd=tmp, check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        files = {}
+        for fn in sorted(os.listdir(tmp)):
+            if fn.endswith(".prof") or fn.endswith(".vtk"):
+                files[fn] = open(os.path.join(tmp, fn), "rb").read()
+        log = [ln for ln in open(os.path.join(tmp, "case.log")).read().splitlines() if ln.startswith("@ ")]
+        inputs = {"case.data": open(data, "rb").read(), "case.grid": open(grid, "rb").read()}
+    out = {"name": name, "dim": dim, "log": json.dumps(log), "names": json.dumps(sorted(files)),
+           "inputs": json.dumps(sorted(inputs))}
+    for k, v in files.items():
+        out["file:" + k] = np.frombuffer(v, dtype=np.uint8)
+    for k, v in inputs.items():
+        out["input:" + k] = np.frombuffer(v, dtype=np.uint8)
+    return out
+
+
+def main_cli():
+    orc.build_oracle(ref=True)
+    for name, dim, p, parts in cli_cases():
+        out = run_cli(name, dim, p, parts)
+        np.savez_compressed(os.path.join(HERE, f"cli_{name}.npz"), **out)
+        print("wrote", f"cli_{name}", json.loads(out["names"]))
+
+
 def main():
     orc.build_oracle(ref=True)
+    main_cli()
     for name, dim, p, parts in small_cases():
         out = run_case(name, dim, p, parts, store_full_a=(name == "dam2d"))
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
@@ -193,4 +248,7 @@ def parse_data_text(txt: str) -> casegen.Params:
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "cli":
+        main_cli()
+    else:
+        main()
