@@ -527,6 +527,8 @@ def main():
                          "last steps' start velocities instead of v_n (0)")
     ap.add_argument("--dense-coarse", type=int, default=1, choices=[0, 1],
                     help="mixed form: solve the V-cycle's first one-block coarse level (<= 224 rows) exactly")
+    ap.add_argument("--cell-sort", type=int, default=0, choices=[0, 1],
+                    help="cell sort: 0 the reference's bitonic network (bit-exact order), 1 the counting sort")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -589,6 +591,7 @@ def run_single(args, dist, rank, world, local):
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
             c.set_option("dense_coarse", args.dense_coarse)
+        c.set_option("cell_sort", args.cell_sort)
         return c
 
     def timed(c, steps, warmup, clocks=None, profile=False):

@@ -141,6 +141,65 @@ __global__ void k_bitonic_tile(int* __restrict__ key, int* __restrict__ perm, in
     }
 }
 
+// ---- counting sort (option cell_sort 1) ------------------------------------
+// The production cell sort: the keys are cell indices in [0, 2T), so one
+// counting pass sorts them.  A warp-aggregated histogram (lanes with equal
+// keys, found with __match_any_sync, add their count once), the bucket
+// offsets from the device scan (warp-level inclusive scans within a block),
+// a warp-aggregated scatter, and last each bucket ordered by the particles'
+// previous positions, so the permutation does not depend on the order in
+// which the scatter's atomics were served: a stable sort.  Unlike the
+// reference's bitonic network (main.cpp:1190-1211, not stable) it gives a
+// different order inside a cell; cell ranges and per-cell particle sets are
+// the same.
+__global__ void k_count_keys(int N, const int* __restrict__ key, int* __restrict__ cnt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < N;
+    const int k = valid ? key[i] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(cnt + k, __popc(peers));
+}
+
+__global__ void k_scatter_keys(int N, const int* __restrict__ key, const long long* __restrict__ off, int* __restrict__ cursor,
+                               int* __restrict__ perm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < N;
+    const int k = valid ? key[i] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (valid && lane == leader) base = atomicAdd(cursor + k, __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) perm[off[k] + base + __popc(peers & ((1u << lane) - 1u))] = i;
+}
+
+// thread per bucket: its particles ordered by previous position (insertion
+// sort: a bucket is one cell's fluid or wall particles), the sorted keys and
+// the bucket starts
+__global__ void k_bucket_order(int nb, const long long* __restrict__ off, int* __restrict__ key, int* __restrict__ perm,
+                               int* __restrict__ bucket)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const long long s = off[b], e = off[b + 1];
+    for (long long j = s + 1; j < e; ++j) {
+        const int v = perm[j];
+        long long k = j - 1;
+        while (k >= s && perm[k] > v) {
+            perm[k + 1] = perm[k];
+            --k;
+        }
+        perm[k + 1] = v;
+    }
+    for (long long j = s; j < e; ++j) key[j] = b;
+    bucket[b] = (int)s;
+    if (b == nb - 1) bucket[nb] = (int)e;
+}
+
 // ---- bucket starts, permutation -------------------------------------------
 // bucket[b] = first sorted position whose key >= b, b in [0, 2T]
 __global__ void k_bucket_starts(const int* __restrict__ key, int N, int T, int* __restrict__ bucket)
@@ -254,10 +313,29 @@ void launch_bitonic_sort(mph_case* c)
     }
 }
 
+int launch_counting_sort(mph_case* c)
+{
+    const int N = c->dp.N, nb = 2 * c->dp.T;
+    DeviceState& d = c->d;
+    if (!d.sort_cnt) {
+        MPH_CUDA(cudaMalloc((void**)&d.sort_cnt, (size_t)(nb + 1) * sizeof(int)));
+        MPH_CUDA(cudaMalloc((void**)&d.sort_off, (size_t)(nb + 1) * sizeof(long long)));
+    }
+    const unsigned g = grid_for(N, 256);
+    MPH_CUDA(cudaMemsetAsync(d.sort_cnt, 0, (size_t)(nb + 1) * sizeof(int), c->stream));
+    { k_count_keys<<<g, 256, 0, c->stream>>>(N, d.key, d.sort_cnt); MPH_COUNT_LAUNCH(); }
+    MPH_TRY(launch_scan_i32_to_i64(c, d.sort_cnt, d.sort_off, nb));
+    MPH_CUDA(cudaMemsetAsync(d.sort_cnt, 0, (size_t)(nb + 1) * sizeof(int), c->stream));
+    { k_scatter_keys<<<g, 256, 0, c->stream>>>(N, d.key, d.sort_off, d.sort_cnt, d.perm); MPH_COUNT_LAUNCH(); }
+    { k_bucket_order<<<grid_for(nb, 128), 128, 0, c->stream>>>(nb, d.sort_off, d.key, d.perm, d.bucket); MPH_COUNT_LAUNCH(); }
+    return MPH_OK;
+}
+
 void launch_cell_ranges_and_permute(mph_case* c)
 {
     const int N = c->dp.N;
-    { k_bucket_starts<<<grid_for(N + 1, 256), 256, 0, c->stream>>>(c->d.key, N, c->dp.T, c->d.bucket); MPH_COUNT_LAUNCH(); }
+    if (!c->cell_sort)   // the counting sort wrote the bucket starts already
+        { k_bucket_starts<<<grid_for(N + 1, 256), 256, 0, c->stream>>>(c->d.key, N, c->dp.T, c->d.bucket); MPH_COUNT_LAUNCH(); }
     const unsigned g = grid_for(N, 256);
     if (c->dim == 2)
         { k_permute<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,

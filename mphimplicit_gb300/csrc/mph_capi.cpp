@@ -123,6 +123,11 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->dense_coarse = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "cell_sort") {
+        if (!(value == 0.0 || value == 1.0)) return mph::fail(MPH_ERR_ARG, "option cell_sort: 0 (bitonic network) or 1 (counting sort)");
+        c->cell_sort = (int)value;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

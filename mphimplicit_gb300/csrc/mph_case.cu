@@ -470,7 +470,8 @@ int stage_step_begin(mph_case* c)
 int stage_cellsort(mph_case* c)
 {
     launch_cell_keys(c);
-    launch_bitonic_sort(c);
+    if (c->cell_sort) MPH_TRY(launch_counting_sort(c));
+    else launch_bitonic_sort(c);
     launch_cell_ranges_and_permute(c);
     const int init[8] = {c->dp.cc[0], c->dp.cc[1], c->dp.cc[2], 0, 0, 0, 0, 0};
     MPH_CUDA(cudaMemcpyAsync(c->d.bbox, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
@@ -674,7 +675,7 @@ int case_destroy(mph_case* c)
                     (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
                     (void*)d.grec16, (void*)d.pscale, (void*)d.uniq, (void*)d.ucount,
                     (void*)d.ctuniq, (void*)d.ctucount, (void*)d.wkey, (void*)d.wval, (void*)d.ccell,
-                    (void*)d.io3, (void*)d.vprev, (void*)d.vprev_alt, d.scan_tmp})
+                    (void*)d.io3, (void*)d.vprev, (void*)d.vprev_alt, (void*)d.sort_cnt, (void*)d.sort_off, d.scan_tmp})
         if (p) cudaFree(p);
     for (auto& p : c->prof.pending) {
         cudaEventDestroy(p.second.first);

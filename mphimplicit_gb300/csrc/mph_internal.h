@@ -85,6 +85,8 @@ struct DeviceState {
     double *divP = nullptr, *presP = nullptr, *virP = nullptr, *virS = nullptr;
     // cell list
     int *key = nullptr, *perm = nullptr, *bucket = nullptr;   // bucket: [2T+1] starts
+    int* sort_cnt = nullptr;            // counting sort: bucket counts, then write cursors [2T+1]
+    long long* sort_off = nullptr;      // counting sort: bucket offsets [2T+1]
     // neighbours
     int *nc = nullptr, *nfc = nullptr, *ncp = nullptr;
     long long *nptr = nullptr, *nptrP = nullptr;
@@ -242,6 +244,7 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
+    int cell_sort = 0;                  // 0: the reference's bitonic network (bit-exact order); 1: counting sort
     bool dense_coarse = true;           // mixed form: solve the first one-block coarse level of <= 224 rows exactly
     int dense_level = -1;               // this step's exactly solved level (-1: none)
     int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
@@ -332,6 +335,7 @@ int stage_output_fields(mph_case* c);
 void launch_step_begin(mph_case* c);
 void launch_cell_keys(mph_case* c);
 void launch_bitonic_sort(mph_case* c);
+int launch_counting_sort(mph_case* c);
 void launch_cell_ranges_and_permute(mph_case* c);
 void launch_fluid_bbox(mph_case* c);
 void launch_neighbor_count(mph_case* c);
