@@ -204,6 +204,13 @@ int mph_server_submit(mph_server* s, const mph_params* prm, const mph_particles*
 int mph_server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count);
 int mph_server_stats_get(mph_server* s, mph_server_stats* out);
 int mph_server_destroy(mph_server* s);
+/* Solver tolerances (as mph_case_set_solver) and engine options (as
+ * mph_case_set_option; the mixed form's own options skip FP64 cases) for the
+ * cases of requests submitted from now on; each case gets them when it is
+ * created.  An invalid option fails that request with the option's error.
+ * Option "extrapolate" adds its velocity history to the admission footprint. */
+int mph_server_set_solver(mph_server* s, double outer_rel_residual, double inner_rel_residual, int max_outer);
+int mph_server_set_option(mph_server* s, const char* name, double value);
 
 /* Solver tolerances.  outer_rel_residual: stop when ||b - A x|| / ||b|| is
  * below it (the reference stops at 1e-6: rr/rr0 < 1e-12, main.cpp:4346; this

@@ -529,8 +529,15 @@ int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done)
         MPH_CUDA(cudaStreamSynchronize(c->stream));
         MPH_TRY(grow_bytes((void**)&dv.arow32, &dv.cap_arow32, slots * D * D * (long long)sizeof(float)));
     }
+    // the attribute is per function and device, shared by the cases (and the
+    // host threads of a batch or a server): always the device's opt-in limit
+    // less the kernel's static shared memory
+    int optin = 0;
+    MPH_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     auto go = [&](auto kern) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncAttributes fa;
+        cudaFuncGetAttributes(&fa, kern);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
         kern<<<P.T, kAsmWarps * 32, smem, c->stream>>>(
             P, M, r[0], r[1], r[2], mwords, kmax, dv.type, dv.bucket, dv.pos, dv.vel, dv.nc, dv.nfc, dv.nptr, dv.nind, dv.ncp,
             dv.nptrP, dv.nindP, dv.cval, dv.pvec, dv.ct_ptr, dv.ct_j, dv.ct_v, dv.sptr, dv.acol, dv.aval, a32, dv.bvec,

@@ -738,13 +738,16 @@ int mixed_dense_coarse(mph_case* c)
         c->d.cap_mg_dinv32 = (long long)kDenseRows * kDenseRows;
     }
     const int smem = (n * n + n) * (int)sizeof(float);
+    // the attribute is per function and device, shared by every case (and
+    // by the host threads of a batch or a server): always the largest size
+    const int smax = (kDenseRows * kDenseRows + kDenseRows) * (int)sizeof(float);
     const LevelK L = level_k(c, lev);
     const float* cof = c->d.mg_cof32 + c->lv[lev].off_cof;
     if (c->dim == 2) {
-        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
         { k_mg_dense_inv<2><<<1, 1024, smem, c->stream>>>(L, cof, c->d.mg_dinv32); MPH_COUNT_LAUNCH(); }
     } else {
-        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        MPH_CUDA(cudaFuncSetAttribute(k_mg_dense_inv<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
         { k_mg_dense_inv<3><<<1, 1024, smem, c->stream>>>(L, cof, c->d.mg_dinv32); MPH_COUNT_LAUNCH(); }
     }
     MPH_CUDA(cudaGetLastError());

@@ -168,6 +168,10 @@ struct Request {
     std::string error;
     double t_submit = 0, t_admit = 0, t_done = 0;
     std::vector<float> times;
+    bool solver_set = false;   // the server's settings at submission
+    double tol_outer = 1.0e-6, tol_inner = 1.0e-3;
+    int max_outer = 50;
+    std::vector<std::pair<std::string, double>> options;
 };
 
 }  // namespace
@@ -184,6 +188,11 @@ struct mph_server {
     int running = 0;                // requests a worker holds right now
     long long next_ticket = 1;
     long long steps_done = 0;
+    // solver settings and options of the cases created from now on
+    bool solver_set = false;
+    double tol_outer = 1.0e-6, tol_inner = 1.0e-3;
+    int max_outer = 50;
+    std::vector<std::pair<std::string, double>> options;
     double particle_steps = 0.0;
     Clock::time_point t0 = Clock::now();
     std::vector<std::thread> workers;
@@ -237,6 +246,11 @@ struct mph_server {
                     cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
                     st = e == cudaSuccess ? mph::case_create(&r->prm, &r->parts, r->dim, r->precision, r->stream, &r->c)
                                           : mph::cuda_check(e, "cudaStreamCreateWithFlags");
+                    // the server's solver settings and options, as they were at submission
+                    if (st == MPH_OK && r->solver_set)
+                        st = mph_case_set_solver(r->c, r->tol_outer, r->tol_inner, r->max_outer);
+                    for (size_t k = 0; st == MPH_OK && k < r->options.size(); ++k)
+                        st = mph_case_set_option(r->c, r->options[k].first.c_str(), r->options[k].second);
                 }
                 if (st == MPH_OK) {
                     const auto a = Clock::now();
@@ -296,7 +310,6 @@ int server_submit(mph_server* s, const mph_params* prm, const mph_particles* par
     if (parts->count < 1 || !parts->type || !parts->pos || !parts->vel) return fail(MPH_ERR_ARG, "bad particle set");
     long long fp = 0;
     MPH_TRY(case_footprint(prm, parts, dim, precision, &fp));
-    if (fp > s->budget) return fail(MPH_ERR_CAPACITY, "case footprint " + std::to_string(fp) + " B exceeds the server budget");
     auto* r = new Request();
     r->prm = *prm;
     r->dim = dim;
@@ -312,13 +325,57 @@ int server_submit(mph_server* s, const mph_params* prm, const mph_particles* par
     r->parts.vel = r->vel.data();
     if (out) r->out = *out;
     r->step_ms = step_ms;
-    r->footprint = fp;
     std::lock_guard<std::mutex> lk(s->mu);
+    r->solver_set = s->solver_set;
+    r->tol_outer = s->tol_outer;
+    r->tol_inner = s->tol_inner;
+    r->max_outer = s->max_outer;
+    if (precision == MPH_PRECISION_MIXED) {
+        r->options = s->options;
+        for (auto& o : r->options)   // the start-velocity history of option extrapolate: 2 x 2 vectors of N x VS doubles
+            if (o.first == "extrapolate" && o.second > 0.0) fp += 4LL * parts->count * (dim == 2 ? 2 : 4) * 8;
+    } else {
+        for (auto& o : s->options)   // options of the mixed form do not apply to FP64 cases
+            if (o.first != "extrapolate" && o.first != "dense_coarse" && o.first != "factored" && o.first != "inner_blocks" &&
+                o.first != "inner_local" && o.first != "mixed_extra_sweeps")
+                r->options.push_back(o);
+    }
+    if (fp > s->budget) {
+        delete r;
+        return fail(MPH_ERR_CAPACITY, "case footprint " + std::to_string(fp) + " B exceeds the server budget");
+    }
+    r->footprint = fp;
     r->ticket = s->next_ticket++;
     r->t_submit = s->now();
     s->pending.push_back(r);
     s->admit();
     *ticket = r->ticket;
+    return MPH_OK;
+}
+
+int server_set_solver(mph_server* s, double outer, double inner, int max_outer)
+{
+    if (!s) return fail(MPH_ERR_ARG, "null server");
+    if (!(outer > 0.0) || !(inner > 0.0) || inner >= 1.0 || max_outer < 1)
+        return fail(MPH_ERR_ARG, "solver tolerances must be positive (inner < 1) and max_outer >= 1");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->solver_set = true;
+    s->tol_outer = outer;
+    s->tol_inner = inner;
+    s->max_outer = max_outer;
+    return MPH_OK;
+}
+
+int server_set_option(mph_server* s, const char* name, double value)
+{
+    if (!s || !name) return fail(MPH_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto& o : s->options)
+        if (o.first == name) {
+            o.second = value;
+            return MPH_OK;
+        }
+    s->options.push_back({name, value});
     return MPH_OK;
 }
 

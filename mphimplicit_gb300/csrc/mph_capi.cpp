@@ -90,6 +90,11 @@ int mph_server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms,
 }
 int mph_server_stats_get(mph_server* s, mph_server_stats* out) { GUARD(mph::server_stats(s, out)) }
 int mph_server_destroy(mph_server* s) { GUARD(mph::server_destroy(s)) }
+int mph_server_set_solver(mph_server* s, double outer_rel_residual, double inner_rel_residual, int max_outer)
+{
+    GUARD(mph::server_set_solver(s, outer_rel_residual, inner_rel_residual, max_outer))
+}
+int mph_server_set_option(mph_server* s, const char* name, double value) { GUARD(mph::server_set_option(s, name, value)) }
 
 int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel_residual, int max_outer)
 {

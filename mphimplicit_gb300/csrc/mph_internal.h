@@ -310,6 +310,8 @@ int server_create(long long budget, int workers, int device, mph_server** out);
 int server_submit(mph_server* s, const mph_params* prm, const mph_particles* parts, int dim, int precision, int steps,
                   const mph_fields* out, float* step_ms, long long* ticket);
 int server_poll(mph_server* s, mph_server_result* out, int max, int wait_ms, int* count);
+int server_set_solver(mph_server* s, double outer, double inner, int max_outer);
+int server_set_option(mph_server* s, const char* name, double value);
 int server_stats(mph_server* s, mph_server_stats* out);
 int server_destroy(mph_server* s);
 int case_profile_read(mph_case* c, double* out, int n);

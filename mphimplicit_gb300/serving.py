@@ -44,6 +44,8 @@ def _lib():
             "mph_server_submit": ([vp, vp, vp, ip, ip, ip, vp, vp, ctypes.POINTER(ctypes.c_longlong)], ip),
             "mph_server_poll": ([vp, ctypes.POINTER(MphServerResult), ip, ip, ctypes.POINTER(ip)], ip),
             "mph_server_stats_get": ([vp, ctypes.POINTER(MphServerStats)], ip),
+            "mph_server_set_solver": ([vp, ctypes.c_double, ctypes.c_double, ip], ip),
+            "mph_server_set_option": ([vp, ctypes.c_char_p, ctypes.c_double], ip),
             "mph_server_destroy": ([vp], ip),
         }
         for name, (args, res) in decl.items():
@@ -83,6 +85,14 @@ class Server:
         _check(self.lib.mph_server_create(int(budget_bytes), workers, device, ctypes.byref(h)))
         self.h = h
         self._live: Dict[int, tuple] = {}
+
+    def set_solver(self, outer_rel_residual: float = 1e-6, inner_rel_residual: float = 1e-3, max_outer: int = 50):
+        """Solver tolerances of the cases of later submissions."""
+        _check(self.lib.mph_server_set_solver(self.h, outer_rel_residual, inner_rel_residual, max_outer))
+
+    def set_option(self, name: str, value: float):
+        """An engine option of the cases of later submissions."""
+        _check(self.lib.mph_server_set_option(self.h, name.encode(), float(value)))
 
     def submit(self, params: casegen.Params, parts: casegen.Particles, dim: int, steps: int,
                precision: int = PRECISION_FP64, fields=("id", "pos", "vel")) -> int:

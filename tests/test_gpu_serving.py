@@ -98,3 +98,38 @@ def test_footprint_bounds_device_memory(engine_lib):
         free1, _ = torch.cuda.mem_get_info()
         g.close()
         assert free0 - free1 <= fp, (prec, free0 - free1, fp)
+
+
+def test_server_settings_apply_to_its_cases(engine_lib):
+    """mph_server_set_solver / mph_server_set_option reach every case the
+    server creates afterwards: served mixed cases refined to 1e-10 with the
+    extrapolated start give the bits of the same settings stepped alone, and
+    an invalid option fails the request, not the server."""
+    mix = [m for m in _mix() if m[4] == PRECISION_MIXED]
+    srv = serving.Server(int(20e9), workers=4)
+    srv.set_solver(1e-10, 1e-3, 50)
+    srv.set_option("extrapolate", 2)
+    tickets = {srv.submit(params, parts, dim, 4, precision=prec): (name, dim, params, parts)
+               for name, dim, params, parts, prec, _ in mix}
+    results = []
+    while len(results) < len(tickets):
+        results += srv.poll(wait_ms=100)
+    for r in results:
+        assert r["status"] == 0, r["error"]
+        name, dim, params, parts = tickets[r["ticket"]]
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_solver(1e-10, 1e-3, 50)
+        g.set_option("extrapolate", 2)
+        g.step(4)
+        ref = g.fields(("id", "pos", "vel"))
+        g.close()
+        for k in ("id", "pos", "vel"):
+            assert np.array_equal(r["fields"][k], ref[k]), (name, k)
+    srv.set_option("no_such_option", 1)
+    name, dim, params, parts = CASES[0]
+    t = srv.submit(params, parts, dim, 1, precision=PRECISION_MIXED)
+    res = []
+    while not res:
+        res = srv.poll(wait_ms=100)
+    assert res[0]["ticket"] == t and res[0]["status"] == 1
+    srv.close()
