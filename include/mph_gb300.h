@@ -247,6 +247,20 @@ int mph_case_set_solver(mph_case* c, double outer_rel_residual, double inner_rel
  *   neighbours fit stages their s in shared memory; 0: every block gathers s
  *   by column.  Both give the same bits. */
 int mph_case_set_option(mph_case* c, const char* name, double value);
+/* More options (no counterpart in the reference):
+ *   "extrapolate" 0 (default) / 1 / 2: mixed form only.  The CR start value:
+ *   the reference's v_n (main.cpp:4299-4308), or the linear / quadratic
+ *   extrapolation of the start velocities of the last steps (the history
+ *   follows the particles through the sort; mph_case_set_state clears it).
+ *   "dense_coarse" 1 (default) / 0: mixed form only.  Solve the V-cycle's
+ *   first one-block coarse level of at most 224 rows exactly with its dense
+ *   FP32 inverse (built each step), or smooth it as the reference does.
+ *   "cell_sort" 0 (default) / 1: the reference's bitonic network (the
+ *   reference's particle order, bit for bit) or a counting sort of the cell
+ *   keys (stable: inside a cell the previous order; same cell ranges).
+ *   "device_loop" 0 (default) / 1: mixed form with graphs.  1 runs the whole
+ *   solve as one CUDA graph whose refinement and CR loops are device-side
+ *   conditional while nodes (no host poll; same bits); not with profiling. */
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);
 int mph_case_time(mph_case* c, double* time);

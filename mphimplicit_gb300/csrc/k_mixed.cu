@@ -24,7 +24,8 @@ namespace mph {
 bool mixed_available() { return true; }
 
 __host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
-enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSTol2 = 23 };   // kSTol2: this phase's inner target
+enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSTol2 = 23, kSScale = 24 };   // kSTol2: this phase's inner target
+constexpr int kDeviceLoopMax = 100000;   // bound on the device-driven solve's inner iterations
 
 template <int D, int MODE, typename V>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
@@ -102,13 +103,20 @@ __global__ void k_pq32(int n, const V* __restrict__ s, const V* __restrict__ y, 
 
 // z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
 // then advances the iteration counter flags[kFlagIter].
+// In the device-driven solve (use_cond) the last block also applies the
+// next iteration's stop test (the one the operator kernels apply when an
+// iteration begins) and sets the inner loop's condition; an iteration that
+// found the solve done at its start clears it.
 template <typename V>
 __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
                         const V* __restrict__ p, const V* __restrict__ q, const V* __restrict__ u,
                         double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
-                        unsigned* __restrict__ counter)
+                        unsigned* __restrict__ counter, int cap = 0, int use_cond = 0, cudaGraphConditionalHandle cond = 0)
 {
-    if (flags[kFlagDone]) return;
+    if (flags[kFlagDone]) {
+        if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+        return;
+    }
     const int it = flags[kFlagIter];
     const V alpha = (V)(scal[rho32_slot(it)] / scal[kSQU32]);
     double acc = 0.0;
@@ -119,16 +127,27 @@ __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restri
         s[k] -= alpha * u[k];
         acc += (double)rk * (double)rk;
     }
-    reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
+    const bool last = reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
+    if (use_cond && last) {
+        const int it1 = flags[kFlagIter];
+        const double rr = scal[kSIn], rr0 = scal[kSIn0];
+        const bool bad = !(rr == rr);
+        const bool stop = it1 >= cap || rr / rr0 < scal[kSTol2] || bad;
+        if (stop) {
+            flags[kFlagDone] = 1;
+            if (bad) flags[kFlagBad] = 1;
+        }
+        cudaGraphSetConditional(cond, stop ? 0u : 1u);
+    }
 }
 
 // r32 = r * inv_scale, z = 0, and the inner reference norm (r32, r32) -> kSIn0
 template <typename V>
 __global__ void k_to32(int n, const double* __restrict__ r, V* __restrict__ r32, V* __restrict__ z,
                        double inv_scale, double* __restrict__ scal, double* __restrict__ partials,
-                       unsigned* __restrict__ counter)
+                       unsigned* __restrict__ counter, const double* __restrict__ scale_src = nullptr)
 {
-    const double sc = inv_scale;
+    const double sc = scale_src ? 1.0 / *scale_src : inv_scale;   // the device-driven solve keeps the scale on the device
     double acc = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const V v = (V)(r[k] * sc);
@@ -153,9 +172,44 @@ __global__ void k_phase_tol(double* __restrict__ scal, double tol_in2, double to
 
 // x += scale z  (FP64 update)
 template <typename V>
-__global__ void k_refine(int n, double* __restrict__ x, const V* __restrict__ z, double scale)
+__global__ void k_refine(int n, double* __restrict__ x, const V* __restrict__ z, double scale,
+                         const double* __restrict__ scale_src = nullptr, const int* __restrict__ flags = nullptr)
 {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += scale * (double)z[k];
+    if (flags && flags[kFlagBad]) return;   // the device-driven solve: a phase that met a NaN ends the solve
+    const double sc = scale_src ? *scale_src : scale;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += sc * (double)z[k];
+}
+
+// ---- the device-driven solve: control kernels --------------------------------------
+// Before every refinement phase (and once before the first): stop when the
+// FP64 residual meets the outer tolerance, is zero or NaN, the refinement
+// steps reach max_outer, a phase met a NaN, or the iterations reached their
+// cap (after the first phase) - the tests of the host-driven loop - and set
+// the outer loop's condition.
+__global__ void k_outer_check(double* __restrict__ scal, int* __restrict__ flags, double tol_out2, int max_outer, int cap,
+                              cudaGraphConditionalHandle cond)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double rr = scal[kSRR], rr0 = scal[kSRR0];
+    const int outer = flags[kFlagOuter];
+    const bool nan = !(rr == rr);
+    if (nan) flags[kFlagBad] = 1;
+    const bool stop = nan || flags[kFlagBad] || rr / rr0 < tol_out2 || outer >= max_outer || rr == 0.0 ||
+                      (outer > 0 && flags[kFlagIter] >= cap);
+    cudaGraphSetConditional(cond, stop ? 0u : 1u);
+}
+
+// Start of a refinement phase: the scale of the FP32 vectors (first phase:
+// the initial FP64 residual norm), the done flag cleared (later phases), the
+// phase count, and the inner loop's condition set.
+__global__ void k_phase_begin(double* __restrict__ scal, int* __restrict__ flags, cudaGraphConditionalHandle inner)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int outer = flags[kFlagOuter];
+    if (outer == 0) scal[kSScale] = sqrt(scal[kSRR]);
+    else flags[kFlagDone] = 0;
+    flags[kFlagOuter] = outer + 1;
+    cudaGraphSetConditional(inner, 1u);
 }
 
 // r = b - A x in FP64 (the outer residual), (r,r) -> scal[kSRR]
@@ -286,11 +340,224 @@ int mixed_prepare(mph_case* c)
 
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
 
+static void fill_mixed_stats(mph_case* c, int total_inner, int outer, const double* hs, bool bad, double tol_out2)
+{
+    c->stats.iterations = total_inner;
+    c->stats.rr0 = hs[kSRR0];
+    c->stats.rr = hs[kSRR];
+    c->stats.rs0 = 0.0;
+    c->stats.rs = 0.0;
+    c->stats.outer_iterations = outer;
+    c->stats.inner_form = c->step_pairs ? 2 : 1;
+    c->stats.inner_local_blocks = c->step_pairs ? c->loc_blocks[0] : 0;
+    c->stats.inner_gather_blocks = c->step_pairs ? c->loc_blocks[1] : 0;
+    c->stats.inner_local_cols = c->step_pairs ? c->loc_cols : 0;
+    c->stats.inner_ct_local_blocks = c->step_pairs ? c->loc_ct_blocks : 0;
+    c->stats.status = bad ? MPH_ERR_NAN : (hs[kSRR] / hs[kSRR0] < tol_out2 || hs[kSRR] == 0.0 ? MPH_OK : MPH_ERR_NOT_CONVERGED);
+}
+
+// A while node on the capturing stream `st` (after its current dependencies),
+// its body graph returned; the stream then continues after the node.
+static int add_while_node(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraph_t* body)
+{
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    MPH_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    MPH_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+    *body = p.conditional.phGraph_out[0];
+    MPH_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return MPH_OK;
+}
+
+// The device-driven mixed solve: the whole solve (start value, FP64
+// residual, refinement phases, FP32 CR iterations, velocity) as one CUDA
+// graph whose two loops are conditional while nodes, so a solve is one graph
+// launch and one read of its results instead of a host poll every few
+// iterations and at every phase.  The same kernels in the same order as the
+// host-driven solve (same bits); iterations stop where that solve's
+// kernels would have found it done, and the inner loop is bounded by
+// kDeviceLoopMax iterations, the outer by max_outer phases.
+template <int D>
+static int device_solve(mph_case* c, double* hs, int* hflags)
+{
+    using V = float;
+    DeviceState& d = c->d;
+    const int Nf = c->dp.Nf;
+    const int n = Nf * D;
+    double* scal = d.scal;
+    int* flags = d.flags;
+    unsigned* counter = (unsigned*)(flags + kFlagCounter);
+    double* part = d.partials;
+    const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
+    const unsigned gs = grid_for(Nf, 128);
+    V* vec = d.v32;
+    V *r32 = vec, *z32 = vec + (size_t)n, *s32 = vec + 2 * (size_t)n, *y32 = vec + 3 * (size_t)n;
+    V *p32 = vec + 4 * (size_t)n, *q32 = vec + 5 * (size_t)n, *u32 = vec + 6 * (size_t)n;
+    const double tol_out2 = c->tol_outer * c->tol_outer;
+    const double tol_in2 = c->tol_inner * c->tol_inner;
+    const int cap = n;
+    const int loop_cap = std::min(cap, kDeviceLoopMax);
+    const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
+    double* vprev = c->extrapolate ? d.vprev : nullptr;
+    const int have = std::min(c->prev_valid, c->extrapolate);
+    unsigned long long sig = graph_signature(c, tol_in2, cap);
+    // unlike the chunk graphs this one reads the particle arrays, which swap
+    // with their alternates every step: two graphs serve the two parities
+    const long long extra[] = {have, c->max_outer, (long long)(vprev != nullptr), (long long)(uintptr_t)d.vel,
+                               (long long)(uintptr_t)d.force, (long long)(uintptr_t)d.type, (long long)(uintptr_t)d.vprev};
+    sig = fnv1a(sig, extra, sizeof(extra));
+    sig = fnv1a(sig, &tol_out2, sizeof(tol_out2));
+    int slot = -1;
+    for (int k = 0; k < 2; ++k)
+        if (c->sx_exec[k] && c->sx_sig[k] == sig) slot = k;
+    if (slot < 0) {
+        slot = c->sx_next;   // replace the older of the two
+        c->sx_next ^= 1;
+        if (c->sx_exec[slot]) {
+            cudaGraphExecDestroy(c->sx_exec[slot]);
+            c->sx_exec[slot] = nullptr;
+        }
+        for (cudaStream_t* sp : {&c->cap_stream, &c->cap_stream2, &c->cap_stream3})
+            if (!*sp) MPH_CUDA(cudaStreamCreateWithFlags(sp, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        MPH_CUDA(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle h_out;
+        MPH_CUDA(cudaGraphConditionalHandleCreate(&h_out, g, 0u, 0u));
+        const long long l0 = t_launch_count;
+        cudaStream_t saved = c->stream;
+        int st_ = MPH_OK;
+        auto fail_capture = [&](int e) { st_ = e; };
+        auto residual = [&]() {
+            if (c->step_factored) {
+                launch_resid_factored(c, d.x, d.r, scal + kSRR);
+            } else {
+                k_resid64<D><<<gs, 128, 0, c->stream>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter,
+                                                        scal + kSRR);
+                MPH_COUNT_LAUNCH();
+            }
+        };
+        // top: start value and first residual, the outer loop, the velocity
+        cudaStream_t s1 = c->cap_stream, s2 = c->cap_stream2, s3 = c->cap_stream3;
+        MPH_CUDA(cudaStreamBeginCaptureToGraph(s1, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        c->stream = s1;
+        cudaMemsetAsync(scal, 0, 32 * sizeof(double), s1);
+        cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), s1);
+        { k_x0<D><<<rb, kReduceThreads, 0, s1>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, nvs, have, c->extrapolate,
+                                                 part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
+        residual();
+        { k_outer_check<<<1, 32, 0, s1>>>(scal, flags, tol_out2, c->max_outer, cap, h_out); MPH_COUNT_LAUNCH(); }
+        cudaGraph_t body_out = nullptr;
+        int e = add_while_node(s1, h_out, &body_out);
+        if (e != MPH_OK) fail_capture(e);
+        // outer body: one refinement phase
+        cudaGraphConditionalHandle h_in;
+        if (st_ == MPH_OK && cudaGraphConditionalHandleCreate(&h_in, body_out, 0u, 0u) != cudaSuccess)
+            fail_capture(fail(MPH_ERR_CUDA, "cudaGraphConditionalHandleCreate"));
+        if (st_ == MPH_OK && cudaStreamBeginCaptureToGraph(s2, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            fail_capture(fail(MPH_ERR_CUDA, "capture of the refinement phase"));
+        const long long l_phase0 = t_launch_count;
+        long long l_iter = 0;
+        if (st_ == MPH_OK) {
+            c->stream = s2;
+            { k_phase_begin<<<1, 32, 0, s2>>>(scal, flags, h_in); MPH_COUNT_LAUNCH(); }
+            { k_to32<V><<<rb, kReduceThreads, 0, s2>>>(n, d.r, r32, z32, 1.0, scal, part, counter, scal + kSScale); MPH_COUNT_LAUNCH(); }
+            { k_phase_tol<<<1, 32, 0, s2>>>(scal, tol_in2, tol_out2); MPH_COUNT_LAUNCH(); }
+            vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
+            cudaGraph_t body_in = nullptr;
+            e = add_while_node(s2, h_in, &body_in);
+            if (e != MPH_OK) fail_capture(e);
+            // inner body: one FP32 CR iteration
+            if (st_ == MPH_OK && cudaStreamBeginCaptureToGraph(s3, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                fail_capture(fail(MPH_ERR_CUDA, "capture of the CR iteration"));
+            if (st_ == MPH_OK) {
+                c->stream = s3;
+                const long long li0 = t_launch_count;
+                if (c->step_pairs) {
+                    launch_apply32(c, s32, y32, cap);
+                } else {
+                    k_spmv32<D, 1, V><<<gs, 128, 0, s3>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, part, counter);
+                    MPH_COUNT_LAUNCH();
+                }
+                { k_pq32<V><<<rb, kReduceThreads, 0, s3>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+                vcycle_mixed(c, q32, u32, scal + kSQU32);
+                { k_xrs32<V><<<rb, kReduceThreads, 0, s3>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter, loop_cap,
+                                                             1, h_in); MPH_COUNT_LAUNCH(); }
+                l_iter = t_launch_count - li0;
+                cudaGraph_t gi = nullptr;
+                if (cudaStreamEndCapture(s3, &gi) != cudaSuccess) fail_capture(fail(MPH_ERR_CUDA, "end of the CR iteration capture"));
+            }
+            c->stream = s2;
+            { k_refine<V><<<rb, kReduceThreads, 0, s2>>>(n, d.x, z32, 1.0, scal + kSScale, flags); MPH_COUNT_LAUNCH(); }
+            residual();
+            { k_outer_check<<<1, 32, 0, s2>>>(scal, flags, tol_out2, c->max_outer, cap, h_out); MPH_COUNT_LAUNCH(); }
+            cudaGraph_t go = nullptr;
+            if (cudaStreamEndCapture(s2, &go) != cudaSuccess) fail_capture(fail(MPH_ERR_CUDA, "end of the phase capture"));
+        }
+        const long long l_phase = t_launch_count - l_phase0 - l_iter;
+        c->stream = s1;
+        { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, s1>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
+        cudaGraph_t gt = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s1, &gt);
+        c->stream = saved;
+        const long long l_all = t_launch_count - l0;
+        c->sx_launches[slot][0] = l_all - l_phase - l_iter;   // kernels of the graph's top level, of a phase, of an iteration
+        c->sx_launches[slot][1] = l_phase;
+        c->sx_launches[slot][2] = l_iter;
+        t_launch_count = l0;
+        g_launch_count -= l_all;
+        if (st_ == MPH_OK && ec != cudaSuccess) st_ = cuda_check(ec, "end of the solve capture");
+        if (st_ == MPH_OK) {
+            const cudaError_t ei = cudaGraphInstantiate(&c->sx_exec[slot], g, 0);
+            if (ei != cudaSuccess) st_ = cuda_check(ei, "cudaGraphInstantiate (solve)");
+        }
+        cudaGraphDestroy(g);
+        if (st_ != MPH_OK) {
+            cudaGetLastError();
+            c->sx_exec[slot] = nullptr;
+            return st_;
+        }
+        c->sx_sig[slot] = sig;
+    }
+    c->prev_valid = vprev ? std::min(c->prev_valid + 1, c->extrapolate) : 0;
+    MPH_CUDA(cudaGraphLaunch(c->sx_exec[slot], c->stream));
+    MPH_CUDA(cudaMemcpyAsync(hs, scal, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaMemcpyAsync(hflags, flags, kFlagCount * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPH_CUDA(cudaStreamSynchronize(c->stream));
+    // the kernels that ran: the top level once, a phase's per refinement
+    // phase, an iteration's per CR iteration
+    g_launch_count += c->sx_launches[slot][0] + (long long)hflags[kFlagOuter] * c->sx_launches[slot][1] +
+                      (long long)hflags[kFlagIter] * c->sx_launches[slot][2];
+    return MPH_OK;
+}
+
 template <int D>
 static int mixed_solve_t(mph_case* c)
 {
     using V = float;
     MPH_TRY(mixed_prepare(c));
+    if (c->device_loop && c->use_graphs && !c->prof.on) {
+        if (c->extrapolate && !c->d.vprev) {
+            const size_t nvs0 = (size_t)c->dp.N * (D == 2 ? 2 : 4);
+            MPH_CUDA(cudaMalloc((void**)&c->d.vprev, 2 * nvs0 * sizeof(double)));
+            MPH_CUDA(cudaMalloc((void**)&c->d.vprev_alt, 2 * nvs0 * sizeof(double)));
+            c->prev_valid = 0;
+        }
+        double hs[32];
+        int hf[kFlagCount];
+        MPH_TRY(device_solve<D>(c, hs, hf));
+        const bool bad = hf[kFlagBad] != 0 || !(hs[kSRR] == hs[kSRR]);
+        const double tol_out2 = c->tol_outer * c->tol_outer;
+        fill_mixed_stats(c, hf[kFlagIter], hf[kFlagOuter], hs, bad, tol_out2);
+        return MPH_OK;
+    }
     DeviceState& d = c->d;
     const int Nf = c->dp.Nf;
     const int n = Nf * D;
@@ -438,18 +705,7 @@ static int mixed_solve_t(mph_case* c)
     { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
     MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
     MPH_CUDA(cudaStreamSynchronize(st));
-    c->stats.iterations = total_inner;
-    c->stats.rr0 = hs[kSRR0];
-    c->stats.rr = hs[kSRR];
-    c->stats.rs0 = 0.0;
-    c->stats.rs = 0.0;
-    c->stats.outer_iterations = outer;
-    c->stats.inner_form = c->step_pairs ? 2 : 1;
-    c->stats.inner_local_blocks = c->step_pairs ? c->loc_blocks[0] : 0;
-    c->stats.inner_gather_blocks = c->step_pairs ? c->loc_blocks[1] : 0;
-    c->stats.inner_local_cols = c->step_pairs ? c->loc_cols : 0;
-    c->stats.inner_ct_local_blocks = c->step_pairs ? c->loc_ct_blocks : 0;
-    c->stats.status = bad ? MPH_ERR_NAN : (hs[kSRR] / hs[kSRR0] < tol_out2 || hs[kSRR] == 0.0 ? MPH_OK : MPH_ERR_NOT_CONVERGED);
+    fill_mixed_stats(c, total_inner, outer, hs, bad, tol_out2);
     return MPH_OK;
 }
 

@@ -133,6 +133,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->cell_sort = (int)value;
         return MPH_OK;
     }
+    if (std::string(name) == "device_loop") {
+        c->device_loop = value != 0.0;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

@@ -660,7 +660,11 @@ int case_destroy(mph_case* c)
     else cudaDeviceSynchronize();
     if (c->cr_exec) cudaGraphExecDestroy(c->cr_exec);
     if (c->mx_exec) cudaGraphExecDestroy(c->mx_exec);
+    for (cudaGraphExec_t e : c->sx_exec)
+        if (e) cudaGraphExecDestroy(e);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->cap_stream2) cudaStreamDestroy(c->cap_stream2);
+    if (c->cap_stream3) cudaStreamDestroy(c->cap_stream3);
     for (cudaEvent_t e : c->gev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);

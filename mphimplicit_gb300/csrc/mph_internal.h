@@ -266,6 +266,12 @@ struct mph_case {
     cudaGraphExec_t cr_exec = nullptr;  // FP64 CR chunk
     cudaGraphExec_t mx_exec = nullptr;  // mixed form: FP32 inner CR chunk
     cudaStream_t cap_stream = nullptr;  // side stream the chunks are captured on
+    cudaStream_t cap_stream2 = nullptr, cap_stream3 = nullptr;   // the device-driven solve's loop bodies are captured on
+    bool device_loop = false;           // mixed form with graphs: the whole solve as one graph with device-side loops
+    cudaGraphExec_t sx_exec[2] = {};    // the device-driven mixed solve (one graph per parity of the swapped arrays)
+    unsigned long long sx_sig[2] = {};
+    int sx_next = 0;
+    long long sx_launches[2][3] = {};   // their kernels: top level, per refinement phase, per CR iteration
     unsigned long long cr_sig = 0, mx_sig = 0;   // signatures the two graphs were captured from
     long long cr_launches = 0, mx_launches = 0;  // kernel launches in one replay of each
     cudaStream_t own_stream = nullptr;  // private stream for batched steps of a legacy-stream case

@@ -18,7 +18,7 @@ enum {
     kSOuterRes = 8, kSOuterRes0 = 9, kSScalarCount = 16
 };
 // int flag slots
-enum { kFlagDone = 0, kFlagIter = 1, kFlagCap = 2, kFlagBad = 3, kFlagCounter = 4, kFlagCount = 8 };
+enum { kFlagDone = 0, kFlagIter = 1, kFlagCap = 2, kFlagBad = 3, kFlagCounter = 4, kFlagOuter = 5, kFlagCount = 8 };
 
 constexpr int kReduceBlocks = 1216;   // 152 SMs x 8 blocks: bound on the partials count
 constexpr int kGraphChunk = 8;        // CR iterations per captured graph chunk
@@ -68,8 +68,9 @@ __device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ p
 }
 
 // As reduce_finalize; the last block also advances the device iteration
-// counter *it (every block read it before taking its ticket).
-__device__ __forceinline__ void reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+// counter *it (every block read it before taking its ticket).  Returns true
+// in thread 0 of the last block, after the stores.
+__device__ __forceinline__ bool reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
                                                      double* __restrict__ out, int* __restrict__ it)
 {
     __shared__ bool last;
@@ -81,7 +82,7 @@ __device__ __forceinline__ void reduce_finalize_step(double v, double* __restric
         last = (ticket == gridDim.x - 1);
     }
     __syncthreads();
-    if (!last) return;
+    if (!last) return false;
     __threadfence();
     double s = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
@@ -91,6 +92,7 @@ __device__ __forceinline__ void reduce_finalize_step(double v, double* __restric
         *counter = 0u;
         *it = *it + 1;
     }
+    return threadIdx.x == 0;
 }
 
 // Capture `body` (a fixed launch sequence on c->stream) into a CUDA graph and
@@ -111,6 +113,9 @@ inline unsigned long long fnv1a(unsigned long long h, const void* p, size_t n)
     return h;
 }
 
+// (The slot total of a step changes every step but is no argument of a
+// captured kernel, which read the slices through their pointers: it is left
+// out so that a case's graphs are replayed from step to step.)
 inline unsigned long long graph_signature(const mph_case* c, double tol, int cap)
 {
     unsigned long long h = 1469598103934665603ull;
@@ -124,7 +129,7 @@ inline unsigned long long graph_signature(const mph_case* c, double tol, int cap
     h = fnv1a(h, &d, sizeof(d));
     h = fnv1a(h, &c->dp, sizeof(c->dp));
     if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));
-    const long long misc[] = {c->depth, c->nslices, c->nslots, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level,
+    const long long misc[] = {c->depth, c->nslices, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level,
                               cap, c->mg_rows_total, c->mg_cof_total};
     h = fnv1a(h, misc, sizeof(misc));
     h = fnv1a(h, &tol, sizeof(tol));

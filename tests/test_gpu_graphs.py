@@ -60,3 +60,48 @@ def test_profiled_mixed_steps_keep_graphs_and_bits(engine_lib, case):
     fa, fb = a.fields(("id", "pos", "vel")), b.fields(("id", "pos", "vel"))
     for k in ("id", "pos", "vel"):
         assert np.array_equal(fa[k], fb[k]), k
+
+
+def _run_mixed(params, parts, dim, device_loop, factored, steps=3):
+    g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_solver(1e-10, 1e-3, 50)
+    g.set_option("extrapolate", 2)
+    g.set_option("factored", factored)
+    g.set_option("device_loop", device_loop)
+    stats = []
+    for _ in range(steps):
+        g.step(1)
+        s = g.solve_stats()
+        stats.append((s["iter"], s["outer"], s["status"], s["rr"], s["rr0"]))
+    f = g.fields(("id", "pos", "vel"))
+    g.close()
+    return f, stats
+
+
+@pytest.mark.parametrize("factored", [1, 0], ids=["factored", "assembled"])
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_device_driven_solve_is_bit_identical(engine_lib, case, factored):
+    """The whole mixed solve as one graph with device-side loops (conditional
+    while nodes for the refinement phases and the CR iterations) runs the
+    kernels of the host-driven solve in the same order: the same bits, the
+    same iteration and phase counts, with refinement to 1e-10 and the
+    extrapolated start (several phases a solve)."""
+    name, dim, params, parts = case
+    fa, sa = _run_mixed(params, parts, dim, 1, factored)
+    fb, sb = _run_mixed(params, parts, dim, 0, factored)
+    assert sa == sb
+    assert all(s[1] >= 2 for s in sa)
+    for k in ("id", "pos", "vel"):
+        assert np.array_equal(fa[k], fb[k]), k
+
+
+def test_device_driven_solve_stops_at_its_caps(engine_lib):
+    """A refinement bound of one phase ends the device-side loops at once:
+    the solve reports one phase and its unmet tolerance."""
+    name, dim, params, parts = CASES[0]
+    g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+    g.set_solver(1e-12, 1e-3, 1)
+    g.set_option("device_loop", 1)
+    g.step(1)
+    s = g.solve_stats()
+    assert s["outer"] == 1 and s["status"] == 7
