@@ -425,14 +425,33 @@ def run_ensemble(args, line_base):
     from mphimplicit_gb300.cabi import PRECISION_FP64, PRECISION_MIXED
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
     ens = casegen.ensemble_2d(args.cases, seed=1)
+
+    def setup(g):
+        g.set_solver(args.outer_tol, args.inner_tol, 50)
+        g.set_option("extrapolate", args.extrapolate)
+        g.set_option("dense_coarse", args.dense_coarse)
+        g.set_option("device_loop", args.device_loop)
+
+    table = None
+    if prec == PRECISION_MIXED and args.autotune:
+        # the project autotuner: one tuning per size class (octave of the
+        # fluid count), on the first case of each class
+        from mphimplicit_gb300 import autotune
+
+        def make(i):
+            g = engine.Case(ens[i][0], ens[i][1], 2, precision=prec)
+            setup(g)
+            return g
+        nfl = [int((parts.types < 2).sum()) for _, parts in ens]
+        table = autotune.tune_table(((2, nfl[i], i) for i in range(len(ens))), make, steps=2, warmup=1)
     cases = []
     for params, parts in ens:
         g = engine.Case(params, parts, 2, precision=prec)
         if prec == PRECISION_MIXED:
-            g.set_solver(args.outer_tol, args.inner_tol, 50)
-            g.set_option("extrapolate", args.extrapolate)
-            g.set_option("dense_coarse", args.dense_coarse)
-            g.set_option("device_loop", args.device_loop)
+            setup(g)
+            if table:
+                from mphimplicit_gb300 import autotune
+                autotune.apply(g, autotune.choose(table, 2, g.fluid_count))
         cases.append(g)
     N = sum(g.count for g in cases)
     for _ in range(args.warmup):
@@ -473,6 +492,7 @@ def run_ensemble(args, line_base):
                    "precision": args.precision, "workers": args.workers, "parallelism": "single",
                    "outer_tol": args.outer_tol if prec == PRECISION_MIXED else 1e-6,
                    "cr_start": "quadratic extrapolation" if args.extrapolate == 2 and prec == PRECISION_MIXED else "v_n",
+                   "autotune": {k: v["settings"] for k, v in table.items()} if table else None,
                    "l2": "inputs larger than L2 (the cases' matrices total ~GBs)",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                    "plain_fp64_sequential_value": plain,
@@ -599,6 +619,8 @@ def main():
                     help="cell sort: 0 the reference's bitonic network (bit-exact order), 1 the counting sort")
     ap.add_argument("--device-loop", type=int, default=0, choices=[0, 1],
                     help="mixed form: the whole solve as one graph with device-side loops (1) or host-driven chunks (0)")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="mixed form: choose the launch shapes (operator block widths, graph chunk) with the autotuner")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -670,6 +692,9 @@ def run_single(args, dist, rank, world, local):
             c.set_option("dense_coarse", args.dense_coarse)
         c.set_option("cell_sort", args.cell_sort)
         c.set_option("device_loop", args.device_loop)
+        if prec_ == PRECISION_MIXED and getattr(args, "tuned_settings", None):
+            for k, v in args.tuned_settings.items():
+                c.set_option(k, v)
         return c
 
     def timed(c, steps, warmup, clocks=None, profile=False):
@@ -701,6 +726,13 @@ def run_single(args, dist, rank, world, local):
         timed.outer = outs
         return [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)], its, launches
 
+    tuned = None
+    if prec == PRECISION_MIXED and args.autotune:
+        # the project autotuner: launch shapes of this workload's mixed form by
+        # coordinate descent over whole steps of fresh copies of the case
+        from mphimplicit_gb300 import autotune
+        tuned = autotune.tune(lambda: make(prec, tol), steps=3, warmup=2)
+        args.tuned_settings = tuned["settings"]
     case = make(prec, tol)
     N, Nf = case.count, case.fluid_count
     clk = Clocks(local)
@@ -721,9 +753,16 @@ def run_single(args, dist, rank, world, local):
     scal = case.scalars()
     st = case.solve_stats()
 
-    # end to end through the public API with host buffers (pinned): every
-    # step uploads the state and reads it back (the wall centres stay on the
-    # case: mph_case_set_state keeps them when given none)
+    # end to end through the public API with host buffers (pinned): a fresh
+    # case over the same simulation steps as the timed region (the same W
+    # untimed warm-up steps), every timed step uploading the state and reading
+    # it back (the wall centres stay on the case: mph_case_set_state keeps
+    # them when given none)
+    case.close()
+    case = make(prec, tol)
+    for _ in range(args.warmup):
+        case.step(1)
+
     def pinned(shape, dt):
         return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
     fields = {"id": pinned((N,), torch.int32), "type": pinned((N,), torch.int32), "pos": pinned((N, 3), torch.float64),
@@ -732,6 +771,8 @@ def run_single(args, dist, rank, world, local):
     host = casegen.Particles(case.time(), parts.spacing, parts.domain_min, parts.domain_max, fields["type"], fields["pos"],
                              fields["vel"])
     ids = fields["id"]
+    if prec == PRECISION_MIXED:   # the uploaded state continues this case's steps
+        case.set_option("keep_history", 1)
     h2d = N * (3 * 8 * 2 + 4 + 4)
     d2h = N * (3 * 8 * 2 + 4 + 4)
     e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
@@ -806,6 +847,8 @@ def run_single(args, dist, rank, world, local):
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
             c.set_option("dense_coarse", args.dense_coarse)
+            for k, v in (getattr(args, "tuned_settings", None) or {}).items():
+                c.set_option(k, v)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,
                                   extra=True, pre=args.warmup, setup=setup)
     max_err = max(errs["mixed"]) if errs else None
@@ -842,7 +885,8 @@ def run_single(args, dist, rank, world, local):
                    "vel_rel_err_vs_fp64_1e-12": errs or None,
                    "max_vel_rel_err": max_err,
                    "meets_1e-6": (max_err <= 1e-6) if max_err is not None else None,
-                   "secondary_mixed_1e-6": secondary},
+                   "secondary_mixed_1e-6": secondary,
+                   "autotune": tuned},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps},
         "gpu_launches": launches,

@@ -258,6 +258,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value);
  *   "cell_sort" 0 (default) / 1: the reference's bitonic network (the
  *   reference's particle order, bit for bit) or a counting sort of the cell
  *   keys (stable: inside a cell the previous order; same cell ranges).
+ *   "keep_history" 0 (default) / 1: with 1, mph_case_set_state keeps the
+ *   extrapolation history: the caller declares that the state continues this
+ *   case's own steps in the case's particle order (e.g. the state it read back
+ *   with mph_get_fields); the start value only changes the iteration count.
  *   "device_loop" 0 (default) / 1: mixed form with graphs.  1 runs the whole
  *   solve as one CUDA graph whose refinement and CR loops are device-side
  *   conditional while nodes (no host poll; same bits); not with profiling. */
@@ -329,11 +333,14 @@ const char* mph_version(void);
  * between that stage and mph_stage_step_end, else MPH_ERR_STATE (also when
  * the step assembled no FP64 blocks: mixed form, option "factored").  Its scratch
  * is one fixed per-device array of 262,400 bytes, so it serves cases of at
- * most 2,097,152 fluid particles (larger: MPH_ERR_CAPACITY).  The first call
- * for a device looks up that array's address: make it before any stream
- * capture.  Calls that overlap on the GPU share the array and race: serialise
- * them.  For servers whose device memory is fully committed to resident cases,
- * where a per-call allocation could fail and a free would stall every stream. */
+ * most 2,097,152 fluid particles (larger: MPH_ERR_CAPACITY).  The first
+ * mph_case_create on a device reserves that array and looks up its address
+ * (before the case takes its own memory), so the check itself needs no device
+ * memory.  Calls that overlap on the GPU share the array and race: serialise
+ * them.  The address is kept for the life of the process: do not use the
+ * check across a reset of the device (cudaDeviceReset).  For servers whose
+ * device memory is fully committed to resident cases, where a per-call
+ * allocation could fail and a free would stall every stream. */
 int mph_residual_noalloc(mph_case* c, double* out);
 
 #ifdef __cplusplus

@@ -47,12 +47,14 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 #ifndef MPH_PAIR_MINB
 #define MPH_PAIR_MINB 1
 #endif
-// threads per block of k_visc_pen32 and k_resid_pairs (rows of a block share
-// L1 for their x gathers)
+// largest threads per block of k_visc_pen32 and k_resid_pairs (rows of a
+// block share L1 for their x gathers); a case runs them with its option
+// "pair_block" (128, 256 or this, the default)
 #ifndef MPH_PAIR_BLOCK
 #define MPH_PAIR_BLOCK 512
 #endif
-// threads per block of k_ct_apply32
+// largest threads per block of k_ct_apply32 (option "ct_block": 128 or this,
+// the default)
 #ifndef MPH_CT_BLOCK
 #define MPH_CT_BLOCK 256
 #endif
@@ -707,36 +709,36 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
     unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
-    const unsigned gt = grid_for(P.N, MPH_CT_BLOCK);
-    const unsigned gv = grid_for(P.Nf, MPH_PAIR_BLOCK);
+    const unsigned gt = grid_for(P.N, c->ct_block);
+    const unsigned gv = grid_for(P.Nf, c->pair_block);
     if (c->dim == 2) {
         if (c->loc_ct_smem)
-            k_ct_apply32<2, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
+            k_ct_apply32<2, true><<<gt, c->ct_block, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
                                                                                 d.scal, d.flags, cap, d.ctuniq, d.ctucount);
         else
-            k_ct_apply32<2, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
+            k_ct_apply32<2, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
                                                                      d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
         if (c->loc_smem)
-            k_visc_pen32<2, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+            k_visc_pen32<2, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
                 d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
-            k_visc_pen32<2, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+            k_visc_pen32<2, false><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
                 d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     } else {
         if (c->loc_ct_smem)
-            k_ct_apply32<3, true><<<gt, MPH_CT_BLOCK, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
+            k_ct_apply32<3, true><<<gt, c->ct_block, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
                                                                                 d.scal, d.flags, cap, d.ctuniq, d.ctucount);
         else
-            k_ct_apply32<3, false><<<gt, MPH_CT_BLOCK, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
+            k_ct_apply32<3, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
                                                                      d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
         if (c->loc_smem)
-            k_visc_pen32<3, true><<<gv, MPH_PAIR_BLOCK, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+            k_visc_pen32<3, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
                 d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
         else
-            k_visc_pen32<3, false><<<gv, MPH_PAIR_BLOCK, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
+            k_visc_pen32<3, false><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
                 d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
     }
@@ -1318,11 +1320,11 @@ static int launch_local_cols(mph_case* c)
     c->loc_cols = 0;
     if (P.Nf == 0 || !c->inner_local) return MPH_OK;
     const int D = c->dim;
-    const long long nb = grid_for(P.Nf, MPH_PAIR_BLOCK), nbc = grid_for(P.N, MPH_CT_BLOCK);
-    MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, MPH_PAIR_BLOCK, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,
+    const long long nb = grid_for(P.Nf, c->pair_block), nbc = grid_for(P.N, c->ct_block);
+    MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, c->pair_block, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,
                                                     &d.ucount, &d.cap_ucount)));
     int* ctw = reinterpret_cast<int*>(d.ctsval);   // the column words of the transposed records
-    MPH_TRY((local_cols<4, 3, int, 4, 3>(c, P.N, MPH_CT_BLOCK, d.ctsptr, d.ct_cnt, ctw, ctw, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
+    MPH_TRY((local_cols<4, 3, int, 4, 3>(c, P.N, c->ct_block, d.ctsptr, d.ct_cnt, ctw, ctw, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
                                          &d.cap_ctucount)));
     int h[2][3] = {};
     MPH_CUDA(cudaMemcpyAsync(h[0], d.ucount + nb, sizeof(h[0]), cudaMemcpyDeviceToHost, c->stream));
@@ -1418,14 +1420,14 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     const long long nv = (long long)P.Nf * c->dim;
     if (c->step_pairs) {
         { k_split_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32, d.x32 + nv); MPH_COUNT_LAUNCH(); }
-        const unsigned gr = grid_for(P.Nf, MPH_PAIR_BLOCK);
+        const unsigned gr = grid_for(P.Nf, c->pair_block);
         if (c->dim == 2) {
             { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<2><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
+            { k_resid_pairs<2><<<gr, c->pair_block, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         } else {
             { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
-            { k_resid_pairs<3><<<gr, MPH_PAIR_BLOCK, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
+            { k_resid_pairs<3><<<gr, c->pair_block, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         }
         return;

@@ -624,14 +624,14 @@ static int mixed_solve_t(mph_case* c)
         vcycle_mixed(c, q32, u32, scal + kSQU32);
         { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
-    const int chunk = kGraphChunk;
+    const int chunk = c->chunk;
     const bool graphs = c->use_graphs;
     // with profiling on, the captured chunk records a fixed event pair around
     // every iteration's operator; the pairs of the iterations that ran are
     // read after each chunk
     const bool gprof = graphs && c->prof.on;
     if (gprof && !c->gev[0])
-        for (int k = 0; k < 2 * kGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
+        for (int k = 0; k < 2 * kMaxGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
     if (graphs) {
         MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, tol_in2, cap), [&] {
             for (int k = 0; k < chunk; ++k) {

@@ -137,6 +137,20 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->device_loop = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "pair_block" || std::string(name) == "ct_block" || std::string(name) == "chunk") {
+        const int v = (int)value;
+        const std::string n(name);
+        const bool ok = (double)v == value &&
+                        (n == "pair_block" ? (v == 128 || v == 256 || v == 512)
+                                           : n == "ct_block" ? (v == 128 || v == 256) : (v == 4 || v == 8 || v == 16 || v == 32));
+        if (!ok) return mph::fail(MPH_ERR_ARG, "option " + n + ": pair_block 128/256/512, ct_block 128/256, chunk 4/8/16/32");
+        (n == "pair_block" ? c->pair_block : n == "ct_block" ? c->ct_block : c->chunk) = v;
+        return MPH_OK;
+    }
+    if (std::string(name) == "keep_history") {
+        c->keep_history = value != 0.0;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

@@ -387,7 +387,10 @@ int case_set_state(mph_case* c, const mph_particles* parts, const double* wall_c
     if (wall_center) std::memcpy(&c->wallC[0][0], wall_center, sizeof(c->wallC));
     c->time = parts->time;
     c->densa_valid = false;
-    c->prev_valid = 0;   // a state from outside has no velocity history
+    // a state from outside has no velocity history, unless the caller
+    // declares (option keep_history) that it continues this case's own
+    // trajectory in the case's particle order
+    if (!c->keep_history) c->prev_valid = 0;
     c->fB = 0;
     c->fE = nf;
     c->wB = nf;

@@ -244,16 +244,20 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
+    int pair_block = 512;               // threads a block of the pair-term operator (and its row blocks)
+    int ct_block = 256;                 // threads a block of the transposed P-list apply (and its particle blocks)
+    int chunk = 8;                      // mixed form: CR iterations per captured graph chunk
     int cell_sort = 0;                  // 0: the reference's bitonic network (bit-exact order); 1: counting sort
     bool dense_coarse = true;           // mixed form: solve the first one-block coarse level of <= 224 rows exactly
     int dense_level = -1;               // this step's exactly solved level (-1: none)
     int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
                                         // (1: 2 v_n - v_{n-1}; 2: 3 v_n - 3 v_{n-1} + v_{n-2}; 0: the reference's v_n)
     int prev_valid = 0;                 // start velocities of previous steps held in vprev (current particle order)
+    bool keep_history = false;          // mph_case_set_state keeps vprev (the state continues this case's steps)
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
-    cudaEvent_t gev[16] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
+    cudaEvent_t gev[64] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     int loc_smem = 0;                   // shared memory of k_visc_pen32's staged s (0: gathers by column)
     int loc_ct_smem = 0;                // shared memory of k_ct_apply32's staged s (0: gathers by column)

@@ -21,7 +21,8 @@ enum {
 enum { kFlagDone = 0, kFlagIter = 1, kFlagCap = 2, kFlagBad = 3, kFlagCounter = 4, kFlagOuter = 5, kFlagCount = 8 };
 
 constexpr int kReduceBlocks = 1216;   // 152 SMs x 8 blocks: bound on the partials count
-constexpr int kGraphChunk = 8;        // CR iterations per captured graph chunk
+constexpr int kGraphChunk = 8;        // CR iterations per captured graph chunk (FP64 form; the mixed form's option "chunk")
+constexpr int kMaxGraphChunk = 32;
 constexpr int kReduceThreads = 256;
 
 __device__ __forceinline__ double block_sum(double v)
@@ -129,7 +130,7 @@ inline unsigned long long graph_signature(const mph_case* c, double tol, int cap
     h = fnv1a(h, &d, sizeof(d));
     h = fnv1a(h, &c->dp, sizeof(c->dp));
     if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));
-    const long long misc[] = {c->depth, c->nslices, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level,
+    const long long misc[] = {c->depth, c->nslices, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level, c->pair_block, c->ct_block, c->chunk,
                               cap, c->mg_rows_total, c->mg_cof_total};
     h = fnv1a(h, misc, sizeof(misc));
     h = fnv1a(h, &tol, sizeof(tol));

@@ -73,3 +73,21 @@ def test_extrapolate_is_mixed_form_only(engine_lib):
     m = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
     with pytest.raises(engine.MphError):
         m.set_option("extrapolate", 3)
+
+
+def test_keep_history_continues_bit_for_bit(engine_lib):
+    """With option keep_history, uploading the state a case just read back
+    changes nothing: the next steps give the bits of the case stepped on."""
+    name, dim, params, parts = CASES[2]
+    runs = []
+    for upload in (False, True):
+        m = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        m.set_option("extrapolate", 2)
+        m.set_option("keep_history", 1)
+        m.step(3)
+        if upload:
+            st, ids, wc = _state(m, parts)
+            m.set_state(st, ids, wc)
+        m.step(2)
+        runs.append((m.export("Velocity"), m.solve_stats()["iter"]))
+    assert np.array_equal(runs[0][0], runs[1][0]) and runs[0][1] == runs[1][1]
