@@ -758,10 +758,12 @@ def run_single(args, dist, rank, world, local):
     # untimed warm-up steps), every timed step uploading the state and reading
     # it back (the wall centres stay on the case: mph_case_set_state keeps
     # them when given none)
-    case.close()
-    case = make(prec, tol)
-    for _ in range(args.warmup):
-        case.step(1)
+    e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
+    if e2e_steps > 0:
+        case.close()
+        case = make(prec, tol)
+        for _ in range(args.warmup):
+            case.step(1)
 
     def pinned(shape, dt):
         return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
@@ -775,7 +777,6 @@ def run_single(args, dist, rank, world, local):
         case.set_option("keep_history", 1)
     h2d = N * (3 * 8 * 2 + 4 + 4)
     d2h = N * (3 * 8 * 2 + 4 + 4)
-    e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
     e2e_value = None
     if e2e_steps > 0:
         torch.cuda.synchronize()

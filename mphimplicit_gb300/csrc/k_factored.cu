@@ -172,8 +172,8 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
     }
 }
 
-// The wall neighbours of every fluid row in FP64 (after k_pair_terms), one
-// thread per row: their viscous terms from the exact minimum image as the
+// The wall neighbours of every fluid row in FP64 (after k_pair_terms), a
+// warp per row: their viscous terms from the exact minimum image as the
 // assembly of A (main.cpp:2274-2303), summed in FP64 into the wall part of
 // the row's viscous diagonal block (sdiag64; an FP32 copy with the FP32
 // inertia in sdiag32 for the inner operator) and, with the wall velocities,
@@ -187,7 +187,10 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
                                                       const int* __restrict__ nind, double* __restrict__ bvec,
                                                       float* __restrict__ sdiag32, double* __restrict__ sdiag64)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // a warp per fluid row, its lanes over the row's wall slots; the lane
+    // sums meet in a fixed shuffle tree (deterministic)
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= P.Nf) return;
     const int ti = type[i];
     const int n = nc[i], nf = nfc[i];
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
         const double rV2 = P.rV * P.rV;
         double xi[3];
         load_vec<D>(pos, i, xi);
-        for (int k = nf; k < n; ++k) {
+        for (int k = nf + lane; k < n; k += 32) {
             const int j = nind[nb + k];
             if (j == i) continue;
             double xj[3], q[3];
@@ -226,9 +229,17 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
             sd[5] += f * e[2] * e[2];
         }
 #pragma unroll
-        for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] += sw[r];
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int t = 0; t < 6; ++t) sd[t] += __shfl_xor_sync(0xffffffffu, sd[t], o);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) sw[r] += __shfl_xor_sync(0xffffffffu, sw[r], o);
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] += sw[r];
     }
-    if (sdiag32) {
+    if (sdiag32 && lane == 0) {
         float4* o = reinterpret_cast<float4*>(sdiag32 + (size_t)i * 8);
         o[0] = make_float4((float)sd[0], (float)sd[1], (float)sd[2], (float)sd[3]);
         o[1] = make_float4((float)sd[4], (float)sd[5], P.inert32[ti], 0.f);
@@ -1269,7 +1280,7 @@ int launch_pair_terms(mph_case* c)
         gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
     }
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
-    const unsigned gw = grid_for(P.Nf, 256);
+    const unsigned gw = grid_for((long long)P.Nf * 32, 256);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
                                                                d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax); MPH_COUNT_LAUNCH(); }

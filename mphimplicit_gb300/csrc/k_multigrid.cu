@@ -482,6 +482,8 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inv(LevelK L, const float* __
                 }
     }
     __syncthreads();
+    // elimination: warp w takes rows w, w + 32, ..., lane l columns l, l + 32, ...
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int k = 0; k < n; ++k) {
         // a cell without fluid particles has a zero row and column: it stays
         // zero in the inverse (the pseudo-inverse on the occupied cells)
@@ -491,10 +493,12 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inv(LevelK L, const float* __
         __syncthreads();
         for (int j = threadIdx.x; j < n; j += blockDim.x) a[(size_t)k * n + j] = (j == k ? 1.f : a[(size_t)k * n + j]) * pk;
         __syncthreads();
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-            const int i = t / n, j = t - i * n;
+        const float* ak = a + (size_t)k * n;
+        for (int i = wid; i < n; i += nw) {
             if (i == k) continue;
-            a[t] = (j == k ? 0.f : a[t]) - colk[i] * a[(size_t)k * n + j];
+            const float ci = colk[i];
+            float* ai = a + (size_t)i * n;
+            for (int j = lane; j < n; j += 32) ai[j] = (j == k ? 0.f : ai[j]) - ci * ak[j];
         }
         __syncthreads();
     }
