@@ -182,3 +182,30 @@ def test_staged_and_gathered_operator_give_the_same_bits(engine_lib, case):
     assert sa["inner_local_blocks"] > 0 and sb["inner_local_blocks"] == 0 and sb["inner_ct_local_blocks"] == 0
     assert sa["iter"] == sb["iter"]
     assert np.array_equal(va, vb) and np.array_equal(pa, pb)
+
+
+def test_mixed_staged_and_gathering_blocks_give_the_same_bits(engine_lib):
+    """A case where some row blocks of the pair-term operator have more
+    distinct neighbours than one block may stage (RadiusV = 7 l0: about 1400
+    neighbours a particle, over 8192 distinct ones for a row block inside
+    the 30^3 fluid), so the staged kernel variant meets blocks that
+    gather by column (and transposed P-lists that keep their columns): its
+    steps agree bit for bit with every block gathering (option inner_local
+    0)."""
+    from mphimplicit_gb300 import casegen
+    parts = casegen.dam_case(3, (30, 30, 30), (36, 34, 34), 0.005, seed=2)
+    params = casegen.baseline_params(3, 0.005, 5.0e-5)
+    params.radius_ratio_v = 7.0
+    out = {}
+    for local in (1, 0):
+        g = engine.Case(params, parts, 3, precision=PRECISION_MIXED)
+        g.set_option("inner_local", local)
+        g.step(2)
+        st = g.solve_stats()
+        assert st["inner_form"] == 2
+        out[local] = (g.export("Velocity"), g.export("Position"), st)
+    (va, pa, sa), (vb, pb, sb) = out[1], out[0]
+    print(f"staged {sa['inner_local_blocks']}, gathering {sa['inner_gather_blocks']} row blocks")
+    assert sa["inner_local_blocks"] > 0 and sa["inner_gather_blocks"] > 0
+    assert sa["iter"] == sb["iter"]
+    assert np.array_equal(va, vb) and np.array_equal(pa, pb)
