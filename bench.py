@@ -269,21 +269,23 @@ def run_reference(args, rank, world):
     o = orc.Oracle(p, parts, dim, threads=threads)
     o.init()
     t_init = time.perf_counter() - t_init
-    for _ in range(args.warmup):
+    warm, steps = min(args.warmup, 2), max(1, min(args.steps, args.ref_max_steps))
+    for _ in range(warm):
         o.step(1)
     times, iters = [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
         iters.append(o.solve_stats()["iter"])
     tot = sum(times)
-    value = parts.count * args.steps / tot
+    value = parts.count * steps / tot
     same = args.workload not in ("ensemble2d", "serve") and args.ref_fluid <= 0
-    sample = (f"{desc}: {parts.count} particles, the full workload; {args.steps} timed steps after {args.warmup} "
-              f"warm-up steps and the initial pass ({t_init:.1f} s, untimed); CR stop test 1e-6 (the reference's)")
+    sample = (f"{desc}: {parts.count} particles{', the full workload' if same else ''}; {steps} timed steps after {warm} "
+              f"warm-up steps and the initial pass ({t_init:.1f} s, untimed); CR stop test 1e-6 (the reference's)"
+              + ("" if steps == args.steps else f"; {steps} of the requested {args.steps} steps timed (bounded sample)"))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": 1000 * tot / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload if same else f"{args.workload} (sampled: {desc})", "description": desc,
                        "dim": dim, "particles": parts.count, "sample": sample, "threads": threads,
@@ -597,8 +599,8 @@ def run_serve(args, line_base):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cube3d_100")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -621,10 +623,16 @@ def main():
                     help="mixed form: the whole solve as one graph with device-side loops (1) or host-driven chunks (0)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
                     help="mixed form: choose the launch shapes (operator block widths, graph chunk) with the autotuner")
+    ap.add_argument("--mg-pre", type=int, default=1,
+                    help="mixed form: V-cycle sweeps before the coarse correction on the levels below 0 (the reference: 2)")
+    ap.add_argument("--mg-post", type=int, default=1, help="mixed form: V-cycle sweeps after it (the reference: 3)")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
                     help="CPU baseline sample: the config-1 geometry at this fluid edge (100: the workload itself)")
+    ap.add_argument("--ref-max-steps", type=int, default=8,
+                    help="reference arm: time at most this many of the K steps after at most 2 warm-up steps (a CPU "
+                         "step of the config-1 workload takes ~15 s; its CR takes the same iterations every step)")
     ap.add_argument("--ref-fluid", type=int, default=0,
                     help="reference arm: time the config-1 geometry scaled to this fluid edge instead of the workload (0)")
     ap.add_argument("--outer-tol", type=float, default=None,
@@ -690,6 +698,8 @@ def run_single(args, dist, rank, world, local):
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
             c.set_option("dense_coarse", args.dense_coarse)
+            c.set_option("mg_pre", args.mg_pre)
+            c.set_option("mg_post", args.mg_post)
         c.set_option("cell_sort", args.cell_sort)
         c.set_option("device_loop", args.device_loop)
         if prec_ == PRECISION_MIXED and getattr(args, "tuned_settings", None):

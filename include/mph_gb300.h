@@ -258,6 +258,15 @@ int mph_case_set_option(mph_case* c, const char* name, double value);
  *   "cell_sort" 0 (default) / 1: the reference's bitonic network (the
  *   reference's particle order, bit for bit) or a counting sort of the cell
  *   keys (stable: inside a cell the previous order; same cell ranges).
+ *   "mg_pre", "mg_post" 1 .. 4 (default 1 and 1): mixed form only.  Jacobi
+ *   sweeps of the V-cycle's levels below level 0 before and after their
+ *   coarse correction (the reference: 2 and 3, main.cpp:4189, 4238; the FP64
+ *   form keeps those).
+ *   "pair_block" 128 / 256 / 512 (default), "ct_block" 128 / 256 (default),
+ *   "chunk" 4 / 8 (default) / 16 / 32: mixed form's launch shapes (block
+ *   widths of the pair-term operator and of the transposed apply, CR
+ *   iterations per captured graph chunk); mphimplicit_gb300/autotune.py
+ *   chooses them by measurement.
  *   "keep_history" 0 (default) / 1: with 1, mph_case_set_state keeps the
  *   extrapolation history: the caller declares that the state continues this
  *   case's own steps in the case's particle order (e.g. the state it read back

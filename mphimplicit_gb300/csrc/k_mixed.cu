@@ -25,7 +25,8 @@ bool mixed_available() { return true; }
 
 __host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
 enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSTol2 = 23, kSScale = 24 };   // kSTol2: this phase's inner target
-constexpr int kDeviceLoopMax = 100000;   // bound on the device-driven solve's inner iterations
+constexpr int kDeviceLoopMax = 100000;
+constexpr int kVcycleEvents = 2 * kMaxGraphChunk;   // gev: operator pairs first, then V-cycle pairs   // bound on the device-driven solve's inner iterations
 
 template <int D, int MODE, typename V>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
@@ -609,7 +610,7 @@ static int mixed_solve_t(mph_case* c)
     // One FP32 CR iteration; its index lives in flags[kFlagIter] (it runs on
     // across refinement steps), so one launch sequence serves every iteration
     // and replays as a graph.  Iterations after a stop return at once.
-    auto iteration = [&, c](cudaEvent_t* e, cudaEvent_t ev_end) {
+    auto iteration = [&, c](cudaEvent_t* e, cudaEvent_t ev_end, cudaEvent_t ev_v0 = nullptr, cudaEvent_t ev_v1 = nullptr) {
         cudaStream_t st = c->stream;   // the capture stream while a graph is recorded
         if (c->step_pairs) {
             launch_apply32(c, s32, y32, cap);   // FP32 pair terms, no assembled blocks
@@ -621,7 +622,9 @@ static int mixed_solve_t(mph_case* c)
         if (ev_end) cudaEventRecordWithFlags(ev_end, st, cudaEventRecordExternal);   // profiled graph: the operator's end
         else if (e) prof_begin(c, 0, &e[1]);
         { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+        if (ev_v0) cudaEventRecordWithFlags(ev_v0, st, cudaEventRecordExternal);   // profiled graph: the V-cycle
         vcycle_mixed(c, q32, u32, scal + kSQU32);
+        if (ev_v1) cudaEventRecordWithFlags(ev_v1, st, cudaEventRecordExternal);
         { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
     const int chunk = c->chunk;
@@ -631,12 +634,13 @@ static int mixed_solve_t(mph_case* c)
     // read after each chunk
     const bool gprof = graphs && c->prof.on;
     if (gprof && !c->gev[0])
-        for (int k = 0; k < 2 * kMaxGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
+        for (int k = 0; k < 4 * kMaxGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
     if (graphs) {
         MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, tol_in2, cap), [&] {
             for (int k = 0; k < chunk; ++k) {
                 if (gprof) cudaEventRecordWithFlags(c->gev[2 * k], c->stream, cudaEventRecordExternal);   // a record node
-                iteration(nullptr, gprof ? c->gev[2 * k + 1] : nullptr);
+                iteration(nullptr, gprof ? c->gev[2 * k + 1] : nullptr, gprof ? c->gev[kVcycleEvents + 2 * k] : nullptr,
+                          gprof ? c->gev[kVcycleEvents + 2 * k + 1] : nullptr);
             }
         }, &c->mx_launches));
     }
@@ -685,6 +689,9 @@ static int mixed_solve_t(mph_case* c)
                     MPH_CUDA(cudaEventElapsedTime(&ms, c->gev[2 * k], c->gev[2 * k + 1]));
                     c->prof.kern_ms[0] += ms;
                     c->prof.kern_n[0] += 1;
+                    MPH_CUDA(cudaEventElapsedTime(&ms, c->gev[kVcycleEvents + 2 * k], c->gev[kVcycleEvents + 2 * k + 1]));
+                    c->prof.kern_ms[1] += ms;
+                    c->prof.kern_n[1] += 1;
                 }
             }
             done = host_flags[kFlagDone] != 0 || launched > cap + chunk;

@@ -451,6 +451,7 @@ struct CoarseArgs {
     T* Sb[kMaxLevels];
     T* R[kMaxLevels];                 // R[first-1] holds the finer level's residual
     T* Sfine;                         // current S of level first-1 (receives the prolongation)
+    int pre, post;                    // smoothing sweeps of the levels below level 0 (the reference: 2 and 3)
     int dense;                        // >= 0: this level (one block's size) is solved exactly with dinv
     const T* dinv;                    // its dense inverse, n x n (symmetric)
 };
@@ -550,7 +551,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
             cur[l][row] = A.invd[l][row] * q;
         }
         sync();
-        const int sweeps = (l == A.depth - 1) ? 4 : 2;
+        const int sweeps = (l == A.depth - 1) ? 4 : A.pre;
         for (int k = 0; k < sweeps; ++k) jacobi(l, t0, nt, sync);
         if (l < A.depth - 1) {
             bool done3 = false;
@@ -593,7 +594,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
         for (int l = bottom < A.depth ? bottom : A.depth - 1; l > narrow; --l) {
             prolong(l, t0, nt);
             bsync();
-            for (int k = 0; k < 3; ++k) jacobi(l - 1, t0, nt, bsync);   // post-smoothing (3 updates)
+            for (int k = 0; k < A.post; ++k) jacobi(l - 1, t0, nt, bsync);   // post-smoothing (3 updates in the reference)
         }
         if (narrow > A.first) {
             prolong(narrow, t0, nt);
@@ -610,7 +611,7 @@ k_mg_small_levels(CoarseArgs<T> A, const int* __restrict__ flags)
             prolong(l, tid, nth);
             csync();
         }
-        for (int k = 0; k < 3; ++k) jacobi(l - 1, tid, nth, csync);
+        for (int k = 0; k < A.post; ++k) jacobi(l - 1, tid, nth, csync);
     }
     // prolongation into the finer, grid-wide level
     const LevelK& S_ = A.L[A.first - 1];
@@ -626,6 +627,10 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
     const int depth = c->depth;
     cudaStream_t st = c->stream;
     const int* flags = c->d.flags;
+    // sweeps of the levels below level 0: the reference's 2 and 3, or the
+    // mixed form's options mg_pre / mg_post
+    const bool mixed = std::is_same<T, float>::value;
+    const int pre = mixed ? c->mg_pre : 2, post = mixed ? c->mg_post : 3;
     LevelK L[kMaxLevels];
     for (int l = 0; l < depth; ++l) L[l] = level_k(c, l);
     auto ov = [&](int l) { return c->lv[l].off_vec; };
@@ -669,7 +674,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         residual(l - 1);
         { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], Rp + ov(l - 1), invd + ov(l), Qp + ov(l),
                                                                         cur[l], flags); MPH_COUNT_LAUNCH(); }
-        const int sweeps = (l == depth - 1) ? 4 : 2;     // coarsest: 4 sweeps + one more update
+        const int sweeps = (l == depth - 1) ? 4 : pre;   // coarsest: 4 sweeps + one more update
         for (int k = 0; k < sweeps; ++k) jacobi(l);
     }
     if (first < depth) {
@@ -687,6 +692,8 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
             A.R[l] = Rp + ov(l);
         }
         A.Sfine = cur[first - 1];
+        A.pre = pre;
+        A.post = post;
         A.dense = -1;
         A.dinv = nullptr;
         if constexpr (std::is_same<T, float>::value) {
@@ -708,7 +715,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         top = depth - 2;
     }
     for (int l = top; l >= 1; --l) {
-        for (int k = 0; k < 3; ++k) jacobi(l);
+        for (int k = 0; k < post; ++k) jacobi(l);
         prolong(l);
     }
     for (int k = 0; k < 2 + extra0; ++k) jacobi(0);      // level 0 post-smoothing

@@ -151,6 +151,12 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->keep_history = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "mg_pre" || std::string(name) == "mg_post") {
+        const int v = (int)value;
+        if ((double)v != value || v < 1 || v > 4) return mph::fail(MPH_ERR_ARG, "options mg_pre / mg_post: 1 .. 4 sweeps");
+        (std::string(name) == "mg_pre" ? c->mg_pre : c->mg_post) = v;
+        return MPH_OK;
+    }
     if (std::string(name) == "graphs") {
         c->use_graphs = value != 0.0;
         return MPH_OK;

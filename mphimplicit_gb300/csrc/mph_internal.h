@@ -248,6 +248,7 @@ struct mph_case {
     int ct_block = 256;                 // threads a block of the transposed P-list apply (and its particle blocks)
     int chunk = 8;                      // mixed form: CR iterations per captured graph chunk
     int cell_sort = 0;                  // 0: the reference's bitonic network (bit-exact order); 1: counting sort
+    int mg_pre = 1, mg_post = 1;        // mixed form: sweeps of the V-cycle's levels below level 0 (the reference's: 2 and 3)
     bool dense_coarse = true;           // mixed form: solve the first one-block coarse level of <= 224 rows exactly
     int dense_level = -1;               // this step's exactly solved level (-1: none)
     int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
@@ -257,7 +258,7 @@ struct mph_case {
     int mixed_extra_sweeps = 0;         // mixed form: extra level-0 smoothing sweeps before and after
     bool step_factored = false;         // this step's system uses the factored form
     bool step_pairs = false;            // this step's FP32 inner operator runs on the sliced pair terms
-    cudaEvent_t gev[64] = {};           // event pairs of a profiled CR graph chunk (operator start, end)
+    cudaEvent_t gev[128] = {};          // event pairs of a profiled CR graph chunk (operators, then V-cycles)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     int loc_smem = 0;                   // shared memory of k_visc_pen32's staged s (0: gathers by column)
     int loc_ct_smem = 0;                // shared memory of k_ct_apply32's staged s (0: gathers by column)
