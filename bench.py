@@ -153,15 +153,17 @@ def spmv_bytes(prof, scal, dim, vb=8):
     return blocks * (dim * dim * vb + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * vb
 
 
-def pair_apply_bytes(prof, scal, dim, st=None):
+def pair_apply_bytes(prof, scal, dim, st=None, rec="pack"):
     """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
     (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
     transposed P-list slot, entry counts and slice pointers, s gathered once,
-    t written.  k_visc_pen32: an 8-byte record per fluid slot (g = sqrt(f) e
-    in FP16 and the neighbour's block-local index) and, unless the row
-    block's neighbours are staged in shared memory, a 4-byte column (counted
-    for no slot once any block is staged: a lower bound), column + D FP32
-    lambda C per P-slot, the
+    t written.  k_visc_pen32, per fluid slot: rec "fp16" an 8-byte record (g
+    in FP16 and the neighbour's block-local index), "pack" a 4-byte packed g
+    and, in a staged row block, a 2-byte block-local index, "recompute" only
+    that index (g evaluated from the positions, read once: 16 bytes a
+    particle); unless the row block's neighbours are staged in shared memory,
+    a 4-byte column instead of the index (counted for no slot once any block
+    is staged: a lower bound).  Then column + D FP32 lambda C per P-slot, the
     8-float diagonal / inertia record, row lengths, slice pointers and
     scales, s read once, t gathered once, y written; a staged block also reads
     its count and its distinct columns (4 bytes each; their s, which the block
@@ -174,12 +176,15 @@ def pair_apply_bytes(prof, scal, dim, st=None):
     st = st or {}
     staged = st.get("inner_local_blocks", 0) > 0
     col = 0 if staged else 4
+    slot = {"fp16": 8, "pack": 4 + (2 if staged else 0), "recompute": 2 if staged else 0}[rec]
     # P-slots and transposed slots: 16-byte records (D values, zero-padded in
     # 2-D, and the column or the block-local rank), counted as D * 4 + 4
     pcol = ctcol = 4
     ct = pslots * (dim * 4 + ctcol) + n * 4 + (nct + 1) * 8 + dim * nf * 4 + n * 4
-    vp = slots * (8 + col) + pslots * (dim * 4 + pcol) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
+    vp = slots * (slot + col) + pslots * (dim * 4 + pcol) + nf * (32 + 8) + 2 * (nsl + 1) * 8 + nsl * 4 \
         + 2 * dim * nf * 4 + n * 4
+    if rec == "recompute":
+        vp += n * 16
     if staged:
         vp += st["inner_local_cols"] * 4 + (st["inner_local_blocks"] + st["inner_gather_blocks"]) * 4
     return ct + vp
@@ -626,6 +631,11 @@ def main():
     ap.add_argument("--mg-pre", type=int, default=1,
                     help="mixed form: V-cycle sweeps before the coarse correction on the levels below 0 (the reference: 2)")
     ap.add_argument("--mg-post", type=int, default=1, help="mixed form: V-cycle sweeps after it (the reference: 3)")
+    ap.add_argument("--pair-recompute", type=int, default=0, choices=[0, 1],
+                    help="mixed form: pair-term operator evaluates its pair terms per slot from the FP32 positions (1) or "
+                         "reads them as FP16 slot records (0)")
+    ap.add_argument("--pair-pack", type=int, default=1, choices=[0, 1],
+                    help="mixed form: 6-byte slot records of the pair-term operator (packed g + 2-byte index; 0: FP16, 8 bytes)")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -700,6 +710,8 @@ def run_single(args, dist, rank, world, local):
             c.set_option("dense_coarse", args.dense_coarse)
             c.set_option("mg_pre", args.mg_pre)
             c.set_option("mg_post", args.mg_post)
+            c.set_option("pair_recompute", args.pair_recompute)
+            c.set_option("pair_pack", args.pair_pack)
         c.set_option("cell_sort", args.cell_sort)
         c.set_option("device_loop", args.device_loop)
         if prec_ == PRECISION_MIXED and getattr(args, "tuned_settings", None):
@@ -808,7 +820,9 @@ def run_single(args, dist, rank, world, local):
     peak, peak_kind = measured_peaks()
     vb = 4 if prec == PRECISION_MIXED else 8
     pairs = st.get("inner_form") == 2
-    kern = {"spmv": ("k_ct_apply32+k_visc_pen32", lambda p_, s_, d_: pair_apply_bytes(p_, s_, d_, st)) if pairs else
+    rec = "recompute" if args.pair_recompute else ("pack" if args.pair_pack else "fp16")
+    kern = {"spmv": ("k_ct_apply32+k_visc_pen32" if rec != "recompute" else "k_ct_apply32+k_visc_rc32",
+                     lambda p_, s_, d_: pair_apply_bytes(p_, s_, d_, st, rec)) if pairs else
                     ("k_spmv32" if vb == 4 else "k_spmv", lambda p_, s_, d_: spmv_bytes(p_, s_, d_, vb)),
             "assemble_a": ("k_assemble_cells", assemble_bytes)}
     dom = max(kern, key=lambda k: prof[f"kern_ms_{k}"])
@@ -858,6 +872,10 @@ def run_single(args, dist, rank, world, local):
                 c.set_option("inner_blocks", args.inner_blocks)
             c.set_option("extrapolate", args.extrapolate)
             c.set_option("dense_coarse", args.dense_coarse)
+            c.set_option("mg_pre", args.mg_pre)
+            c.set_option("mg_post", args.mg_post)
+            c.set_option("pair_recompute", args.pair_recompute)
+            c.set_option("pair_pack", args.pair_pack)
             for k, v in (getattr(args, "tuned_settings", None) or {}).items():
                 c.set_option(k, v)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,
@@ -869,7 +887,8 @@ def run_single(args, dist, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == PRECISION_FP64 else
-                 ("f32-inner(fp16 pair-term storage)/f64-outer" if pairs else "f32-inner/f64-outer"),
+                 (f"f32-inner({ {'fp16': 'fp16', 'pack': '11/11/10-bit fixed-point', 'recompute': 'recomputed fp32'}[rec]} "
+                  f"pair terms)/f64-outer" if pairs else "f32-inner/f64-outer"),
         "data": "synthetic",
         "config": {"workload": args.workload, "description": desc, "dim": dim, "particles": N, "fluid": Nf,
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",

@@ -25,6 +25,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"] + ARCH
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off"]
+# tuning builds: -D definitions of the kernels' compile-time constants (MPH_PAIR_BLOCK,
+# MPH_CTA_ROWS, ...) from the environment, e.g. MPH_NVCC_DEFINES="-DMPH_CLUSTER_CTAS=16"
+NVCC_FLAGS += [f for f in os.environ.get("MPH_NVCC_DEFINES", "").split() if f.startswith("-D")]
 
 LIB_SOURCES = ["k_particles.cu", "k_neighbor.cu", "k_explicit.cu", "k_assemble.cu", "k_multigrid.cu",
                "k_solver.cu", "k_mixed.cu", "k_assemble_cells.cu", "k_factored.cu", "k_resid_noalloc.cu", "mph_case.cu", "mph_export.cu",

@@ -24,6 +24,8 @@
 // accumulation of the assembled form; in the residual only inertia and
 // C Lambda C^T (about 20 P-slots a row) are FP64.
 #include <cuda_fp16.h>
+#include <algorithm>
+#include <atomic>
 #include <climits>
 
 #include "mph_device.cuh"
@@ -67,6 +69,7 @@ constexpr int kUMax = 8192;
 constexpr int kWinWords = 1 << 13;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 
+
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
 // (main.cpp:2261-2304 for e, f; 2318-2333 and 2574-2584 for b).  The
 // separation is the difference of the two-float positions (pos32, poslo32),
@@ -83,7 +86,8 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
-             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ cvl32, unsigned* __restrict__ gmax)
+             float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ cvl32, unsigned* __restrict__ gmax,
+             int* __restrict__ wrap)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -120,6 +124,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                     inner = inner && fabsf(q32[d]) < 0.48f * P.hw32[d];
                 }
                 if (!inner) {
+                    *wrap = 1;   // the recomputing inner operator then takes the minimum image
                     double xi[3], xj[3], q[3];
                     load_vec<D>(pos, i, xi);
                     load_vec<D>(pos, j, xj);
@@ -388,6 +393,7 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
         U = ucount[blockIdx.x];
         if (U >= 0) {
             const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+#pragma unroll 4
             for (int a = threadIdx.x; a < U; a += blockDim.x) {
                 const int j = ul[a];
 #pragma unroll
@@ -413,61 +419,108 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
     t[k] = s;
 }
 
-// The viscous part of row i in FP32 from the sliced pair terms:
-// yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)), with g from the FP32
-// slices (pes32) or (HALF) from the slot records: 8 bytes a fluid slot, in
-// the slot order of the sliced layout, g in FP16 (scaled per slice) in the
-// first D halves and the neighbour's block-local index in the fourth.
-template <int D, bool HALF, bool LOC = false>
+// Slot records of the inner operator's viscous pairs, in the slot order of
+// the sliced layout.  FP16 form (8 bytes a slot): g = sqrt(f) e in FP16,
+// scaled per slice, in the first D halves and the neighbour's block-local
+// index in the fourth.  Packed form (option pair_pack, 6 bytes a slot): g in
+// one 32-bit word as signed fixed point in units of the slice's scale
+// (bits 0-10 x, 11-21 y, 22-31 z in units of twice the scale: relative
+// rounding about 2^-11 of the slice's largest component) and the block-local
+// index in a separate 2-byte stream.  A record is carried as a uint2: the
+// FP16 record, or (g word, index).
+template <bool PACK, bool LOC>
+__device__ __forceinline__ uint2 load_slot(const uint2* __restrict__ r16, const unsigned* __restrict__ r32,
+                                           const unsigned short* __restrict__ l16, long long e)
+{
+    if (PACK) return make_uint2(__ldcs(r32 + e), LOC ? (unsigned)__ldcs(l16 + e) : 0u);
+    return __ldcs(r16 + e);
+}
+
+// g in units of the slice's scale, and the block-local index
+template <int D, bool PACK>
+__device__ __forceinline__ int decode_slot(uint2 r, float* g)
+{
+    if (PACK) {
+        g[0] = (float)(((int)(r.x << 21)) >> 21);
+        g[1] = (float)(((int)(r.x << 10)) >> 21);
+        g[2] = D == 3 ? 2.f * (float)(((int)r.x) >> 22) : 0.f;
+        return (int)r.y;
+    }
+    g[0] = __half2float(__ushort_as_half((unsigned short)(r.x & 0xffffu)));
+    g[1] = __half2float(__ushort_as_half((unsigned short)(r.x >> 16)));
+    g[2] = D == 3 ? __half2float(__ushort_as_half((unsigned short)(r.y & 0xffffu))) : 0.f;
+    return (int)(r.y >> 16);
+}
+
+// The viscous part of row i in FP32 from the slot records:
+// yv = S_wall x_i + sum_{fluid j} g (g . (x_i - x_j)).  LOC: the neighbour's
+// x from the block's shared-memory copy by its block-local index, else
+// gathered by column.  The record stream is software-pipelined: the next
+// kPairUnroll records (and columns) are loaded while the current ones are
+// applied; pre holds the first ones, loaded by the caller.
+template <int D, bool PACK, bool LOC>
 __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, const float* __restrict__ sdiag,
                                            const int* __restrict__ nfc, const long long* __restrict__ sptr,
-                                           const int* __restrict__ acol, const float* __restrict__ pes,
-                                           const unsigned short* __restrict__ grec, const float* __restrict__ pscale,
-                                           const float* __restrict__ x, float* yv, const float* xs = nullptr)
+                                           const int* __restrict__ acol, const uint2* __restrict__ r16,
+                                           const unsigned* __restrict__ r32, const unsigned short* __restrict__ l16,
+                                           const float* __restrict__ pscale, const float* __restrict__ x, float* yv,
+                                           const float* xs, const uint2* pre)
 {
     const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
     const float4 s1 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8 + 4);
     yv[0] = s0.x * xi[0] + s0.y * xi[1] + s0.z * xi[2];
     yv[1] = s0.y * xi[0] + s0.w * xi[1] + s1.x * xi[2];
     yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
-    const long long base = sptr[i >> 5];
-    const int* cp = acol + base + lane;
-    const uint2* rp = reinterpret_cast<const uint2*>(grec) + base + lane;
-    const long long vo = base * D + lane;
+    const long long base = sptr[i >> 5] + lane;
+    const int* cp = acol + base;
     const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
-#pragma unroll (kPairUnroll)
-    for (int k = 0; k < n; ++k) {
-        float g[3] = {0.f, 0.f, 0.f};
-        const float* xj;
-        if (HALF) {
-            const uint2 r = __ldcs(rp + (long long)k * 32);
-            g[0] = __half2float(__ushort_as_half((unsigned short)(r.x & 0xffffu)));
-            g[1] = __half2float(__ushort_as_half((unsigned short)(r.x >> 16)));
-            if (D == 3) g[2] = __half2float(__ushort_as_half((unsigned short)(r.y & 0xffffu)));
-            // LOC: the neighbour's x from the block's shared-memory copy, by
-            // its block-local index; else the global gather by column
-            xj = LOC ? xs + (size_t)(r.y >> 16) * D : x + (size_t)__ldcs(cp + (long long)k * 32) * D;
-        } else {
+    constexpr int R = kPairUnroll;
+    uint2 cur[R];
+    int ccur[R];
 #pragma unroll
-            for (int d = 0; d < D; ++d) g[d] = __ldcs(pes + vo + ((long long)k * D + d) * 32);
-            xj = x + (size_t)__ldcs(cp + (long long)k * 32) * D;
-        }
-        float gx = 0.f;
-#pragma unroll
-        for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - xj[d]);
-#pragma unroll
-        for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
+    for (int u = 0; u < R; ++u) {
+        cur[u] = pre[u];
+        ccur[u] = (!LOC && u < n) ? __ldcs(cp + (long long)u * 32) : 0;
     }
-    const float s2 = HALF ? pscale[i >> 5] * pscale[i >> 5] : 1.f;
+    for (int k0 = 0; k0 < n; k0 += R) {
+        uint2 nxt[R];
+        int cnxt[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k = k0 + R + u;
+            nxt[u] = k < n ? load_slot<PACK, LOC>(r16, r32, l16, base + (long long)k * 32) : make_uint2(0u, 0u);
+            cnxt[u] = (!LOC && k < n) ? __ldcs(cp + (long long)k * 32) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            if (k0 + u < n) {
+                float g[3];
+                const int lj = decode_slot<D, PACK>(cur[u], g);
+                const float* xj = LOC ? xs + (size_t)lj * D : x + (size_t)ccur[u] * D;
+                float gx = 0.f;
+#pragma unroll
+                for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - xj[d]);
+#pragma unroll
+                for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            cur[u] = nxt[u];
+            ccur[u] = cnxt[u];
+        }
+    }
+    const float s2 = pscale[i >> 5] * pscale[i >> 5];
 #pragma unroll
     for (int d = 0; d < 3; ++d) yv[d] += ys[d] * s2;
 }
 
-template <int D, bool LOC>
-__global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
+template <int D, bool LOC, bool PACK>
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK, 2)   // two 512-row blocks an SM
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
-             const unsigned short* __restrict__ grec, const float* __restrict__ pscale, const float* __restrict__ sdiag,
+             const unsigned short* __restrict__ grec, const unsigned* __restrict__ grec32, const unsigned short* __restrict__ lcol,
+             const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const float4* __restrict__ psrec,
              const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
@@ -477,11 +530,21 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint2* r16 = reinterpret_cast<const uint2*>(grec);
+    uint2 pre[kPairUnroll];   // the row's first slot records, in flight while s is staged
+    {
+        const int n0 = i < Nf ? nfc[i] : 0;
+        const long long b0 = i < Nf ? sptr[i >> 5] + (i & 31) : 0;
+#pragma unroll
+        for (int u = 0; u < kPairUnroll; ++u)
+            pre[u] = u < n0 ? load_slot<PACK, LOC>(r16, grec32, lcol, b0 + (long long)u * 32) : make_uint2(0u, 0u);
+    }
     int U = -1;
     if (LOC) {   // stage s of the block's distinct neighbours once (block-uniform)
         U = ucount[blockIdx.x];
         if (U >= 0) {
             const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+#pragma unroll 4
             for (int k = threadIdx.x; k < U; k += blockDim.x) {
                 const int j = ul[k];
 #pragma unroll
@@ -497,11 +560,144 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 #pragma unroll
         for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
         float yv[3];
-        if (LOC && U >= 0) visc_row32<D, true, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, grec, pscale, x, yv, xs_loc);
-        else visc_row32<D, true>(i, lane, xi, sdiag, nfc, sptr, acol, nullptr, grec, pscale, x, yv);
+        if (LOC && U >= 0)
+            visc_row32<D, PACK, true>(i, lane, xi, sdiag, nfc, sptr, acol, r16, grec32, lcol, pscale, x, yv, xs_loc, pre);
+        else
+            visc_row32<D, PACK, false>(i, lane, xi, sdiag, nfc, sptr, acol, r16, grec32, lcol, pscale, x, yv, nullptr, pre);
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
+        {   // C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
+            const float4* rp = psrec + psptr[i >> 5] + lane;
+            const int np = ncp[i];
+#pragma unroll 4
+            for (int a = 0; a < np; ++a) {
+                const float4 r = __ldcs(rp + (long long)a * 32);
+                const float tk = t[__float_as_int(r.w)];
+                yv[0] += r.x * tk;
+                yv[1] += r.y * tk;
+                if (D == 3) yv[2] += r.z * tk;
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            y[(size_t)i * D + d] = yv[d];
+            acc += (double)xi[d] * (double)yv[d];
+        }
+    }
+    reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
+}
+
+// The pair-term operator with its pair terms evaluated per slot (option
+// pair_recompute, the default): a fluid slot reads only its neighbour's
+// block-local index (2 bytes) or, in a row block that gathers by column, its
+// column; the neighbour's FP32 position and type (pt32) and its s come from
+// the block's shared-memory copy, or by column.  Per pair, as k_pair_terms:
+// q = p_j - p_i from the high parts of the two-float positions,
+// w = -dwvdr(|q|, RadiusV) (main.cpp:301, 2276) and f = visc mu_ij w / |q|
+// (main.cpp:2285-2289), and the term g (g . (s_i - s_j)) with g = sqrt(f) e
+// is f / |q|^2 q (q . (s_i - s_j)).  q_ji = -q_ij exactly, so the operator is
+// exactly symmetric; its pair coefficients carry the FP32 rounding of the
+// separation (about 1e-5 of it at the closest pairs of a unit-sized domain)
+// instead of the FP16 storage of the slot records (2^-11).  WRAP: the minimum
+// image of each separation, as the neighbour search (only when a pair of the
+// step is a periodic image).
+template <int D, bool LOC, bool WRAP>
+__device__ __forceinline__ void visc_rc_loop(const DevParams& P, int n, const unsigned short* __restrict__ lp,
+                                             const int* __restrict__ cp, const float4* pts, const float* xs,
+                                             const float* pi, const float* xi, float vm0, float vm1, float* ys)
+{
+#pragma unroll (kPairUnroll)
+    for (int k = 0; k < n; ++k) {
+        const int j = LOC ? (int)__ldcs(lp + (long long)k * 32) : __ldcs(cp + (long long)k * 32);
+        const float4 pj = pts[j];
+        const float* xj = xs + (size_t)j * D;
+        float q[3] = {pj.x - pi[0], pj.y - pi[1], D == 3 ? pj.z - pi[2] : 0.f};
+        if (WRAP) {
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                q[d] = q[d] > P.hw32[d] ? q[d] - P.w32[d] : (q[d] < -P.hw32[d] ? q[d] + P.w32[d] : q[d]);
+        }
+        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const bool in = r2 > 0.f && r2 < P.rV2_32;
+        const float inv = rsqrtf(in ? r2 : 1.f);
+        const float wd = P.wdA32 * (1.f - (r2 * inv) * P.inv_rv32);
+        const float vm = __float_as_int(pj.w) == 1 ? vm1 : vm0;   // fluid types 0 and 1
+        const float cf = in ? vm * wd * (inv * inv * inv) : 0.f;
+        float dot = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) dot += q[d] * (xi[d] - xj[d]);
+        const float cd = cf * dot;
+#pragma unroll
+        for (int d = 0; d < D; ++d) ys[d] += cd * q[d];
+    }
+}
+
+template <int D, bool LOC>
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK, MPH_PAIR_MINB)
+k_visc_rc32(DevParams P, int Nf, const float4* __restrict__ pt32, const int* __restrict__ nfc, const long long* __restrict__ sptr,
+            const int* __restrict__ acol, const unsigned short* __restrict__ lcol, const float* __restrict__ sdiag,
+            const int* __restrict__ ncp, const long long* __restrict__ psptr, const float4* __restrict__ psrec,
+            const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
+            const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
+            const int* __restrict__ uniq, const int* __restrict__ ucount, int ucap, const int* __restrict__ wrap)
+{
+    // LOC: the position and type of the block's distinct fluid neighbours
+    // (ucap records), then their s, by block-local index
+    extern __shared__ float4 rc_smem[];
+    if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float4* ps = rc_smem;
+    float* xs = reinterpret_cast<float*>(rc_smem + ucap);
+    int U = -1;
+    if (LOC) {   // block-uniform
+        U = ucount[blockIdx.x];
+        if (U >= 0) {
+            const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+#pragma unroll 4
+            for (int k = threadIdx.x; k < U; k += blockDim.x) {
+                const int j = ul[k];
+                ps[k] = pt32[j];
+#pragma unroll
+                for (int d = 0; d < D; ++d) xs[k * D + d] = x[(size_t)j * D + d];
+            }
+            __syncthreads();
+        }
+    }
+    const bool wr = *wrap != 0;
+    double acc = 0.0;
+    if (i < Nf) {
+        const int lane = i & 31;
+        float xi[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) xi[d] = x[(size_t)i * D + d];
+        const float4 p4 = pt32[i];
+        const float pi[3] = {p4.x, p4.y, p4.z};
+        const int ti = __float_as_int(p4.w);
+        const float vm0 = P.vm32[ti][0], vm1 = P.vm32[ti][1];
+        // wall part of the viscous diagonal block and the inertia
+        const float4 s0 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8);
+        const float4 s1 = *reinterpret_cast<const float4*>(sdiag + (size_t)i * 8 + 4);
+        float yv[3];
+        yv[0] = s0.x * xi[0] + s0.y * xi[1] + s0.z * xi[2];
+        yv[1] = s0.y * xi[0] + s0.w * xi[1] + s1.x * xi[2];
+        yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
+        const float in32 = s1.z;
+#pragma unroll
+        for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
+        const long long base = sptr[i >> 5] + lane;
+        const int n = nfc[i];
+        float ys[3] = {0.f, 0.f, 0.f};
+        if (LOC && U >= 0) {
+            if (wr) visc_rc_loop<D, true, true>(P, n, lcol + base, nullptr, ps, xs, pi, xi, vm0, vm1, ys);
+            else visc_rc_loop<D, true, false>(P, n, lcol + base, nullptr, ps, xs, pi, xi, vm0, vm1, ys);
+        } else {
+            if (wr) visc_rc_loop<D, false, true>(P, n, nullptr, acol + base, pt32, x, pi, xi, vm0, vm1, ys);
+            else visc_rc_loop<D, false, false>(P, n, nullptr, acol + base, pt32, x, pi, xi, vm0, vm1, ys);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) yv[d] += ys[d];
         {   // C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
             const float4* rp = psrec + psptr[i >> 5] + lane;
             const int np = ncp[i];
@@ -538,7 +734,8 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
                                                         const long long* __restrict__ rptr, const int* __restrict__ cols,
                                                         const float4* __restrict__ pe32, const float* __restrict__ v32,
                                                         int* __restrict__ scol, float* __restrict__ sval,
-                                                        unsigned short* __restrict__ sval16, float* __restrict__ sscale)
+                                                        unsigned short* __restrict__ sval16, float* __restrict__ sscale,
+                                                        unsigned* __restrict__ sval32)
 {
     constexpr int W = kLtsK * D + 1;   // odd row stride: no bank conflicts
     __shared__ float tile[32 * W];
@@ -555,9 +752,11 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
     const long long sb = sptr[sl];
     const int w = (int)((sptr[sl + 1] - sb) / 32);   // entries per row of the slice
     float inv16 = 0.f;
-    if (PAIRS) {   // the slice's largest |g| component (from k_pair_terms, as bits) maps to 2^15
+    if (PAIRS && (sval16 || sval32)) {
+        // the slice's largest |g| component (from k_pair_terms, as bits) maps
+        // to 2^15 (FP16 records) or to 1023 (packed records)
         const float m = __uint_as_float(reinterpret_cast<const unsigned*>(sscale)[sl]);
-        const float sigma = m / 32768.f;
+        const float sigma = m / (sval32 ? 1023.f : 32768.f);
         inv16 = m > 0.f ? 1.f / sigma : 0.f;
         __syncthreads();   // every thread has read the maximum before it is replaced by the scale
         if (threadIdx.x == 0) sscale[sl] = sigma;
@@ -600,7 +799,21 @@ __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long lon
                     make_float4(v[0], v[1], D == 3 ? v[2] : 0.f, __int_as_float(ctile[ln * (kLtsK + 1) + kl]));
             }
         }
-        if (PAIRS) {   // whole slot records (the index half is written later)
+        if (PAIRS && sval32) {   // packed g words (the indices are a separate stream)
+            for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+                const int ln = o & 31, kl = o >> 5;
+                int q[3] = {0, 0, 0};
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const int lim = d == 2 ? 511 : 1023;
+                    const float v = tile[ln * W + kl * D + d] * inv16 * (d == 2 ? 0.5f : 1.f);
+                    q[d] = max(-lim, min(lim, __float2int_rn(v)));
+                }
+                sval32[sb + (long long)(k0 + kl) * 32 + ln] =
+                    ((unsigned)q[0] & 0x7ffu) | (((unsigned)q[1] & 0x7ffu) << 11) | (((unsigned)q[2] & 0x3ffu) << 22);
+            }
+        }
+        if (PAIRS && sval16) {   // whole slot records (the index half is written later)
             for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
                 const int ln = o & 31, kl = o >> 5;
                 unsigned h[3] = {0u, 0u, 0u};
@@ -715,6 +928,21 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
     reduce_finalize(acc, partials, counter, out);
 }
 
+template <int D, bool PACK>
+static void visc_pen_launch(mph_case* c, unsigned gv, const float* x, float* y, unsigned* counter)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    if (c->loc_smem)
+        k_visc_pen32<D, true, PACK><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32, d.lcol16,
+            d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
+            d.ucount);
+    else
+        k_visc_pen32<D, false, PACK><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32, d.lcol16,
+            d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
+            nullptr);
+}
+
 void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 {
     DeviceState& d = c->d;
@@ -730,12 +958,19 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
             k_ct_apply32<2, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
                                                                      d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
-        if (c->loc_smem)
-            k_visc_pen32<2, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        if (c->pair_recompute) {
+            if (c->loc_smem)
+                k_visc_rc32<2, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, d.lcol16,
+                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
+                    d.ucount, c->loc_cap, d.wrap32);
+            else
+                k_visc_rc32<2, false><<<gv, c->pair_block, 0, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, nullptr,
+                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
+                    nullptr, 0, d.wrap32);
+        } else if (c->pair_pack)
+            visc_pen_launch<2, true>(c, gv, x, y, counter);
         else
-            k_visc_pen32<2, false><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+            visc_pen_launch<2, false>(c, gv, x, y, counter);
         MPH_COUNT_LAUNCH();
     } else {
         if (c->loc_ct_smem)
@@ -745,12 +980,19 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
             k_ct_apply32<3, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
                                                                      d.flags, cap, nullptr, nullptr);
         MPH_COUNT_LAUNCH();
-        if (c->loc_smem)
-            k_visc_pen32<3, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq, d.ucount);
+        if (c->pair_recompute) {
+            if (c->loc_smem)
+                k_visc_rc32<3, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, d.lcol16,
+                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
+                    d.ucount, c->loc_cap, d.wrap32);
+            else
+                k_visc_rc32<3, false><<<gv, c->pair_block, 0, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, nullptr,
+                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
+                    nullptr, 0, d.wrap32);
+        } else if (c->pair_pack)
+            visc_pen_launch<3, true>(c, gv, x, y, counter);
         else
-            k_visc_pen32<3, false><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.pscale, d.sdiag32, d.ncp,
-                d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr, nullptr);
+            visc_pen_launch<3, false>(c, gv, x, y, counter);
         MPH_COUNT_LAUNCH();
     }
 }
@@ -1277,17 +1519,19 @@ int launch_pair_terms(mph_case* c)
         cvl = d.cvl32;
         if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float)));
         MPH_CUDA(cudaMemsetAsync(d.pscale, 0, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float), c->stream));
-        gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
+        if (!c->pair_recompute)
+            gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
     }
+    MPH_CUDA(cudaMemsetAsync(d.wrap32, 0, sizeof(int), c->stream));
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
     const unsigned gw = grid_for((long long)P.Nf * 32, 256);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<2><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<3><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
@@ -1312,6 +1556,26 @@ static int local_cols(mph_case* c, int rows, int block, const long long* sptr, c
     return MPH_OK;
 }
 
+// Dynamic shared memory the staging k_visc_rc32 may take: kUMax records (a
+// float4 and D floats each), within the device's opt-in limit less the
+// kernel's static shared memory.  The attribute is set to this fixed value
+// (a per-launch value would race between host threads of batched cases).
+static int rc_smem_max(int D)
+{
+    static std::atomic<int> cached[4];
+    if (const int v = cached[D].load()) return v;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (D == 2) cudaFuncGetAttributes(&fa, k_visc_rc32<2, true>);
+    else cudaFuncGetAttributes(&fa, k_visc_rc32<3, true>);
+    const int want = kUMax * ((int)sizeof(float4) + D * (int)sizeof(float));
+    const int v = std::max(0, std::min(want, optin - (int)fa.sharedSizeBytes));
+    cached[D].store(v);
+    return v;
+}
+
 // a step's count rounded up so that small changes keep the captured graphs
 static int round_cols(int umax) { return umax > 0 ? (umax + 511) / 512 * 512 : 0; }
 
@@ -1332,8 +1596,12 @@ static int launch_local_cols(mph_case* c)
     if (P.Nf == 0 || !c->inner_local) return MPH_OK;
     const int D = c->dim;
     const long long nb = grid_for(P.Nf, c->pair_block), nbc = grid_for(P.N, c->ct_block);
-    MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, c->pair_block, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,
-                                                    &d.ucount, &d.cap_ucount)));
+    if (c->pair_recompute || c->pair_pack)
+        MPH_TRY((local_cols<1, 0, unsigned short, 1, 0>(c, P.Nf, c->pair_block, d.sptr, d.nfc, d.acol, d.lcol16, &d.uniq, &d.cap_uniq,
+                                                        &d.ucount, &d.cap_ucount)));
+    else
+        MPH_TRY((local_cols<1, 0, unsigned short, 4, 3>(c, P.Nf, c->pair_block, d.sptr, d.nfc, d.acol, d.grec16, &d.uniq, &d.cap_uniq,
+                                                        &d.ucount, &d.cap_ucount)));
     int* ctw = reinterpret_cast<int*>(d.ctsval);   // the column words of the transposed records
     MPH_TRY((local_cols<4, 3, int, 4, 3>(c, P.N, c->ct_block, d.ctsptr, d.ct_cnt, ctw, ctw, &d.ctuniq, &d.cap_ctuniq, &d.ctucount,
                                          &d.cap_ctucount)));
@@ -1346,13 +1614,24 @@ static int launch_local_cols(mph_case* c)
     c->loc_blocks[1] = (int)nb - c->loc_blocks[0];
     c->loc_cols = xcap ? (long long)(unsigned)h[0][2] : 0;
     c->loc_ct_blocks = ctcap ? h[1][1] : 0;
-    c->loc_smem = xcap * D * (int)sizeof(float);
+    c->loc_cap = xcap;
+    c->loc_smem = xcap * (c->pair_recompute ? (int)sizeof(float4) + D * (int)sizeof(float) : D * (int)sizeof(float));
     c->loc_ct_smem = ctcap * D * (int)sizeof(float);
+    if (c->pair_recompute && c->loc_smem > rc_smem_max(D)) {   // a block's records do not fit: every block gathers
+        c->loc_smem = 0;
+        c->loc_blocks[1] += c->loc_blocks[0];
+        c->loc_blocks[0] = 0;
+        c->loc_cols = 0;
+    }
     if (D == 2) {
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(2)));
         MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
     } else {
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(3)));
         MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
     }
     return MPH_OK;
@@ -1365,7 +1644,25 @@ int launch_pairs_to_slices(mph_case* c)
     const int D = c->dim;
     if (c->nslices == 0) return MPH_OK;
     MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
-    if (c->nslots * 4 > d.cap_grec16) {   // slot records, 4 halves a slot
+    const bool lrec = c->pair_recompute || c->pair_pack;   // records without the index half
+    if (c->pair_pack && !c->pair_recompute && c->nslots > d.cap_grec32) {   // packed g, a word a slot
+        if (d.grec32) cudaFree(d.grec32);
+        d.grec32 = nullptr;
+        d.cap_grec32 = 0;
+        const long long n = c->nslots + c->nslots / 8 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.grec32, (size_t)n * sizeof(unsigned)));
+        d.cap_grec32 = n;
+    }
+    if (lrec) {   // block-local indices, a half a slot
+        if (c->nslots > d.cap_lcol16) {
+            if (d.lcol16) cudaFree(d.lcol16);
+            d.lcol16 = nullptr;
+            d.cap_lcol16 = 0;
+            const long long n = c->nslots + c->nslots / 8 + 1024;
+            MPH_CUDA(cudaMalloc((void**)&d.lcol16, (size_t)n * sizeof(unsigned short)));
+            d.cap_lcol16 = n;
+        }
+    } else if (c->nslots * 4 > d.cap_grec16) {   // slot records, 4 halves a slot
         if (d.grec16) cudaFree(d.grec16);
         d.grec16 = nullptr;
         d.cap_grec16 = 0;
@@ -1381,16 +1678,18 @@ int launch_pairs_to_slices(mph_case* c)
     long long pslots = 0;
     MPH_TRY(launch_slice_ptr(c, P.Nf, d.ncp, d.pswidth, d.psptr, &pslots));
     MPH_TRY(grow_f(&d.psval, &d.cap_psval, pslots * 4));   // 16-byte records
+    unsigned short* rec16 = lrec ? nullptr : d.grec16;
+    unsigned* rec32 = c->pair_pack && !c->pair_recompute ? d.grec32 : nullptr;
     if (D == 2) {
         { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       nullptr, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                                       nullptr, d.psval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, d.grec16, d.pscale); MPH_COUNT_LAUNCH(); }
+                                                                      d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
-                                                                       nullptr, d.psval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                                       nullptr, d.psval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return launch_local_cols(c);
 }
@@ -1413,10 +1712,10 @@ int launch_ct_slices(mph_case* c)
     MPH_TRY(grow_f(&d.ctsval, &d.cap_ctsval, slots * 4));   // 16-byte records
     if (D == 2) {
         { k_list_to_slices<2, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, nullptr,
-                                                               d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                               d.ctsval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
         { k_list_to_slices<3, false><<<ns, 256, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, d.ct_ptr, d.ct_j, nullptr, d.ct_v32, nullptr,
-                                                               d.ctsval, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
+                                                               d.ctsval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
 }

@@ -25,6 +25,7 @@
 //         The mixed form's FP32 sweeps on grid-wide levels run three threads
 //         a row (k_mg_sweep3), one stencil plane each.
 #include <cooperative_groups.h>
+#include <mutex>
 #include <type_traits>
 
 #include "mph_device.cuh"
@@ -35,9 +36,15 @@ namespace cg = cooperative_groups;
 
 namespace mph {
 
-constexpr int kCtaRows = 8192;
+#ifndef MPH_CTA_ROWS
+#define MPH_CTA_ROWS 8192
+#endif
+#ifndef MPH_CLUSTER_CTAS
+#define MPH_CLUSTER_CTAS 8
+#endif
+constexpr int kCtaRows = MPH_CTA_ROWS;
 constexpr int kCtaThreads = 1024;
-constexpr int kClusterCtas = 8;
+constexpr int kClusterCtas = MPH_CLUSTER_CTAS;   // above 8: a non-portable cluster size
 constexpr int kDenseRows = 224;   // dense coarse level of the mixed form: n x n floats in one block's shared memory
 
 struct LevelK {
@@ -701,6 +708,12 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
                 A.dense = c->dense_level;
                 A.dinv = c->d.mg_dinv32;
             }
+        }
+        if (kClusterCtas > 8) {
+            static std::once_flag once;
+            std::call_once(once, [] {
+                cudaFuncSetAttribute(k_mg_small_levels<D, T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            });
         }
         { k_mg_small_levels<D, T><<<kClusterCtas, kCtaThreads, 0, st>>>(A, flags); MPH_COUNT_LAUNCH(); }
     }

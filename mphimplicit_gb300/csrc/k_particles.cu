@@ -215,7 +215,7 @@ template <int D>
 __global__ void k_permute(int N, const int* __restrict__ perm, const int* __restrict__ id, const int* __restrict__ type,
                           const double* __restrict__ pos, const double* __restrict__ vel, int* __restrict__ id2,
                           int* __restrict__ type2, double* __restrict__ pos2, double* __restrict__ vel2,
-                          float* __restrict__ pos32, float* __restrict__ poslo32)
+                          float* __restrict__ pos32, float* __restrict__ poslo32, float4* __restrict__ pt2)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
@@ -236,8 +236,10 @@ __global__ void k_permute(int N, const int* __restrict__ perm, const int* __rest
     if (D == 2) {
         reinterpret_cast<float2*>(pos32)[i] = make_float2(h[0], h[1]);
         reinterpret_cast<float2*>(poslo32)[i] = make_float2(l[0], l[1]);
+        pt2[i] = make_float4(h[0], h[1], 0.f, __int_as_float(type[s]));
     } else {
-        reinterpret_cast<float4*>(pos32)[i] = make_float4(h[0], h[1], h[2], 0.f);
+        // w: the type bits (read with the position by the pair-term operator)
+        reinterpret_cast<float4*>(pos32)[i] = make_float4(h[0], h[1], h[2], __int_as_float(type[s]));
         reinterpret_cast<float4*>(poslo32)[i] = make_float4(l[0], l[1], l[2], 0.f);
     }
 }
@@ -340,11 +342,11 @@ void launch_cell_ranges_and_permute(mph_case* c)
     if (c->dim == 2)
         { k_permute<2><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
                                                 c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32,
-                                                c->d.poslo32); MPH_COUNT_LAUNCH(); }
+                                                c->d.poslo32, c->d.pt32); MPH_COUNT_LAUNCH(); }
     else
         { k_permute<3><<<g, 256, 0, c->stream>>>(N, c->d.perm, c->d.id, c->d.type, c->d.pos, c->d.vel, c->d.id_alt,
                                                 c->d.type_alt, c->d.pos_alt, c->d.vel_alt, c->d.pos32,
-                                                c->d.poslo32); MPH_COUNT_LAUNCH(); }
+                                                c->d.poslo32, nullptr); MPH_COUNT_LAUNCH(); }
     std::swap(c->d.id, c->d.id_alt);
     std::swap(c->d.type, c->d.type_alt);
     std::swap(c->d.pos, c->d.pos_alt);

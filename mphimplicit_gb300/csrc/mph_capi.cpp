@@ -173,6 +173,14 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->inner_local = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "pair_recompute") {
+        c->pair_recompute = value != 0.0;
+        return MPH_OK;
+    }
+    if (std::string(name) == "pair_pack") {
+        c->pair_pack = value != 0.0;
+        return MPH_OK;
+    }
     if (std::string(name) == "mixed_extra_sweeps") {
         if (!(value >= 0.0 && value <= 8.0)) return mph::fail(MPH_ERR_ARG, "mixed_extra_sweeps must be 0..8");
         c->mixed_extra_sweeps = (int)value;

@@ -332,6 +332,9 @@ int case_alloc_particles(mph_case* c)
     MPH_TRY(dalloc(c, &d.vel_alt, N * VSn));
     MPH_TRY(dalloc(c, &d.pos32, N * VSn));
     MPH_TRY(dalloc(c, &d.poslo32, N * VSn));
+    if (c->dim == 2) MPH_TRY(dalloc(c, &d.pt32, N));
+    else d.pt32 = reinterpret_cast<float4*>(d.pos32);   // its w holds the type bits
+    MPH_TRY(dalloc(c, &d.wrap32, 1));
     MPH_TRY(dalloc(c, &d.type, N));
     MPH_TRY(dalloc(c, &d.id, N));
     MPH_TRY(dalloc(c, &d.type_alt, N));
@@ -677,7 +680,7 @@ int case_destroy(mph_case* c)
                     (void*)d.mg_invd32, (void*)d.mg_dinv32, (void*)d.pe32, (void*)d.tct, (void*)d.x32, (void*)d.arow32, (void*)d.ct_v32, (void*)d.cval32,
                     (void*)d.tct32, (void*)d.pes32, (void*)d.sdiag32, (void*)d.sdiag64, (void*)d.cvl32, (void*)d.psptr, (void*)d.ctsptr,
                     (void*)d.pswidth, (void*)d.ctswidth, (void*)d.pscol, (void*)d.ctscol, (void*)d.psval, (void*)d.ctsval,
-                    (void*)d.grec16, (void*)d.pscale, (void*)d.uniq, (void*)d.ucount,
+                    (void*)d.grec16, (void*)d.grec32, (void*)d.pscale, (void*)d.lcol16, (void*)d.uniq, (void*)d.ucount,
                     (void*)d.ctuniq, (void*)d.ctucount, (void*)d.wkey, (void*)d.wval, (void*)d.ccell,
                     (void*)d.io3, (void*)d.vprev, (void*)d.vprev_alt, (void*)d.sort_cnt, (void*)d.sort_off, d.scan_tmp})
         if (p) cudaFree(p);

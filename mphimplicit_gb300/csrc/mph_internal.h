@@ -140,6 +140,12 @@ struct DeviceState {
     unsigned short* grec16 = nullptr;  // inner operator slot records: g in FP16 scaled per slice (D halves), block-local index (4th)
     long long cap_grec16 = 0;
     float* pscale = nullptr;           // per slice: g = FP16 g * pscale
+    unsigned* grec32 = nullptr;        // option pair_pack: g per fluid slot, packed fixed point (sliced layout)
+    long long cap_grec32 = 0;
+    unsigned short* lcol16 = nullptr;  // options pair_pack, pair_recompute: block-local index per fluid slot (sliced layout)
+    long long cap_lcol16 = 0;
+    int* wrap32 = nullptr;             // set when a pair of this step's fluid rows is a periodic image
+    float4* pt32 = nullptr;            // FP32 position (high part) and type bits per particle (3D: pos32 itself)
     // block-local neighbour columns of the inner operator (per block its
     // distinct neighbours, kUMax a block, and their count or -1; their
     // maximum, the staged blocks and their columns after the blocks)
@@ -244,6 +250,8 @@ struct mph_case {
     bool factored = true;               // mixed form: FP64 operator in factored form where it applies
     bool inner_blocks = false;          // factored form: inner FP32 SpMV on assembled blocks (else sliced pair terms)
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
+    bool pair_recompute = false;        // pair-term operator: evaluate g from the FP32 positions per slot (else slot records)
+    bool pair_pack = true;              // pair-term operator: 6-byte slot records (packed g, 2-byte index; else FP16, 8 bytes)
     int pair_block = 512;               // threads a block of the pair-term operator (and its row blocks)
     int ct_block = 256;                 // threads a block of the transposed P-list apply (and its particle blocks)
     int chunk = 8;                      // mixed form: CR iterations per captured graph chunk
@@ -261,6 +269,7 @@ struct mph_case {
     cudaEvent_t gev[128] = {};          // event pairs of a profiled CR graph chunk (operators, then V-cycles)
     bool level0_done = false;           // this step's level-0 multigrid stencils were written by the assembly
     int loc_smem = 0;                   // shared memory of k_visc_pen32's staged s (0: gathers by column)
+    int loc_cap = 0;                    // staged neighbours a block of the pair-term operator has room for
     int loc_ct_smem = 0;                // shared memory of k_ct_apply32's staged s (0: gathers by column)
     int loc_blocks[2] = {};             // row blocks staged / gathering by column
     int loc_ct_blocks = 0;              // particle blocks of k_ct_apply32 staging s

@@ -163,16 +163,26 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
     assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 1e-5
 
 
+# slot-record formats of the pair-term operator: FP16 records (8 bytes a
+# slot), packed records (the default: 4-byte fixed-point g and a 2-byte
+# index) and g evaluated from the staged positions
+FORMATS = [("fp16", {"pair_pack": 0}), ("pack", {}), ("recompute", {"pair_recompute": 1})]
+FIDS = [f[0] for f in FORMATS]
+
+
+@pytest.mark.parametrize("fmt", FORMATS, ids=FIDS)
 @pytest.mark.parametrize("case", CASES, ids=IDS)
-def test_staged_and_gathered_operator_give_the_same_bits(engine_lib, case):
+def test_staged_and_gathered_operator_give_the_same_bits(engine_lib, case, fmt):
     """The pair-term operator sums the same terms in the same order whether a
     block reads its neighbours' s from its shared-memory copy or gathers it
     by column (option inner_local 0), so whole mixed steps agree bit for
-    bit."""
+    bit, in every slot-record format."""
     name, dim, params, parts = case
     out = {}
     for local in (1, 0):
         g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        for k, v in fmt[1].items():
+            g.set_option(k, v)
         g.set_option("inner_local", local)
         g.step(2)
         st = g.solve_stats()
@@ -184,14 +194,38 @@ def test_staged_and_gathered_operator_give_the_same_bits(engine_lib, case):
     assert np.array_equal(va, vb) and np.array_equal(pa, pb)
 
 
-def test_mixed_staged_and_gathering_blocks_give_the_same_bits(engine_lib):
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_slot_record_formats_reach_the_same_solution(engine_lib, case):
+    """The three slot-record formats are FP32 (or finer) roundings of one
+    operator used only inside the refinement: refined to 1e-10, their
+    velocities agree to about that, and their iteration counts stay close."""
+    name, dim, params, parts = case
+    res = {}
+    for fid, opts in FORMATS:
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_solver(1e-10, 1e-3, 50)
+        for k, v in opts.items():
+            g.set_option(k, v)
+        g.step(1)
+        st = g.solve_stats()
+        assert st["status"] == 0 and st["inner_form"] == 2, (fid, st)
+        res[fid] = (vec_proj(g.export("Velocity"), dim)[:g.fluid_count], st["iter"])
+    v0, it0 = res["fp16"]
+    for fid in ("pack", "recompute"):
+        v, it = res[fid]
+        assert np.linalg.norm(v - v0) / np.linalg.norm(v0) <= 1e-8, fid
+        assert abs(it - it0) <= max(3, it0 // 10), (fid, it, it0)
+
+
+@pytest.mark.parametrize("fmt", FORMATS, ids=FIDS)
+def test_mixed_staged_and_gathering_blocks_give_the_same_bits(engine_lib, fmt):
     """A case where some row blocks of the pair-term operator have more
     distinct neighbours than one block may stage (RadiusV = 7 l0: about 1400
     neighbours a particle, over 8192 distinct ones for a row block inside
     the 30^3 fluid), so the staged kernel variant meets blocks that
     gather by column (and transposed P-lists that keep their columns): its
     steps agree bit for bit with every block gathering (option inner_local
-    0)."""
+    0), in every slot-record format."""
     from mphimplicit_gb300 import casegen
     parts = casegen.dam_case(3, (30, 30, 30), (36, 34, 34), 0.005, seed=2)
     params = casegen.baseline_params(3, 0.005, 5.0e-5)
@@ -199,13 +233,15 @@ def test_mixed_staged_and_gathering_blocks_give_the_same_bits(engine_lib):
     out = {}
     for local in (1, 0):
         g = engine.Case(params, parts, 3, precision=PRECISION_MIXED)
+        for k, v in fmt[1].items():
+            g.set_option(k, v)
         g.set_option("inner_local", local)
         g.step(2)
         st = g.solve_stats()
         assert st["inner_form"] == 2
         out[local] = (g.export("Velocity"), g.export("Position"), st)
     (va, pa, sa), (vb, pb, sb) = out[1], out[0]
-    print(f"staged {sa['inner_local_blocks']}, gathering {sa['inner_gather_blocks']} row blocks")
+    print(f"{fmt[0]}: staged {sa['inner_local_blocks']}, gathering {sa['inner_gather_blocks']} row blocks")
     assert sa["inner_local_blocks"] > 0 and sa["inner_gather_blocks"] > 0
     assert sa["iter"] == sb["iter"]
     assert np.array_equal(va, vb) and np.array_equal(pa, pb)
