@@ -86,14 +86,16 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` on the bench workload from the
-    committed ncu summary (profiles/), or None."""
+def ncu_traffic(kernel: str, algorithmic_bytes: float):
+    """DRAM bytes per launch of `kernel` on the bench workload: the ratio of
+    DRAM traffic to algorithmic bytes measured by the committed ncu summary
+    (profiles/, captured on a smaller case of the same kernels; traffic grows
+    with the slot counts) times this launch's algorithmic bytes, or None."""
     path = os.path.join(REPO, "profiles", f"{kernel.split('+')[-1]}_cube3d_100.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_launch_full:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    m = re.search(r"dram_to_algorithmic_ratio:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) * algorithmic_bytes if m else None
 
 
 class Clocks:
@@ -198,21 +200,24 @@ def assemble_bytes(prof, scal, dim):
             + dim * 8 * scal["NonzeroCountC"] / dim)
 
 
-def assemble_pair_bytes(prof, scal, dim, case):
+def assemble_pair_bytes(prof, scal, dim, case, jacobi=False, rec_bytes=6):
     """Algorithmic bytes of the mixed form's assembly stage on the pair path
     (no blocks): the neighbour and P-neighbour lists and the particle state
-    read once, and once written what the solve consumes: per fluid slot an
-    8-byte inner record, D FP32 g and a 4-byte column (outer residual); per
+    read once, and once written what the solve consumes: per fluid slot the
+    inner operator's record (rec_bytes: 6 packed, 8 FP16), D FP32 g and a
+    4-byte column (outer residual); per
     P-slot of a fluid row a 16-byte lambda-C record and a 16-byte transposed
     record; per fluid row b (D doubles) and a 32-byte diagonal / inertia
-    record; the level-0 multigrid stencils (doubles)."""
+    record; the level-0 multigrid stencils (doubles), which the point-Jacobi
+    mixed form (jacobi) does not build: it writes D^-1 (D doubles a row)
+    instead."""
     nf = int(scal["FluidParticleEnd"])
     n = int(scal["ParticleCount"])
     slots = scal["NonzeroCountA"] / (dim * dim)
     pslots = scal["NonzeroCountC"] / dim
-    lv0 = case.export("MultiGridCsrCofA:0").size
-    return (4 * prof["nnb"] + 4 * prof["nnbP"] + 64 * n + slots * (12 + 4 * dim) + pslots * 32
-            + nf * (dim * 8 + 32) + lv0 * 8)
+    lv0 = 0 if jacobi else case.export("MultiGridCsrCofA:0").size
+    return (4 * prof["nnb"] + 4 * prof["nnbP"] + 64 * n + slots * (rec_bytes + 4 + 4 * dim) + pslots * 32
+            + nf * (dim * 8 + 32) + lv0 * 8 + (nf * dim * 8 if jacobi else 0))
 
 
 def cpu_sample(threads: int, steps: int = 1, fluid: int = 100, check_gpu: bool = False):
@@ -438,6 +443,7 @@ def run_ensemble(args, line_base):
         g.set_option("extrapolate", args.extrapolate)
         g.set_option("dense_coarse", args.dense_coarse)
         g.set_option("device_loop", args.device_loop)
+        g.set_option("mg_depth", args.mg_depth)
 
     table = None
     if prec == PRECISION_MIXED and args.autotune:
@@ -529,6 +535,7 @@ def run_serve(args, line_base):
         srv.set_option("extrapolate", args.extrapolate)
         srv.set_option("dense_coarse", args.dense_coarse)
         srv.set_option("device_loop", args.device_loop)
+        srv.set_option("mg_depth", args.mg_depth)
     lock = threading.Lock()
     tickets = {}
     t0 = time.perf_counter()
@@ -631,6 +638,10 @@ def main():
     ap.add_argument("--mg-pre", type=int, default=1,
                     help="mixed form: V-cycle sweeps before the coarse correction on the levels below 0 (the reference: 2)")
     ap.add_argument("--mg-post", type=int, default=1, help="mixed form: V-cycle sweeps after it (the reference: 3)")
+    ap.add_argument("--mg-depth", type=int, default=-1,
+                    help="mixed form preconditioner: -1 point Jacobi (no multigrid), 0 the reference's V-cycle over every "
+                         "level, k >= 1 its first k levels")
+    ap.add_argument("--mg-coarsest", type=int, default=4, help="mixed form: sweeps of a grid-wide coarsest level")
     ap.add_argument("--pair-recompute", type=int, default=0, choices=[0, 1],
                     help="mixed form: pair-term operator evaluates its pair terms per slot from the FP32 positions (1) or "
                          "reads them as FP16 slot records (0)")
@@ -712,6 +723,8 @@ def run_single(args, dist, rank, world, local):
             c.set_option("mg_post", args.mg_post)
             c.set_option("pair_recompute", args.pair_recompute)
             c.set_option("pair_pack", args.pair_pack)
+            c.set_option("mg_depth", args.mg_depth)
+            c.set_option("mg_coarsest", args.mg_coarsest)
         c.set_option("cell_sort", args.cell_sort)
         c.set_option("device_loop", args.device_loop)
         if prec_ == PRECISION_MIXED and getattr(args, "tuned_settings", None):
@@ -831,11 +844,13 @@ def run_single(args, dist, rank, world, local):
     bytes_per = kern[dom][1](prof, scal, dim)
     achieved = bytes_per / avg_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(kern[dom][0]) if args.workload == "cube3d_100" else None,
+                "traffic": ncu_traffic(kern[dom][0], bytes_per) if args.workload == "cube3d_100" else None,
                 "kernel": kern[dom][0], "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_per, "avg_launch_ms": avg_s * 1000.0, "launches": nlaunch}
     asm_ms = prof["stage_ms_assemble"] / psteps
-    asm_bytes = (assemble_pair_bytes(prof, scal, dim, case) if pairs else assemble_bytes(prof, scal, dim))
+    asm_bytes = (assemble_pair_bytes(prof, scal, dim, case, jacobi=args.mg_depth < 0,
+                                     rec_bytes={"pack": 6, "fp16": 8, "recompute": 2}[rec]) if pairs
+                 else assemble_bytes(prof, scal, dim))
     roofline_asm = {"bound": "hbm", "achieved": asm_bytes / (asm_ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
                     "frac": asm_bytes / (asm_ms / 1000.0) / 1e9 / peak, "stage": "assemble",
                     "algorithmic_bytes_per_step": asm_bytes, "ms_per_step": asm_ms, "peak_source": peak_kind,
@@ -876,6 +891,8 @@ def run_single(args, dist, rank, world, local):
             c.set_option("mg_post", args.mg_post)
             c.set_option("pair_recompute", args.pair_recompute)
             c.set_option("pair_pack", args.pair_pack)
+            c.set_option("mg_depth", args.mg_depth)
+            c.set_option("mg_coarsest", args.mg_coarsest)
             for k, v in (getattr(args, "tuned_settings", None) or {}).items():
                 c.set_option(k, v)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,

@@ -500,11 +500,19 @@ int launch_assemble(mph_case* c)
         if (c->step_pairs) MPH_TRY(launch_ct_slices(c));
         MPH_TRY(launch_pair_terms(c));
     }
-    if (c->cell_assembly) {
+    // the pair path of the point-Jacobi mixed form has all it needs (b and
+    // D^-1 from k_pair_terms): no level-0 stencils, no per-row kernel
+    const bool skip_rows = c->step_pairs && mixed_jacobi(c);
+    if (c->cell_assembly && !skip_rows) {
         if (c->step_pairs) MPH_TRY(launch_part_pairs(c, M, &cells));   // no blocks: level-0 stencils and D^-1 only
         else MPH_TRY(launch_assemble_cells(c, kmax_rows, c->step_factored, &cells));
     }
     const int* only = cells ? c->d.cell_flags : nullptr;
+    if (skip_rows) {
+        if (c->step_pairs) MPH_TRY(launch_pairs_to_slices(c));
+        if (pon) prof_end(c, 2, pe);
+        return MPH_OK;
+    }
     float* a32 = c->precision == MPH_PRECISION_MIXED ? c->d.aval32 : nullptr;   // null on the pair path
     if (D == 2) {
         { k_matrix_a<2><<<gf, 128, 0, c->stream>>>(P, M, only, c->d.type, c->d.key, c->d.pos, c->d.vel, c->d.force, c->d.nc, c->d.nfc,

@@ -87,7 +87,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
              float4* __restrict__ pe32, double* __restrict__ bvec, float* __restrict__ cvl32, unsigned* __restrict__ gmax,
-             int* __restrict__ wrap)
+             int* __restrict__ wrap, double* __restrict__ dinv)
 {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -102,6 +102,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
         load_f32<D>(pos32, i, hi);
         load_f32<D>(poslo32, i, li);
         float lm = 0.f;                                  // largest |g| component of the fluid slots
+        float tvd[3] = {0.f, 0.f, 0.f}, dpd[3] = {0.f, 0.f, 0.f};   // dinv: viscous and C Lambda C^T diagonals
         for (int k = lane; k < n; k += 32) {
             const int j = nind[nb + k];
             float e[3] = {0.f, 0.f, 0.f};
@@ -142,6 +143,10 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                 }
             }
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
+            if (dinv) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) tvd[d] += f * e[d] * e[d];
+            }
             if (k < nf) lm = fmaxf(lm, sqrtf(f) * fmaxf(fabsf(e[0]), fmaxf(fabsf(e[1]), fabsf(e[2]))));
         }
         if (gmax) {   // the slice's largest |g| component, for the FP16 scale (f >= 0: bits order as values)
@@ -162,7 +167,11 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
             if (cvl32) {   // lambda_k C_ik for the FP32 inner operator
                 const double lam = P.lambda[type[k]];
 #pragma unroll
-                for (int r = 0; r < D; ++r) cvl32[(pb + a) * D + r] = (float)(cval[(pb + a) * D + r] * lam);
+                for (int r = 0; r < D; ++r) {
+                    const float cl = (float)(cval[(pb + a) * D + r] * lam);
+                    cvl32[(pb + a) * D + r] = cl;
+                    dpd[r] += cl * (float)cval[(pb + a) * D + r];
+                }
             }
         }
 #pragma unroll
@@ -173,6 +182,23 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
             const double inert = P.density[ti] * P.vol / P.vol / P.dt;   // as the assembly
 #pragma unroll
             for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
+        }
+        if (dinv) {   // the inverse diagonal of A, FP32 sums (the mixed form's point-Jacobi preconditioner)
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    tvd[r] += __shfl_xor_sync(0xffffffffu, tvd[r], o);
+                    dpd[r] += __shfl_xor_sync(0xffffffffu, dpd[r], o);
+                }
+            if (lane == 0) {
+                const float in32 = P.inert32[ti];
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    const float dg = in32 + tvd[r] + dpd[r];
+                    dinv[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
+                }
+            }
         }
     }
 }
@@ -1523,15 +1549,17 @@ int launch_pair_terms(mph_case* c)
             gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
     }
     MPH_CUDA(cudaMemsetAsync(d.wrap32, 0, sizeof(int), c->stream));
+    // the mixed form without grid levels takes D^-1 from here (no level-0 pass)
+    double* dinv = c->step_pairs && mixed_jacobi(c) ? d.invDiag : nullptr;
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
     const unsigned gw = grid_for((long long)P.Nf * 32, 256);
     if (c->dim == 2) {
         { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<2><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     } else {
         { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32); MPH_COUNT_LAUNCH(); }
+                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<3><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;

@@ -318,6 +318,13 @@ static int grow_f(float** p, long long* cap, long long need)
 int mixed_prepare(mph_case* c)
 {
     DeviceState& d = c->d;
+    if (mixed_jacobi(c)) {   // point Jacobi: the FP32 D^-1 only
+        const long long nv = (long long)c->dp.Nf * c->dim;
+        if (!d.v32) MPH_CUDA(cudaMalloc((void**)&d.v32, (size_t)nv * 8 * sizeof(float)));
+        c->dense_level = -1;
+        { k_convert<double, float><<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, d.invDiag, d.v32 + 7 * nv); MPH_COUNT_LAUNCH(); }
+        return MPH_OK;
+    }
     MPH_TRY(grow_f(&d.mg_cof32, &d.cap_mg_cof32, c->mg_cof_total));
     if (c->mg_rows_total > d.cap_mg_vec32) {
         for (float** b : {&d.mg_invd32, &d.mg_q32, &d.mg_s32, &d.mg_r32, &d.mg_res32}) {

@@ -446,6 +446,24 @@ __global__ void k_mg_g2p_dot(DevParams P, LevelK L, const int* __restrict__ key,
     reduce_finalize(acc, partials, counter, out);
 }
 
+// u = D^-1 q with the (q, u) dot: the preconditioner without grid levels
+// (mixed form, option mg_depth -1)
+template <typename TQ>
+__global__ void k_jacobi_dot(long long n, const TQ* __restrict__ invDiag, const TQ* __restrict__ q, TQ* __restrict__ u,
+                             double* __restrict__ partials, unsigned* __restrict__ counter, double* __restrict__ out,
+                             const int* __restrict__ flags)
+{
+    if (flags[kFlagDone]) return;
+    double acc = 0.0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const TQ qk = q[k];
+        const TQ v = invDiag[k] * qk;
+        u[k] = v;
+        acc += (double)qk * (double)v;
+    }
+    reduce_finalize(acc, partials, counter, out);
+}
+
 // ---- the small levels in one block ------------------------------------------------
 template <typename T>
 struct CoarseArgs {
@@ -631,12 +649,21 @@ template <int D, typename T, typename TQ>
 static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T* cof, const T* invd, T* Qp, T* Sa, T* Sb,
                      T* Rp, double* dot_out, int extra0 = 0)
 {
-    const int depth = c->depth;
+    // sweeps of the levels below level 0: the reference's 2 and 3, or the
+    // mixed form's options mg_pre / mg_post; the mixed form's option mg_depth
+    // (>= 2) cuts the cycle after that many levels (the last one coarsest)
+    const bool mixed = std::is_same<T, float>::value;
+    if (mixed && c->mg_depth < 0) {   // no grid levels: point Jacobi on the particles
+        const long long n = (long long)c->dp.Nf * D;
+        const int blocks = std::min<int>(grid_for(n, 256), kReduceBlocks);
+        { k_jacobi_dot<TQ><<<blocks, 256, 0, c->stream>>>(n, invDiag, q, u, c->d.partials, (unsigned*)(c->d.flags + kFlagCounter),
+                                                         dot_out, c->d.flags); MPH_COUNT_LAUNCH(); }
+        return;
+    }
+    const int depth = mixed && c->mg_depth >= 1 ? std::min(c->depth, c->mg_depth) : c->depth;
+    const int coarsest = mixed ? c->mg_coarsest : 4;   // sweeps of the coarsest grid-wide level
     cudaStream_t st = c->stream;
     const int* flags = c->d.flags;
-    // sweeps of the levels below level 0: the reference's 2 and 3, or the
-    // mixed form's options mg_pre / mg_post
-    const bool mixed = std::is_same<T, float>::value;
     const int pre = mixed ? c->mg_pre : 2, post = mixed ? c->mg_post : 3;
     LevelK L[kMaxLevels];
     for (int l = 0; l < depth; ++l) L[l] = level_k(c, l);
@@ -681,7 +708,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         residual(l - 1);
         { k_mg_restrict<D, T><<<grid_for(L[l].rows, 128), 128, 0, st>>>(L[l - 1], L[l], Rp + ov(l - 1), invd + ov(l), Qp + ov(l),
                                                                         cur[l], flags); MPH_COUNT_LAUNCH(); }
-        const int sweeps = (l == depth - 1) ? 4 : pre;   // coarsest: 4 sweeps + one more update
+        const int sweeps = (l == depth - 1) ? coarsest : pre;   // coarsest: 4 sweeps + one more update
         for (int k = 0; k < sweeps; ++k) jacobi(l);
     }
     if (first < depth) {
@@ -704,7 +731,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         A.dense = -1;
         A.dinv = nullptr;
         if constexpr (std::is_same<T, float>::value) {
-            if (c->dense_level >= first) {
+            if (c->dense_level >= first && c->dense_level < depth) {
                 A.dense = c->dense_level;
                 A.dinv = c->d.mg_dinv32;
             }
@@ -723,7 +750,7 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
         { k_mg_prolong<D, T><<<grid_for(L[l - 1].rows, 128), 128, 0, st>>>(L[l - 1], L[l], cur[l], cur[l - 1], flags); MPH_COUNT_LAUNCH(); }
     };
     int top = first - 1;
-    if (first == depth) {
+    if (first == depth && depth > 1) {
         prolong(depth - 1);
         top = depth - 2;
     }
@@ -745,12 +772,13 @@ static void vcycle_t(mph_case* c, const TQ* q, TQ* u, const TQ* invDiag, const T
 int mixed_dense_coarse(mph_case* c)
 {
     c->dense_level = -1;
-    if (!c->dense_coarse) return MPH_OK;
-    int first = c->depth;
-    for (int l = 1; l < c->depth; ++l)
+    if (!c->dense_coarse || c->mg_depth < 0) return MPH_OK;
+    const int depth = c->mg_depth >= 1 ? std::min(c->depth, c->mg_depth) : c->depth;   // the cycle's levels
+    int first = depth;
+    for (int l = 1; l < depth; ++l)
         if (c->lv[l].rows <= kCtaRows) { first = l; break; }
     int lev = -1;
-    for (int l = first; l < c->depth; ++l)
+    for (int l = first; l < depth; ++l)
         if (c->lv[l].rows <= kDenseRows) { lev = l; break; }
     if (lev < 0) return MPH_OK;
     const int n = c->lv[lev].rows;

@@ -177,6 +177,19 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->pair_recompute = value != 0.0;
         return MPH_OK;
     }
+    if (std::string(name) == "mg_depth") {
+        const int v = (int)value;
+        if ((double)v != value || v < -1 || v > 24)
+            return mph::fail(MPH_ERR_ARG, "option mg_depth: 0 (every level), 1 .. 24 levels, or -1 (no grid levels)");
+        c->mg_depth = v;
+        return MPH_OK;
+    }
+    if (std::string(name) == "mg_coarsest") {
+        const int v = (int)value;
+        if ((double)v != value || v < 1 || v > 8) return mph::fail(MPH_ERR_ARG, "option mg_coarsest: 1 .. 8 sweeps");
+        c->mg_coarsest = v;
+        return MPH_OK;
+    }
     if (std::string(name) == "pair_pack") {
         c->pair_pack = value != 0.0;
         return MPH_OK;

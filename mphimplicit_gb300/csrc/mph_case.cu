@@ -554,6 +554,10 @@ int ensure_mg_cof(mph_case* c)
 int stage_mg_build(mph_case* c)
 {
     if (c->stage < 5) return fail(MPH_ERR_STATE, "multigrid build before assembly");
+    if (mixed_jacobi(c)) {   // no multigrid levels in the point-Jacobi mixed form
+        c->stage = 6;
+        return MPH_OK;
+    }
     MPH_TRY(ensure_mg_cof(c));
     if (c->mg_rows_total > c->d.cap_mg_vec) {
         for (double** b : {&c->d.mg_invd, &c->d.mg_q, &c->d.mg_s, &c->d.mg_r, &c->d.mg_res}) {

@@ -180,6 +180,7 @@ static int build_export(mph_case* c, const std::string& name, Out& o)
         const std::string base = name.substr(0, colon);
         const int L = std::atoi(name.c_str() + colon + 1);
         if (L < 0 || L >= c->depth) return fail(MPH_ERR_ARG, "no such multigrid level");
+        if (mixed_jacobi(c)) return fail(MPH_ERR_STATE, "the point-Jacobi mixed form builds no multigrid levels");
         const LevelGeom& g = c->lv[L];
         if (base == "MultiGridCsrCofA") {
             // stored entry-major; returned row-major like the reference's CSR rows

@@ -257,6 +257,8 @@ struct mph_case {
     int chunk = 8;                      // mixed form: CR iterations per captured graph chunk
     int cell_sort = 0;                  // 0: the reference's bitonic network (bit-exact order); 1: counting sort
     int mg_pre = 1, mg_post = 1;        // mixed form: sweeps of the V-cycle's levels below level 0 (the reference's: 2 and 3)
+    int mg_depth = -1;                  // mixed form: -1 point Jacobi (no multigrid), 0 every level, k >= 1 the first k
+    int mg_coarsest = 4;                // mixed form: sweeps of a coarsest level run grid-wide (the reference's 4)
     bool dense_coarse = true;           // mixed form: solve the first one-block coarse level of <= 224 rows exactly
     int dense_level = -1;               // this step's exactly solved level (-1: none)
     int extrapolate = 0;                // mixed form: CR start from the last 1 + extrapolate start velocities
@@ -373,6 +375,9 @@ int launch_assemble(mph_case* c);
 int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done);
 int build_ct(mph_case* c);
 bool factored_applies(const mph_case* c);
+// the mixed form preconditioned by point Jacobi (option mg_depth -1): no
+// multigrid levels are built or used
+inline bool mixed_jacobi(const mph_case* c) { return c->precision == MPH_PRECISION_MIXED && c->mg_depth < 0; }
 bool pair_path_expected(const mph_params* prm, const mph_particles* parts, int dim);
 int launch_pair_terms(mph_case* c);
 void launch_resid_factored(mph_case* c, const double* x, double* r, double* out);

@@ -83,6 +83,7 @@ def test_fp32_cell_assembly_of_the_factored_form(engine_lib, case):
     name, dim, params, parts = case
     a = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
     a.set_option("inner_blocks", 1)   # keep the FP32 blocks to compare them
+    a.set_option("mg_depth", 0)       # and the multigrid levels
     b = _assembled(params, parts, dim, True)
     for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
         a.stage(st)
@@ -103,19 +104,21 @@ def test_fp32_cell_assembly_of_the_factored_form(engine_lib, case):
 
 @pytest.mark.parametrize("case", CASES, ids=IDS)
 def test_pair_term_inner_operator_solves(engine_lib, case):
-    """The mixed form with its inner SpMV on the FP32 pair terms (no blocks)
-    reaches the FP64 form's velocity."""
+    """The mixed form with its inner SpMV on the FP32 pair terms (no blocks),
+    refined to 1e-10, reaches the FP64 form's velocity solved to 1e-12."""
     name, dim, params, parts = case
     a = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
     a.set_option("inner_blocks", 0)
+    a.set_solver(1e-10, 1e-3, 50)
     b = engine.Case(params, parts, dim)
+    b.set_solver(1e-12, 1e-3, 50)
     a.step(1)
     b.step(1)
     assert a.solve_stats()["status"] == 0
     nf = a.fluid_count
     va = vec_proj(a.export("Velocity"), dim)[:nf]
     vb = vec_proj(b.export("Velocity"), dim)[:nf]
-    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 2e-5
+    assert np.linalg.norm(va - vb) / np.linalg.norm(vb) <= 1e-8
 
 
 @pytest.mark.parametrize("case", CASES, ids=IDS)
@@ -132,6 +135,7 @@ def test_sliced_pair_terms_match_blocks(engine_lib, case):
     for blocks in (1, 0):
         g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
         g.set_option("inner_blocks", blocks)
+        g.set_option("mg_depth", 0)   # the multigrid-preconditioned form, whose levels are compared
         for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
             g.stage(st)
         cols = g.export("CsrIndA")
@@ -245,3 +249,31 @@ def test_mixed_staged_and_gathering_blocks_give_the_same_bits(engine_lib, fmt):
     assert sa["inner_local_blocks"] > 0 and sa["inner_gather_blocks"] > 0
     assert sa["iter"] == sb["iter"]
     assert np.array_equal(va, vb) and np.array_equal(pa, pb)
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_point_jacobi_diagonal_and_solution(engine_lib, case):
+    """The point-Jacobi mixed form (the default, option mg_depth -1) takes D^-1
+    from the pair-term kernel instead of the level-0 pass: the same FP32 sums
+    of the diagonal in another order (rel 1e-6), no multigrid levels, and a
+    step refined to 1e-10 reaches the multigrid-preconditioned form's
+    velocity to about that."""
+    name, dim, params, parts = case
+    res = {}
+    for depth in (-1, 0):
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_solver(1e-10, 1e-3, 50)
+        g.set_option("mg_depth", depth)
+        for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build"):
+            g.stage(st)
+        dinv = g.export("InvDiagA")
+        if depth < 0:
+            with pytest.raises(engine.MphError):
+                g.export("MultiGridCsrCofA:0")
+        g.stage("solve")
+        st = g.solve_stats()
+        assert st["status"] == 0 and st["inner_form"] == 2
+        res[depth] = (dinv, vec_proj(g.export("Velocity"), dim)[:g.fluid_count])
+    (dj, vj), (dm, vm) = res[-1], res[0]
+    assert rel(dj, dm) <= 1e-6
+    assert np.linalg.norm(vj - vm) / np.linalg.norm(vm) <= 1e-8
