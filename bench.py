@@ -155,6 +155,14 @@ def spmv_bytes(prof, scal, dim, vb=8):
     return blocks * (dim * dim * vb + 4) + nf * 4 + (nsl + 1) * 8 + 2 * dim * nf * vb
 
 
+def precond_name(args, mixed: bool) -> str:
+    if not mixed:
+        return "multigrid V-cycle (the reference's)"
+    if args.mg_depth < 0:
+        return "point Jacobi, fused with the CR vector update"
+    return "multigrid V-cycle, " + ("every level" if args.mg_depth == 0 else f"{args.mg_depth} level(s)")
+
+
 def pair_apply_bytes(prof, scal, dim, st=None, rec="pack"):
     """Algorithmic bytes of one FP32 inner operator on the sliced pair terms
     (k_ct_apply32 + k_visc_pen32).  k_ct_apply32: column + D FP32 C values per
@@ -505,6 +513,7 @@ def run_ensemble(args, line_base):
                    "precision": args.precision, "workers": args.workers, "parallelism": "single",
                    "outer_tol": args.outer_tol if prec == PRECISION_MIXED else 1e-6,
                    "cr_start": "quadratic extrapolation" if args.extrapolate == 2 and prec == PRECISION_MIXED else "v_n",
+                   "preconditioner": precond_name(args, prec == PRECISION_MIXED),
                    "autotune": {k: v["settings"] for k, v in table.items()} if table else None,
                    "l2": "inputs larger than L2 (the cases' matrices total ~GBs)",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
@@ -592,6 +601,7 @@ def run_serve(args, line_base):
                    "1e4..5e5 particles log-uniform, steps U[50,400] x step scale, 150 GB admission budget (config 4)",
                    "requests": len(reqs), "step_scale": args.serve_step_scale, "precision": args.precision,
                    "outer_tol": args.outer_tol if prec == PRECISION_MIXED else 1e-6,
+                   "preconditioner": precond_name(args, prec == PRECISION_MIXED),
                    "workers": args.workers, "parallelism": "single", "particle_steps": psteps, "span_s": span,
                    "l2": "inputs larger than L2",
                    "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
@@ -915,6 +925,7 @@ def run_single(args, dist, rank, world, local):
                    "cr_start": {0: "v_n (the reference's)", 1: "linear extrapolation of the last start velocities",
                                 2: "quadratic extrapolation of the last start velocities"}[args.extrapolate]
                    if prec == PRECISION_MIXED else "v_n (the reference's)",
+                   "preconditioner": precond_name(args, prec == PRECISION_MIXED),
                    "inner_row_blocks": {"staged": st.get("inner_local_blocks"), "gathering": st.get("inner_gather_blocks"),
                                         "ct_blocks_staging_s": st.get("inner_ct_local_blocks"),
                                         "mean_distinct_cols": (st["inner_local_cols"] / st["inner_local_blocks"]
@@ -924,8 +935,8 @@ def run_single(args, dist, rank, world, local):
                                          ("step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve")},
                    "stage_sum_ms_per_step": stage_total / psteps,
                    "kernel_avg_ms": {k: (prof[f"kern_ms_{k}"] / prof[f"kern_n_{k}"] if prof[f"kern_n_{k}"] else None)
-                                     for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
-                   "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "vcycle", "assemble_a", "neighbors")},
+                                     for k in ("spmv", "precond", "assemble_a", "neighbors")},
+                   "kernel_launches": {k: prof[f"kern_n_{k}"] for k in ("spmv", "precond", "assemble_a", "neighbors")},
                    "plain_fp64_value": plain,
                    "plain_fp64_cr_iterations": plain_iters if plain else None,
                    "speedup_vs_plain_fp64": (value / plain) if plain else None,

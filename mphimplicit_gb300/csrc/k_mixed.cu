@@ -102,6 +102,29 @@ __global__ void k_pq32(int n, const V* __restrict__ s, const V* __restrict__ y, 
     }
 }
 
+// The same update fused with the point-Jacobi preconditioner of the mixed
+// form: u = D^-1 q and (q, u) -> kSQU32 in the same pass.
+template <typename V>
+__global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restrict__ y, V* __restrict__ p, V* __restrict__ q,
+                              const V* __restrict__ invD, V* __restrict__ u, double* __restrict__ scal,
+                              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
+{
+    if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
+    const V beta = it == 0 ? (V)0 : (V)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
+    double acc = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const V pk = it == 0 ? s[k] : beta * p[k] + s[k];
+        const V qk = it == 0 ? y[k] : beta * q[k] + y[k];
+        p[k] = pk;
+        q[k] = qk;
+        const V uk = invD[k] * qk;
+        u[k] = uk;
+        acc += (double)qk * (double)uk;
+    }
+    reduce_finalize(acc, partials, counter, scal + kSQU32);
+}
+
 // z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
 // then advances the iteration counter flags[kFlagIter].
 // In the device-driven solve (use_cond) the last block also applies the
@@ -348,6 +371,24 @@ int mixed_prepare(mph_case* c)
 
 void vcycle_mixed(mph_case* c, const float* q, float* u, double* dot_out);
 
+// p = beta p + s, q = beta q + y and u = M q with (q, u): the point-Jacobi
+// mixed form in one kernel, else the update and the V-cycle
+static void pq_precond(mph_case* c, cudaStream_t st, int n, unsigned rb, const float* s32, const float* y32, float* p32,
+                       float* q32, float* u32)
+{
+    DeviceState& d = c->d;
+    double* scal = d.scal;
+    const int* flags = d.flags;
+    if (mixed_jacobi(c)) {
+        const float* invD = d.v32 + 7 * (size_t)c->dp.Nf * c->dim;
+        { k_pq_jacobi32<float><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, invD, u32, scal, flags, d.partials,
+                                                              (unsigned*)(d.flags + kFlagCounter)); MPH_COUNT_LAUNCH(); }
+        return;
+    }
+    { k_pq32<float><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+    vcycle_mixed(c, q32, u32, scal + kSQU32);
+}
+
 static void fill_mixed_stats(mph_case* c, int total_inner, int outer, const double* hs, bool bad, double tol_out2)
 {
     c->stats.iterations = total_inner;
@@ -494,8 +535,7 @@ static int device_solve(mph_case* c, double* hs, int* hflags)
                     k_spmv32<D, 1, V><<<gs, 128, 0, s3>>>(Nf, d.nfc, d.sptr, d.acol, d.aval32, s32, y32, scal, flags, cap, part, counter);
                     MPH_COUNT_LAUNCH();
                 }
-                { k_pq32<V><<<rb, kReduceThreads, 0, s3>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
-                vcycle_mixed(c, q32, u32, scal + kSQU32);
+                pq_precond(c, s3, n, rb, s32, y32, p32, q32, u32);
                 { k_xrs32<V><<<rb, kReduceThreads, 0, s3>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter, loop_cap,
                                                              1, h_in); MPH_COUNT_LAUNCH(); }
                 l_iter = t_launch_count - li0;
@@ -628,10 +668,16 @@ static int mixed_solve_t(mph_case* c)
         }
         if (ev_end) cudaEventRecordWithFlags(ev_end, st, cudaEventRecordExternal);   // profiled graph: the operator's end
         else if (e) prof_begin(c, 0, &e[1]);
-        { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
-        if (ev_v0) cudaEventRecordWithFlags(ev_v0, st, cudaEventRecordExternal);   // profiled graph: the V-cycle
-        vcycle_mixed(c, q32, u32, scal + kSQU32);
-        if (ev_v1) cudaEventRecordWithFlags(ev_v1, st, cudaEventRecordExternal);
+        if (mixed_jacobi(c)) {   // profiled graph: the update fused with the preconditioner
+            if (ev_v0) cudaEventRecordWithFlags(ev_v0, st, cudaEventRecordExternal);
+            pq_precond(c, st, n, rb, s32, y32, p32, q32, u32);
+            if (ev_v1) cudaEventRecordWithFlags(ev_v1, st, cudaEventRecordExternal);
+        } else {
+            { k_pq32<V><<<rb, kReduceThreads, 0, st>>>(n, s32, y32, p32, q32, scal, flags); MPH_COUNT_LAUNCH(); }
+            if (ev_v0) cudaEventRecordWithFlags(ev_v0, st, cudaEventRecordExternal);   // profiled graph: the V-cycle
+            vcycle_mixed(c, q32, u32, scal + kSQU32);
+            if (ev_v1) cudaEventRecordWithFlags(ev_v1, st, cudaEventRecordExternal);
+        }
         { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
     const int chunk = c->chunk;

@@ -253,7 +253,7 @@ class Case:
             _check(n)
         v = list(buf)
         stages = ["step_begin", "cellsort", "neighbors", "explicit", "assemble", "mg_build", "solve"]
-        kern = ["spmv", "vcycle", "assemble_a", "neighbors"]
+        kern = ["spmv", "precond", "assemble_a", "neighbors"]
         out = {f"stage_ms_{s}": v[k] for k, s in enumerate(stages)}
         out.update({f"kern_ms_{s}": v[7 + k] for k, s in enumerate(kern)})
         out.update({f"kern_n_{s}": int(v[11 + k]) for k, s in enumerate(kern)})
