@@ -17,12 +17,13 @@
 
 namespace mph {
 
-__global__ void k_slice_width(int Nf, const int* __restrict__ nfc, int* __restrict__ width32)
+__global__ void k_slice_width(int Nf, const int* __restrict__ nfc, int* __restrict__ width32, int pad = 1)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int v = i < Nf ? nfc[i] : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    v = (v + pad - 1) / pad * pad;
     if ((threadIdx.x & 31) == 0 && i < ((Nf + 31) / 32) * 32) width32[i >> 5] = 32 * v;
 }
 
@@ -409,7 +410,10 @@ int launch_assemble(mph_case* c)
     const int D = c->dim;
     // slice pointers
     c->nslices = (Nf + 31) / 32;
-    { k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth); MPH_COUNT_LAUNCH(); }
+    // the fluid rows' slices padded to a multiple of 4 slots (zero padding
+    // records): the pair-term operator then loops over whole slices in steps
+    // of four without per-slot bounds tests
+    { k_slice_width<<<grid_for((long long)c->nslices * 32, 256), 256, 0, c->stream>>>(Nf, c->d.nfc, c->d.swidth, 4); MPH_COUNT_LAUNCH(); }
     MPH_CUDA(cudaMemsetAsync(c->d.dmax, 0, sizeof(int), c->stream));
     { k_max_int<<<grid_for(c->nslices, 256), 256, 0, c->stream>>>(c->d.swidth, c->nslices, c->d.dmax); MPH_COUNT_LAUNCH(); }
     MPH_TRY(launch_scan_i32_to_i64(c, c->d.swidth, c->d.sptr, c->nslices));

@@ -68,6 +68,12 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 constexpr int kUMax = 8192;
 constexpr int kWinWords = 1 << 13;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
+// floats a staged s takes in shared memory in 3-D (3: packed, the default;
+// 4: one 16-byte load, measured slower for the wider bank-conflict pattern)
+#ifndef MPH_XS3
+#define MPH_XS3 3
+#endif
+constexpr int kXs3 = MPH_XS3;
 
 
 // (e, f) of every neighbour slot of the fluid rows in FP32, and b
@@ -399,7 +405,8 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
                                                     const double* __restrict__ scal, int* __restrict__ flags, int cap,
                                                     const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
-    extern __shared__ float xs_ct[];
+    extern __shared__ float xs_ct[];   // LOC: s of the lists' fluid rows by rank, a float4 (3-D) or float2 (2-D) each
+    constexpr int XS = D == 3 ? kXs3 : 2;
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const double tol2 = scal[kSTol2];
@@ -423,7 +430,7 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
             for (int a = threadIdx.x; a < U; a += blockDim.x) {
                 const int j = ul[a];
 #pragma unroll
-                for (int d = 0; d < D; ++d) xs_ct[a * D + d] = x[(size_t)j * D + d];
+                for (int d = 0; d < D; ++d) xs_ct[a * XS + d] = x[(size_t)j * D + d];
             }
             __syncthreads();
         }
@@ -431,16 +438,38 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
     if (k >= N) return;
     const int lane = k & 31;
     const float4* rp = ctrec + ctsptr[k >> 5] + lane;
-    const float* xb = (LOC && U >= 0) ? xs_ct : x;   // by rank from shared memory, or by column
     float s = 0.f;
     const int n = ctcnt[k];
+    if (LOC && U >= 0) {   // by rank from shared memory
 #pragma unroll 4
-    for (int e = 0; e < n; ++e) {
-        const float4 r = __ldcs(rp + (long long)e * 32);
-        const float* xj = xb + (size_t)__float_as_int(r.w) * D;
-        s += r.x * xj[0];
-        s += r.y * xj[1];
-        if (D == 3) s += r.z * xj[2];
+        for (int e = 0; e < n; ++e) {
+            const float4 r = __ldcs(rp + (long long)e * 32);
+            float xj[3];
+            if (D == 3) {
+                if (kXs3 == 4) {
+                    const float4 v = reinterpret_cast<const float4*>(xs_ct)[__float_as_int(r.w)];
+                    xj[0] = v.x; xj[1] = v.y; xj[2] = v.z;
+                } else {
+                    const float* v = xs_ct + (size_t)__float_as_int(r.w) * 3;
+                    xj[0] = v[0]; xj[1] = v[1]; xj[2] = v[2];
+                }
+            } else {
+                const float2 v = reinterpret_cast<const float2*>(xs_ct)[__float_as_int(r.w)];
+                xj[0] = v.x; xj[1] = v.y; xj[2] = 0.f;
+            }
+            s += r.x * xj[0];
+            s += r.y * xj[1];
+            if (D == 3) s += r.z * xj[2];
+        }
+    } else {   // by column
+#pragma unroll 4
+        for (int e = 0; e < n; ++e) {
+            const float4 r = __ldcs(rp + (long long)e * 32);
+            const float* xj = x + (size_t)__float_as_int(r.w) * D;
+            s += r.x * xj[0];
+            s += r.y * xj[1];
+            if (D == 3) s += r.z * xj[2];
+        }
     }
     t[k] = s;
 }
@@ -497,9 +526,12 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     yv[0] = s0.x * xi[0] + s0.y * xi[1] + s0.z * xi[2];
     yv[1] = s0.y * xi[0] + s0.w * xi[1] + s1.x * xi[2];
     yv[2] = s0.z * xi[0] + s1.x * xi[1] + s1.y * xi[2];
-    const long long base = sptr[i >> 5] + lane;
+    // whole slices (a multiple of R slots; padding records are zero and
+    // point at column 0 / rank 0, so they add exact zeros): no per-slot tests
+    const long long sb = sptr[i >> 5];
+    const int w = (int)((sptr[(i >> 5) + 1] - sb) >> 5);
+    const long long base = sb + lane;
     const int* cp = acol + base;
-    const int n = nfc[i];
     float ys[3] = {0.f, 0.f, 0.f};
     constexpr int R = kPairUnroll;
     uint2 cur[R];
@@ -507,29 +539,52 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
 #pragma unroll
     for (int u = 0; u < R; ++u) {
         cur[u] = pre[u];
-        ccur[u] = (!LOC && u < n) ? __ldcs(cp + (long long)u * 32) : 0;
+        ccur[u] = (!LOC && u < w) ? __ldcs(cp + (long long)u * 32) : 0;
     }
-    for (int k0 = 0; k0 < n; k0 += R) {
+    for (int k0 = 0; k0 < w; k0 += R) {
         uint2 nxt[R];
         int cnxt[R];
+        if (k0 + R < w) {   // warp-uniform
 #pragma unroll
-        for (int u = 0; u < R; ++u) {
-            const int k = k0 + R + u;
-            nxt[u] = k < n ? load_slot<PACK, LOC>(r16, r32, l16, base + (long long)k * 32) : make_uint2(0u, 0u);
-            cnxt[u] = (!LOC && k < n) ? __ldcs(cp + (long long)k * 32) : 0;
+            for (int u = 0; u < R; ++u) {
+                const long long e = base + (long long)(k0 + R + u) * 32;
+                nxt[u] = load_slot<PACK, LOC>(r16, r32, l16, e);
+                cnxt[u] = !LOC ? __ldcs(cp + (e - base)) : 0;
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+                nxt[u] = make_uint2(0u, 0u);
+                cnxt[u] = 0;
+            }
         }
 #pragma unroll
         for (int u = 0; u < R; ++u) {
-            if (k0 + u < n) {
-                float g[3];
-                const int lj = decode_slot<D, PACK>(cur[u], g);
-                const float* xj = LOC ? xs + (size_t)lj * D : x + (size_t)ccur[u] * D;
-                float gx = 0.f;
+            float g[3];
+            const int lj = decode_slot<D, PACK>(cur[u], g);
+            float xj[3];
+            if (LOC) {   // staged s: a float4 (3-D) or float2 (2-D) per neighbour
+                if (D == 3) {
+                    if (kXs3 == 4) {
+                        const float4 v = reinterpret_cast<const float4*>(xs)[lj];
+                        xj[0] = v.x; xj[1] = v.y; xj[2] = v.z;
+                    } else {
+                        const float* v = xs + (size_t)lj * 3;
+                        xj[0] = v[0]; xj[1] = v[1]; xj[2] = v[2];
+                    }
+                } else {
+                    const float2 v = reinterpret_cast<const float2*>(xs)[lj];
+                    xj[0] = v.x; xj[1] = v.y; xj[2] = 0.f;
+                }
+            } else {
 #pragma unroll
-                for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - xj[d]);
-#pragma unroll
-                for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
+                for (int d = 0; d < D; ++d) xj[d] = x[(size_t)ccur[u] * D + d];
             }
+            float gx = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) gx += g[d] * (xi[d] - xj[d]);
+#pragma unroll
+            for (int d = 0; d < D; ++d) ys[d] += gx * g[d];
         }
 #pragma unroll
         for (int u = 0; u < R; ++u) {
@@ -552,18 +607,21 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
              const int* __restrict__ uniq, const int* __restrict__ ucount)
 {
-    extern __shared__ float xs_loc[];   // LOC: s of the block's distinct fluid neighbours, by block-local index
+    // LOC: s of the block's distinct fluid neighbours by block-local index,
+    // a float4 (3-D) or float2 (2-D) each
+    extern __shared__ float xs_loc[];
+    constexpr int XS = D == 3 ? kXs3 : 2;
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint2* r16 = reinterpret_cast<const uint2*>(grec);
     uint2 pre[kPairUnroll];   // the row's first slot records, in flight while s is staged
     {
-        const int n0 = i < Nf ? nfc[i] : 0;
-        const long long b0 = i < Nf ? sptr[i >> 5] + (i & 31) : 0;
+        const long long s0 = i < Nf ? sptr[i >> 5] : 0;
+        const int w0 = i < Nf ? (int)((sptr[(i >> 5) + 1] - s0) >> 5) : 0;
 #pragma unroll
         for (int u = 0; u < kPairUnroll; ++u)
-            pre[u] = u < n0 ? load_slot<PACK, LOC>(r16, grec32, lcol, b0 + (long long)u * 32) : make_uint2(0u, 0u);
+            pre[u] = u < w0 ? load_slot<PACK, LOC>(r16, grec32, lcol, s0 + (i & 31) + (long long)u * 32) : make_uint2(0u, 0u);
     }
     int U = -1;
     if (LOC) {   // stage s of the block's distinct neighbours once (block-uniform)
@@ -574,7 +632,7 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
             for (int k = threadIdx.x; k < U; k += blockDim.x) {
                 const int j = ul[k];
 #pragma unroll
-                for (int d = 0; d < D; ++d) xs_loc[k * D + d] = x[(size_t)j * D + d];
+                for (int d = 0; d < D; ++d) xs_loc[k * XS + d] = x[(size_t)j * D + d];
             }
             __syncthreads();
         }
@@ -1432,6 +1490,10 @@ __global__ void __launch_bounds__(MPH_PAIR_BLOCK) k_local_cols(int Nf, const lon
         const unsigned word = bm[off >> 5];
         out16[e * OS + OO] = (OutT)(rank[off >> 5] + __popc(word & ((1u << (off & 31)) - 1u)));
     }
+    if (row) {   // the slice's padding slots (zero records) point at rank 0
+        const int w = (int)((sptr[(i >> 5) + 1] - sptr[i >> 5]) >> 5);
+        for (int k = n; k < w; ++k) out16[(base + (long long)k * 32) * OS + OO] = (OutT)0;
+    }
     int* ul = uniq + (size_t)blockIdx.x * kUMax;
     for (int w = w0; w < w1; ++w) {
         unsigned word = bm[w];
@@ -1643,8 +1705,9 @@ static int launch_local_cols(mph_case* c)
     c->loc_cols = xcap ? (long long)(unsigned)h[0][2] : 0;
     c->loc_ct_blocks = ctcap ? h[1][1] : 0;
     c->loc_cap = xcap;
-    c->loc_smem = xcap * (c->pair_recompute ? (int)sizeof(float4) + D * (int)sizeof(float) : D * (int)sizeof(float));
-    c->loc_ct_smem = ctcap * D * (int)sizeof(float);
+    const int xs = D == 3 ? kXs3 : 2;   // floats a staged s (float4 / float2)
+    c->loc_smem = xcap * (c->pair_recompute ? (int)sizeof(float4) + D * (int)sizeof(float) : xs * (int)sizeof(float));
+    c->loc_ct_smem = ctcap * xs * (int)sizeof(float);
     if (c->pair_recompute && c->loc_smem > rc_smem_max(D)) {   // a block's records do not fit: every block gathers
         c->loc_smem = 0;
         c->loc_blocks[1] += c->loc_blocks[0];
@@ -1657,10 +1720,10 @@ static int launch_local_cols(mph_case* c)
         MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(2)));
         MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
     } else {
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
         MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(3)));
-        MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 3 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
     }
     return MPH_OK;
 }
