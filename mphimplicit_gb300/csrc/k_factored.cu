@@ -68,6 +68,9 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 constexpr int kUMax = 8192;
 constexpr int kWinWords = 1 << 13;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
+// the fluid slices are padded to a multiple of 4 slots (k_slice_width), which
+// the operator's whole-slice loop steps through kPairUnroll at a time
+static_assert(4 % kPairUnroll == 0, "the slice padding must be a multiple of the unroll");
 // floats a staged s takes in shared memory in 3-D (3: packed, the default;
 // 4: one 16-byte load, measured slower for the wider bank-conflict pattern)
 #ifndef MPH_XS3
