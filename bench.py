@@ -657,6 +657,8 @@ def main():
                          "reads them as FP16 slot records (0)")
     ap.add_argument("--pair-pack", type=int, default=1, choices=[0, 1],
                     help="mixed form: 6-byte slot records of the pair-term operator (packed g + 2-byte index; 0: FP16, 8 bytes)")
+    ap.add_argument("--split-apply", type=int, default=0, choices=[0, 1],
+                    help="mixed form: the operator's transposed apply beside its viscous kernel (1) or before it (0)")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-fluid", type=int, default=100,
@@ -735,6 +737,7 @@ def run_single(args, dist, rank, world, local):
             c.set_option("pair_pack", args.pair_pack)
             c.set_option("mg_depth", args.mg_depth)
             c.set_option("mg_coarsest", args.mg_coarsest)
+            c.set_option("split_apply", args.split_apply)
         c.set_option("cell_sort", args.cell_sort)
         c.set_option("device_loop", args.device_loop)
         if prec_ == PRECISION_MIXED and getattr(args, "tuned_settings", None):
@@ -903,6 +906,7 @@ def run_single(args, dist, rank, world, local):
             c.set_option("pair_pack", args.pair_pack)
             c.set_option("mg_depth", args.mg_depth)
             c.set_option("mg_coarsest", args.mg_coarsest)
+            c.set_option("split_apply", args.split_apply)
             for k, v in (getattr(args, "tuned_settings", None) or {}).items():
                 c.set_option(k, v)
         errs = _vel_error_vs_fp64(engine, [(params, parts, dim)], PRECISION_MIXED, PRECISION_FP64, args.outer_tol,

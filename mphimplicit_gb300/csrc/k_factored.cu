@@ -477,6 +477,23 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
     t[k] = s;
 }
 
+// C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
+template <int D>
+__device__ __forceinline__ void p_part32(int i, int lane, const int* __restrict__ ncp, const long long* __restrict__ psptr,
+                                         const float4* __restrict__ psrec, const float* __restrict__ t, float* yv)
+{
+    const float4* rp = psrec + psptr[i >> 5] + lane;
+    const int np = ncp[i];
+#pragma unroll 4
+    for (int a = 0; a < np; ++a) {
+        const float4 r = __ldcs(rp + (long long)a * 32);
+        const float tk = t[__float_as_int(r.w)];
+        yv[0] += r.x * tk;
+        yv[1] += r.y * tk;
+        if (D == 3) yv[2] += r.z * tk;
+    }
+}
+
 // Slot records of the inner operator's viscous pairs, in the slot order of
 // the sliced layout.  FP16 form (8 bytes a slot): g = sqrt(f) e in FP16,
 // scaled per slice, in the first D halves and the neighbour's block-local
@@ -600,7 +617,10 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
     for (int d = 0; d < 3; ++d) yv[d] += ys[d] * s2;
 }
 
-template <int D, bool LOC, bool PACK>
+// PPART false: the viscous pairs and the diagonal only, y written without
+// the dot; k_ppart32 adds lambda C t and forms the dot (the split operator,
+// whose transposed apply runs beside this kernel)
+template <int D, bool LOC, bool PACK, bool PPART>
 __global__ void __launch_bounds__(MPH_PAIR_BLOCK, 2)   // two 512-row blocks an SM
 k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ grec, const unsigned* __restrict__ grec32, const unsigned short* __restrict__ lcol,
@@ -654,22 +674,39 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
         const float in32 = sdiag[(size_t)i * 8 + 6];
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
-        {   // C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
-            const float4* rp = psrec + psptr[i >> 5] + lane;
-            const int np = ncp[i];
-#pragma unroll 4
-            for (int a = 0; a < np; ++a) {
-                const float4 r = __ldcs(rp + (long long)a * 32);
-                const float tk = t[__float_as_int(r.w)];
-                yv[0] += r.x * tk;
-                yv[1] += r.y * tk;
-                if (D == 3) yv[2] += r.z * tk;
-            }
-        }
+        if (PPART) p_part32<D>(i, lane, ncp, psptr, psrec, t, yv);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
             acc += (double)xi[d] * (double)yv[d];
+        }
+    }
+    if (PPART) reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
+}
+
+// The second half of the split operator: y_i += sum_k lambda_k C_ik t_k, then
+// (s, y) into the iteration's rho slot (after the transposed apply and the
+// viscous kernel; the same arithmetic as the fused kernel's P-part)
+template <int D>
+__global__ void __launch_bounds__(256) k_ppart32(int Nf, const int* __restrict__ ncp, const long long* __restrict__ psptr,
+                                                 const float4* __restrict__ psrec, const float* __restrict__ t,
+                                                 const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
+                                                 const int* __restrict__ flags, double* __restrict__ partials,
+                                                 unsigned* __restrict__ counter)
+{
+    if (flags[kFlagDone]) return;
+    const int it = flags[kFlagIter];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    if (i < Nf) {
+        float yv[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) yv[d] = y[(size_t)i * D + d];
+        p_part32<D>(i, i & 31, ncp, psptr, psrec, t, yv);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            y[(size_t)i * D + d] = yv[d];
+            acc += (double)x[(size_t)i * D + d] * (double)yv[d];
         }
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
@@ -1015,73 +1052,85 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
     reduce_finalize(acc, partials, counter, out);
 }
 
-template <int D, bool PACK>
+template <int D, bool PACK, bool PPART>
 static void visc_pen_launch(mph_case* c, unsigned gv, const float* x, float* y, unsigned* counter)
 {
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
     if (c->loc_smem)
-        k_visc_pen32<D, true, PACK><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32, d.lcol16,
-            d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
-            d.ucount);
+        k_visc_pen32<D, true, PACK, PPART><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32,
+            d.lcol16, d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter,
+            d.uniq, d.ucount);
     else
-        k_visc_pen32<D, false, PACK><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32, d.lcol16,
-            d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
-            nullptr);
+        k_visc_pen32<D, false, PACK, PPART><<<gv, c->pair_block, 0, c->stream>>>(P.Nf, d.nfc, d.sptr, d.acol, d.grec16, d.grec32,
+            d.lcol16, d.pscale, d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter,
+            nullptr, nullptr);
+    MPH_COUNT_LAUNCH();
 }
 
-void launch_apply32(mph_case* c, const float* x, float* y, int cap)
+template <int D>
+static void ct_launch(mph_case* c, cudaStream_t st, const float* x, int cap)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    const unsigned gt = grid_for(P.N, c->ct_block);
+    if (c->loc_ct_smem)
+        k_ct_apply32<D, true><<<gt, c->ct_block, c->loc_ct_smem, st>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
+                                                                      d.scal, d.flags, cap, d.ctuniq, d.ctucount);
+    else
+        k_ct_apply32<D, false><<<gt, c->ct_block, 0, st>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
+                                                          d.flags, cap, nullptr, nullptr);
+    MPH_COUNT_LAUNCH();
+}
+
+// The inner operator y = A32 x (and (x, y) into the iteration's rho slot).
+// Split form (option split_apply, off by default; the packed and FP16
+// records): the transposed apply t = C^T x runs on a side stream beside the
+// viscous kernel, which does not read t; k_ppart32 then adds lambda C t.  In
+// a captured graph the fork and the join are graph edges.  Measured slower
+// on the config-1 workload (0.409 against 0.404 ms an application): the
+// viscous kernel keeps every SM busy, so the two do not overlap, and the
+// third kernel costs more than the fork saves.
+template <int D>
+static void apply32(mph_case* c, const float* x, float* y, int cap)
 {
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
     unsigned* counter = (unsigned*)(d.flags + kFlagCounter);
-    const unsigned gt = grid_for(P.N, c->ct_block);
     const unsigned gv = grid_for(P.Nf, c->pair_block);
-    if (c->dim == 2) {
-        if (c->loc_ct_smem)
-            k_ct_apply32<2, true><<<gt, c->ct_block, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
-                                                                                d.scal, d.flags, cap, d.ctuniq, d.ctucount);
-        else
-            k_ct_apply32<2, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
-                                                                     d.flags, cap, nullptr, nullptr);
-        MPH_COUNT_LAUNCH();
-        if (c->pair_recompute) {
-            if (c->loc_smem)
-                k_visc_rc32<2, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, d.lcol16,
-                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
-                    d.ucount, c->loc_cap, d.wrap32);
-            else
-                k_visc_rc32<2, false><<<gv, c->pair_block, 0, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, nullptr,
-                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
-                    nullptr, 0, d.wrap32);
-        } else if (c->pair_pack)
-            visc_pen_launch<2, true>(c, gv, x, y, counter);
-        else
-            visc_pen_launch<2, false>(c, gv, x, y, counter);
-        MPH_COUNT_LAUNCH();
-    } else {
-        if (c->loc_ct_smem)
-            k_ct_apply32<3, true><<<gt, c->ct_block, c->loc_ct_smem, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32,
-                                                                                d.scal, d.flags, cap, d.ctuniq, d.ctucount);
-        else
-            k_ct_apply32<3, false><<<gt, c->ct_block, 0, c->stream>>>(P.N, d.ctsptr, d.ct_cnt, (const float4*)d.ctsval, x, d.tct32, d.scal,
-                                                                     d.flags, cap, nullptr, nullptr);
-        MPH_COUNT_LAUNCH();
-        if (c->pair_recompute) {
-            if (c->loc_smem)
-                k_visc_rc32<3, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, d.lcol16,
-                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
-                    d.ucount, c->loc_cap, d.wrap32);
-            else
-                k_visc_rc32<3, false><<<gv, c->pair_block, 0, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, nullptr,
-                    d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
-                    nullptr, 0, d.wrap32);
-        } else if (c->pair_pack)
-            visc_pen_launch<3, true>(c, gv, x, y, counter);
-        else
-            visc_pen_launch<3, false>(c, gv, x, y, counter);
-        MPH_COUNT_LAUNCH();
+    if (c->split_apply && !c->pair_recompute && c->fork_stream) {
+        cudaEventRecord(c->ev_fork, c->stream);
+        cudaStreamWaitEvent(c->fork_stream, c->ev_fork, 0);
+        ct_launch<D>(c, c->fork_stream, x, cap);
+        cudaEventRecord(c->ev_join, c->fork_stream);
+        if (c->pair_pack) visc_pen_launch<D, true, false>(c, gv, x, y, counter);
+        else visc_pen_launch<D, false, false>(c, gv, x, y, counter);
+        cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+        { k_ppart32<D><<<grid_for(P.Nf, 256), 256, 0, c->stream>>>(P.Nf, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal,
+                                                                   d.flags, d.partials, counter); MPH_COUNT_LAUNCH(); }
+        return;
     }
+    ct_launch<D>(c, c->stream, x, cap);
+    if (c->pair_recompute) {
+        if (c->loc_smem)
+            k_visc_rc32<D, true><<<gv, c->pair_block, c->loc_smem, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, d.lcol16,
+                d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, d.uniq,
+                d.ucount, c->loc_cap, d.wrap32);
+        else
+            k_visc_rc32<D, false><<<gv, c->pair_block, 0, c->stream>>>(P, P.Nf, d.pt32, d.nfc, d.sptr, d.acol, nullptr,
+                d.sdiag32, d.ncp, d.psptr, (const float4*)d.psval, d.tct32, x, y, d.scal, d.flags, d.partials, counter, nullptr,
+                nullptr, 0, d.wrap32);
+        MPH_COUNT_LAUNCH();
+    } else if (c->pair_pack)
+        visc_pen_launch<D, true, true>(c, gv, x, y, counter);
+    else
+        visc_pen_launch<D, false, true>(c, gv, x, y, counter);
+}
+
+void launch_apply32(mph_case* c, const float* x, float* y, int cap)
+{
+    if (c->dim == 2) apply32<2>(c, x, y, cap);
+    else apply32<3>(c, x, y, cap);
 }
 
 // ---- level-0 multigrid stencils and D^-1 on the pair-term path --------------------
@@ -1718,13 +1767,17 @@ static int launch_local_cols(mph_case* c)
         c->loc_cols = 0;
     }
     if (D == 2) {
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<2, true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
         MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(2)));
         MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float)));
     } else {
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
-        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
+        MPH_CUDA(cudaFuncSetAttribute(k_visc_pen32<3, true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
         MPH_CUDA(cudaFuncSetAttribute(k_visc_rc32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rc_smem_max(3)));
         MPH_CUDA(cudaFuncSetAttribute(k_ct_apply32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float)));
     }

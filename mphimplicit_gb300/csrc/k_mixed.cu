@@ -341,6 +341,11 @@ static int grow_f(float** p, long long* cap, long long need)
 int mixed_prepare(mph_case* c)
 {
     DeviceState& d = c->d;
+    if (c->split_apply && !c->fork_stream) {   // the split operator's side stream (created outside any capture)
+        MPH_CUDA(cudaStreamCreateWithFlags(&c->fork_stream, cudaStreamNonBlocking));
+        MPH_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        MPH_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    }
     if (mixed_jacobi(c)) {   // point Jacobi: the FP32 D^-1 only
         const long long nv = (long long)c->dp.Nf * c->dim;
         if (!d.v32) MPH_CUDA(cudaMalloc((void**)&d.v32, (size_t)nv * 8 * sizeof(float)));

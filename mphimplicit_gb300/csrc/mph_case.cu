@@ -675,6 +675,9 @@ int case_destroy(mph_case* c)
     for (cudaEvent_t e : c->gev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    if (c->fork_stream) cudaStreamDestroy(c->fork_stream);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     for (void* p : c->allocations) cudaFree(p);
     DeviceState& d = c->d;
     for (void* p : {(void*)d.nind, (void*)d.nindP, (void*)d.acol, (void*)d.aval, (void*)d.aval32, (void*)d.cval,

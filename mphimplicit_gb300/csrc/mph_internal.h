@@ -252,6 +252,10 @@ struct mph_case {
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
     bool pair_recompute = false;        // pair-term operator: evaluate g from the FP32 positions per slot (else slot records)
     bool pair_pack = true;              // pair-term operator: 6-byte slot records (packed g, 2-byte index; else FP16, 8 bytes)
+    bool split_apply = false;           // pair-term operator: transposed apply beside the viscous kernel (fork / join;
+                                        // measured slower: the viscous kernel fills every SM)
+    cudaStream_t fork_stream = nullptr; // its side stream and events
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int pair_block = 512;               // threads a block of the pair-term operator (and its row blocks)
     int ct_block = 256;                 // threads a block of the transposed P-list apply (and its particle blocks)
     int chunk = 8;                      // mixed form: CR iterations per captured graph chunk
