@@ -131,14 +131,18 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
 // next iteration's stop test (the one the operator kernels apply when an
 // iteration begins) and sets the inner loop's condition; an iteration that
 // found the solve done at its start clears it.
-template <typename V>
+// COND (the device-driven solve only): the variant that sets the loop's
+// condition; the host-driven solve's variant holds no device graph call (a
+// kernel with one is not profiled by ncu).
+template <typename V, bool COND>
 __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
                         const V* __restrict__ p, const V* __restrict__ q, const V* __restrict__ u,
                         double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                         unsigned* __restrict__ counter, int cap = 0, int use_cond = 0, cudaGraphConditionalHandle cond = 0)
 {
     if (flags[kFlagDone]) {
-        if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+        if constexpr (COND)
+            if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
         return;
     }
     const int it = flags[kFlagIter];
@@ -152,16 +156,18 @@ __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restri
         acc += (double)rk * (double)rk;
     }
     const bool last = reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
-    if (use_cond && last) {
-        const int it1 = flags[kFlagIter];
-        const double rr = scal[kSIn], rr0 = scal[kSIn0];
-        const bool bad = !(rr == rr);
-        const bool stop = it1 >= cap || rr / rr0 < scal[kSTol2] || bad;
-        if (stop) {
-            flags[kFlagDone] = 1;
-            if (bad) flags[kFlagBad] = 1;
+    if constexpr (COND) {
+        if (use_cond && last) {
+            const int it1 = flags[kFlagIter];
+            const double rr = scal[kSIn], rr0 = scal[kSIn0];
+            const bool bad = !(rr == rr);
+            const bool stop = it1 >= cap || rr / rr0 < scal[kSTol2] || bad;
+            if (stop) {
+                flags[kFlagDone] = 1;
+                if (bad) flags[kFlagBad] = 1;
+            }
+            cudaGraphSetConditional(cond, stop ? 0u : 1u);
         }
-        cudaGraphSetConditional(cond, stop ? 0u : 1u);
     }
 }
 
@@ -541,7 +547,7 @@ static int device_solve(mph_case* c, double* hs, int* hflags)
                     MPH_COUNT_LAUNCH();
                 }
                 pq_precond(c, s3, n, rb, s32, y32, p32, q32, u32);
-                { k_xrs32<V><<<rb, kReduceThreads, 0, s3>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter, loop_cap,
+                { k_xrs32<V, true><<<rb, kReduceThreads, 0, s3>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter, loop_cap,
                                                              1, h_in); MPH_COUNT_LAUNCH(); }
                 l_iter = t_launch_count - li0;
                 cudaGraph_t gi = nullptr;
@@ -683,7 +689,7 @@ static int mixed_solve_t(mph_case* c)
             vcycle_mixed(c, q32, u32, scal + kSQU32);
             if (ev_v1) cudaEventRecordWithFlags(ev_v1, st, cudaEventRecordExternal);
         }
-        { k_xrs32<V><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
+        { k_xrs32<V, false><<<rb, kReduceThreads, 0, st>>>(n, z32, r32, s32, p32, q32, u32, scal, flags, part, counter); MPH_COUNT_LAUNCH(); }
     };
     const int chunk = c->chunk;
     const bool graphs = c->use_graphs;
