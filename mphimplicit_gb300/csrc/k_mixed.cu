@@ -112,7 +112,8 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const V beta = it == 0 ? (V)0 : (V)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
-    double acc = 0.0;
+    // a thread's few terms (q u = q^2 / d >= 0) in FP32, the threads in FP64
+    float acc = 0.f;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const V pk = it == 0 ? s[k] : beta * p[k] + s[k];
         const V qk = it == 0 ? y[k] : beta * q[k] + y[k];
@@ -120,9 +121,9 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
         q[k] = qk;
         const V uk = invD[k] * qk;
         u[k] = uk;
-        acc += (double)qk * (double)uk;
+        acc += qk * uk;
     }
-    reduce_finalize(acc, partials, counter, scal + kSQU32);
+    reduce_finalize((double)acc, partials, counter, scal + kSQU32);
 }
 
 // z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
@@ -147,15 +148,15 @@ __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restri
     }
     const int it = flags[kFlagIter];
     const V alpha = (V)(scal[rho32_slot(it)] / scal[kSQU32]);
-    double acc = 0.0;
+    float acc = 0.f;   // a thread's few squares in FP32, the threads in FP64
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         z[k] += alpha * p[k];
         const V rk = r[k] - alpha * q[k];
         r[k] = rk;
         s[k] -= alpha * u[k];
-        acc += (double)rk * (double)rk;
+        acc += rk * rk;
     }
-    const bool last = reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter);
+    const bool last = reduce_finalize_step((double)acc, partials, counter, scal + kSIn, flags + kFlagIter);
     if constexpr (COND) {
         if (use_cond && last) {
             const int it1 = flags[kFlagIter];
