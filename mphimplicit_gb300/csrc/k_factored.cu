@@ -298,8 +298,9 @@ __global__ void k_cval_f32(long long n, const double* __restrict__ a, float* __r
 
 // t_k = sum over the transposed P-list of k of C_jk . x_j (every particle k)
 template <int D>
-__global__ void k_ct_apply(int N, const long long* __restrict__ ctptr, const int* __restrict__ ct_j,
-                           const double* __restrict__ ct_v, const double* __restrict__ x, double* __restrict__ t)
+__global__ void k_ct_apply(int N, DevParams P, const int* __restrict__ type, const long long* __restrict__ ctptr,
+                           const int* __restrict__ ct_j, const double* __restrict__ ct_v, const double* __restrict__ x,
+                           double* __restrict__ t)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
@@ -310,7 +311,7 @@ __global__ void k_ct_apply(int N, const long long* __restrict__ ctptr, const int
 #pragma unroll
         for (int d = 0; d < D; ++d) s += ct_v[e * D + d] * x[(size_t)j * D + d];
     }
-    t[k] = s;
+    t[k] = P.lambda[type[k]] * s;   // lambda_k t_k, as the residuals use it
 }
 
 // r = b - A x in factored form, (r, r) -> *out (deterministic reduction):
@@ -355,7 +356,7 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
         const int np = ncp[i];
         for (int a = lane; a < np; a += 32) {
             const int k = nindP[pb + a];
-            const double lt = P.lambda[type[k]] * t[k];
+            const double lt = t[k];   // lambda_k t_k
 #pragma unroll
             for (int d = 0; d < D; ++d) y[d] += cval[(pb + a) * D + d] * lt;
         }
@@ -675,11 +676,13 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
         if (PPART) p_part32<D>(i, lane, ncp, psptr, psrec, t, yv);
+        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
-            acc += (double)xi[d] * (double)yv[d];
+            dot += xi[d] * yv[d];
         }
+        acc = (double)dot;
     }
     if (PPART) reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }
@@ -703,11 +706,13 @@ __global__ void __launch_bounds__(256) k_ppart32(int Nf, const int* __restrict__
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] = y[(size_t)i * D + d];
         p_part32<D>(i, i & 31, ncp, psptr, psrec, t, yv);
+        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
-            acc += (double)x[(size_t)i * D + d] * (double)yv[d];
+            dot += x[(size_t)i * D + d] * yv[d];
         }
+        acc = (double)dot;
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }
@@ -834,11 +839,13 @@ k_visc_rc32(DevParams P, int Nf, const float4* __restrict__ pt32, const int* __r
                 if (D == 3) yv[2] += r.z * tk;
             }
         }
+        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
-            acc += (double)xi[d] * (double)yv[d];
+            dot += xi[d] * yv[d];
         }
+        acc = (double)dot;
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }
@@ -1036,7 +1043,7 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
         const int np = ncp[i];
         for (int a = 0; a < np; ++a) {
             const int k = nindP[pb + a];
-            const double lt = P.lambda[type[k]] * t[k];
+            const double lt = t[k];   // lambda_k t_k
 #pragma unroll
             for (int d = 0; d < D; ++d) y[d] += cval[(pb + a) * D + d] * lt;
         }
@@ -1879,11 +1886,11 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
         { k_split_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32, d.x32 + nv); MPH_COUNT_LAUNCH(); }
         const unsigned gr = grid_for(P.Nf, c->pair_block);
         if (c->dim == 2) {
-            { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+            { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, P, d.type, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
             { k_resid_pairs<2><<<gr, c->pair_block, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         } else {
-            { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+            { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, P, d.type, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
             { k_resid_pairs<3><<<gr, c->pair_block, 0, c->stream>>>(P, P.Nf, d.type, d.nfc, d.sptr, d.acol, d.pes32, d.sdiag64, d.ncp, d.nptrP,
                                                           d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter, out); MPH_COUNT_LAUNCH(); }
         }
@@ -1891,12 +1898,12 @@ void launch_resid_factored(mph_case* c, const double* x, double* r, double* out)
     }
     { k_cval_f32<<<grid_for(nv, 256), 256, 0, c->stream>>>(nv, x, d.x32); MPH_COUNT_LAUNCH(); }
     if (c->dim == 2) {
-        { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply<2><<<gt, 256, 0, c->stream>>>(P.N, P, d.type, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
         { k_resid_factored<2><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
                                                                    d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter,
                                                                    out); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
+        { k_ct_apply<3><<<gt, 256, 0, c->stream>>>(P.N, P, d.type, d.ct_ptr, d.ct_j, d.ct_v, x, d.tct); MPH_COUNT_LAUNCH(); }
         { k_resid_factored<3><<<g, kPairWarps * 32, 0, c->stream>>>(P, d.type, d.nc, d.nfc, d.nptr, d.nind, d.pe32, d.ncp, d.nptrP,
                                                                    d.nindP, d.cval, d.tct, x, d.x32, d.bvec, r, d.partials, counter,
                                                                    out); MPH_COUNT_LAUNCH(); }
