@@ -273,7 +273,27 @@ int mph_case_set_option(mph_case* c, const char* name, double value);
  *   with mph_get_fields); the start value only changes the iteration count.
  *   "device_loop" 0 (default) / 1: mixed form with graphs.  1 runs the whole
  *   solve as one CUDA graph whose refinement and CR loops are device-side
- *   conditional while nodes (no host poll; same bits); not with profiling. */
+ *   conditional while nodes (no host poll; same bits); not with profiling.
+ *   "mg_depth" -1 (default) / 0 / 1 .. 24: mixed form only.  The inner CR's
+ *   preconditioner: -1 point Jacobi (D^-1 from the pair terms; no multigrid
+ *   levels are built, so their export fails with MPH_ERR_STATE), 0 the
+ *   reference's V-cycle over every level (preconditionWithMultiGrid,
+ *   main.cpp:4122), k the V-cycle cut after its first k levels.
+ *   "mg_coarsest" 1 .. 8 (default 4): mixed form only, sweeps of a coarsest
+ *   level run grid-wide (the reference's 4, main.cpp:4216).
+ *   "pair_pack" 1 (default) / 0: pair-term inner operator only.  Slot records
+ *   of 6 bytes (g as 11/11/10-bit fixed point of its slice's scale, and a
+ *   2-byte block-local index) or 8 bytes (g in FP16 and the index).
+ *   "pair_recompute" 0 (default) / 1: pair-term inner operator only; 1
+ *   evaluates g per slot from the staged FP32 positions (2 bytes a slot).
+ *   "pair_fuse" 0 (default) / 1: point-Jacobi mixed form on the pair path;
+ *   1 writes the sliced pair terms in one kernel without the per-slot
+ *   pair-term list (16 bytes a neighbour slot less device memory; slower).
+ *   "split_apply" 0 (default) / 1: pair-term inner operator only; 1 runs the
+ *   transposed apply on a side stream beside the viscous kernel and adds
+ *   lambda C t in a third kernel.  The forms of these three options reach
+ *   solutions within the refinement tolerance of each other (their inner
+ *   operators differ in rounding or summation order only). */
 
 int mph_case_count(mph_case* c, int* count, int* fluid_count);
 int mph_case_time(mph_case* c, double* time);

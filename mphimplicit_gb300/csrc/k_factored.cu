@@ -66,6 +66,7 @@ constexpr int kPtWarps = MPH_PT_WARPS;
 // bitmap of an index window of at most kWinWords * 32 particles (2^18: two
 // planes of neighbour cells of a 10^6-particle fluid body fit).
 constexpr int kUMax = 8192;
+constexpr int kLtsK = 32;   // slots of a row a slicing chunk takes
 constexpr int kWinWords = 1 << 13;
 constexpr int kPairUnroll = MPH_PAIR_UNROLL;
 // the fluid slices are padded to a multiple of 4 slots (k_slice_width), which
@@ -88,6 +89,51 @@ constexpr int kXs3 = MPH_XS3;
 // inertia term, so its FP32 rounding moves A x by ~1e-10 of |b| (the host
 // keeps the factored form off when that bound would reach 1e-2 of the outer
 // tolerance).  Inertia and C p stay FP64.
+// (e, f) of the pair (i, j) in FP32, as every pair-term kernel evaluates it
+// (one function, so that they agree bit for bit): x_j - x_i from the
+// two-float positions (the high parts of nearby positions subtract with one
+// FP32 rounding at most, so q is within about one FP32 ulp of the FP64
+// difference, with no FP64 arithmetic); the exact minimum image only when a
+// component is not well inside a quarter of the domain width (a periodic
+// image, which also sets *wrap).  e = q / |q|, f = visc mu_ij w'(|q|) / |q|
+// within RadiusV, else 0 (main.cpp:2261-2289).
+template <int D>
+__device__ __forceinline__ void pair_ef(const DevParams& P, int i, int j, int ti, const float* hi, const float* li,
+                                        const int* __restrict__ type, const double* __restrict__ pos,
+                                        const float* __restrict__ pos32, const float* __restrict__ poslo32,
+                                        int* __restrict__ wrap, float* e, float& f)
+{
+    if (j != i) {
+        float hj[3], lj[3];
+        load_f32<D>(pos32, j, hj);
+        load_f32<D>(poslo32, j, lj);
+        float q32[3] = {0.f, 0.f, 0.f};
+        bool inner = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            q32[d] = (hj[d] - hi[d]) + (lj[d] - li[d]);
+            inner = inner && fabsf(q32[d]) < 0.48f * P.hw32[d];
+        }
+        if (!inner) {
+            *wrap = 1;   // the recomputing inner operator then takes the minimum image
+            double xi[3], xj[3], q[3];
+            load_vec<D>(pos, i, xi);
+            load_vec<D>(pos, j, xj);
+            sep_vec<D>(P, xj, xi, q);
+#pragma unroll
+            for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
+        }
+        const float r2 = q32[0] * q32[0] + q32[1] * q32[1] + q32[2] * q32[2];
+        if (r2 != 0.f && P.rV2_32 - r2 > 0.f) {
+            const float inv = rsqrtf(r2);
+            const float wd = P.wdA32 * (1.f - (r2 * inv) * P.inv_rv32);
+            f = P.vm32[ti][type[j]] * wd * inv;
+#pragma unroll
+            for (int d = 0; d < D; ++d) e[d] = q32[d] * inv;
+        }
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(kPtWarps * 32)
 k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const float* __restrict__ pos32,
@@ -116,41 +162,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
             const int j = nind[nb + k];
             float e[3] = {0.f, 0.f, 0.f};
             float f = 0.f;
-            if (j != i) {
-                // x_j - x_i from the two-float positions: the high parts of
-                // nearby positions subtract with one FP32 rounding at most,
-                // so q is within about one FP32 ulp of the FP64 difference,
-                // with no FP64 arithmetic; the exact minimum image only when
-                // a component is not well inside a quarter of the domain
-                // width (a periodic image)
-                float hj[3], lj[3];
-                load_f32<D>(pos32, j, hj);
-                load_f32<D>(poslo32, j, lj);
-                float q32[3] = {0.f, 0.f, 0.f};
-                bool inner = true;
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    q32[d] = (hj[d] - hi[d]) + (lj[d] - li[d]);
-                    inner = inner && fabsf(q32[d]) < 0.48f * P.hw32[d];
-                }
-                if (!inner) {
-                    *wrap = 1;   // the recomputing inner operator then takes the minimum image
-                    double xi[3], xj[3], q[3];
-                    load_vec<D>(pos, i, xi);
-                    load_vec<D>(pos, j, xj);
-                    sep_vec<D>(P, xj, xi, q);
-#pragma unroll
-                    for (int d = 0; d < D; ++d) q32[d] = (float)q[d];
-                }
-                const float r2 = q32[0] * q32[0] + q32[1] * q32[1] + q32[2] * q32[2];
-                if (r2 != 0.f && P.rV2_32 - r2 > 0.f) {
-                    const float inv = rsqrtf(r2);
-                    const float wd = P.wdA32 * (1.f - (r2 * inv) * P.inv_rv32);
-                    f = P.vm32[ti][type[j]] * wd * inv;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) e[d] = q32[d] * inv;
-                }
-            }
+            pair_ef<D>(P, i, j, ti, hi, li, type, pos, pos32, poslo32, wrap, e, f);
             pe32[nb + k] = make_float4(e[0], e[1], e[2], f);
             if (dinv) {
 #pragma unroll
@@ -208,6 +220,162 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                     dinv[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
                 }
             }
+        }
+    }
+}
+
+// k_pair_terms and the slicing of its fluid pair terms in one pass, for the
+// point-Jacobi mixed form (which reads the pair terms only in the sliced
+// layouts): a block of 32 warps per slice of 32 fluid rows, warp w on row w.
+// Chunks of 32 fluid slots go through a shared-memory tile into the sliced
+// FP32 g (pes32) and columns; the slice's largest |g| component then sets
+// its scale and a second sweep over the slice (L2) writes the packed (or
+// FP16) slot records.  The wall slots add to the diagonal only; b, lambda C
+// and D^-1 as in k_pair_terms.  The same pair_ef and the same expressions as
+// k_pair_terms and k_list_to_slices, so the outputs are theirs bit for bit.
+template <int D, bool PACK>
+__global__ void __launch_bounds__(1024)
+k_pair_slices(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const float* __restrict__ pos32,
+              const float* __restrict__ poslo32, const double* __restrict__ vel,
+              const int* __restrict__ nc, const long long* __restrict__ nptr, const int* __restrict__ nind,
+              const int* __restrict__ nfc, const int* __restrict__ ncp, const long long* __restrict__ nptrP,
+              const int* __restrict__ nindP, const double* __restrict__ cval, const double* __restrict__ pvec,
+              const long long* __restrict__ sptr, int* __restrict__ scol, float* __restrict__ sval,
+              unsigned* __restrict__ sval32, unsigned short* __restrict__ sval16, float* __restrict__ sscale,
+              double* __restrict__ bvec, float* __restrict__ cvl32, int* __restrict__ wrap, double* __restrict__ dinv)
+{
+    constexpr int W = kLtsK * D + 1;   // odd row stride: no bank conflicts
+    __shared__ float tile[32 * W];
+    __shared__ int ctile[32 * (kLtsK + 1)];
+    __shared__ float smax[32];
+    const int sl = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = sl * 32 + w;
+    const bool row = i < P.Nf;
+    const long long sb = sptr[sl];
+    const int width = (int)((sptr[sl + 1] - sb) / 32);
+    int ti = 0, n = 0, nf = 0;
+    long long nb = 0;
+    float hi[3] = {0.f, 0.f, 0.f}, li[3] = {0.f, 0.f, 0.f};
+    if (row) {
+        ti = type[i];
+        nb = nptr[i];
+        n = nc[i];
+        nf = nfc[i];
+        load_f32<D>(pos32, i, hi);
+        load_f32<D>(poslo32, i, li);
+    }
+    float lm = 0.f;
+    float tvd[3] = {0.f, 0.f, 0.f}, dpd[3] = {0.f, 0.f, 0.f};
+    for (int k0 = 0; k0 < width; k0 += kLtsK) {   // fluid slots (the slice's width is theirs, padded)
+        const int k = k0 + lane;
+        float g[3] = {0.f, 0.f, 0.f};
+        int col = 0;
+        if (row && k < nf) {
+            const int j = nind[nb + k];
+            float e[3] = {0.f, 0.f, 0.f};
+            float f = 0.f;
+            pair_ef<D>(P, i, j, ti, hi, li, type, pos, pos32, poslo32, wrap, e, f);
+#pragma unroll
+            for (int d = 0; d < D; ++d) tvd[d] += f * e[d] * e[d];
+            const float sf = sqrtf(f);
+#pragma unroll
+            for (int d = 0; d < D; ++d) g[d] = sf * e[d];
+            lm = fmaxf(lm, sqrtf(f) * fmaxf(fabsf(e[0]), fmaxf(fabsf(e[1]), fabsf(e[2]))));
+            col = j;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) tile[w * W + lane * D + d] = g[d];
+        ctile[w * (kLtsK + 1) + lane] = col;
+        __syncthreads();
+        const int kc = min(kLtsK, width - k0);
+        for (int o = threadIdx.x; o < kc * D * 32; o += blockDim.x) {
+            const int ln = o & 31, ec = o >> 5;   // ec = k_local * D + component
+            sval[sb * D + (long long)k0 * D * 32 + o] = tile[ln * W + ec];
+        }
+        for (int o = threadIdx.x; o < kc * 32; o += blockDim.x) {
+            const int ln = o & 31, kl = o >> 5;
+            scol[sb + (long long)(k0 + kl) * 32 + ln] = ctile[ln * (kLtsK + 1) + kl];
+        }
+        __syncthreads();
+    }
+    if (row)   // the wall slots: the viscous diagonal only
+        for (int k = nf + lane; k < n; k += 32) {
+            float e[3] = {0.f, 0.f, 0.f};
+            float f = 0.f;
+            pair_ef<D>(P, i, nind[nb + k], ti, hi, li, type, pos, pos32, poslo32, wrap, e, f);
+#pragma unroll
+            for (int d = 0; d < D; ++d) tvd[d] += f * e[d] * e[d];
+        }
+    // the slice's scale: its largest |g| component maps to 1023 (packed) or 2^15 (FP16)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lm = fmaxf(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+    if (lane == 0) smax[w] = lm;
+    __syncthreads();
+    float m = 0.f;
+    for (int q = 0; q < 32; ++q) m = fmaxf(m, smax[q]);
+    const float sigma = m / (PACK ? 1023.f : 32768.f);
+    const float inv16 = m > 0.f ? 1.f / sigma : 0.f;
+    if (threadIdx.x == 0) sscale[sl] = sigma;
+    // the slot records from the sliced g just written (this block's, in L2)
+    for (int o = threadIdx.x; o < width * 32; o += blockDim.x) {
+        const int ln = o & 31, k = o >> 5;
+        float gd[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < D; ++d) gd[d] = sval[sb * D + ((long long)k * D + d) * 32 + ln];
+        if (PACK) {
+            int q[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const int lim = d == 2 ? 511 : 1023;
+                const float v = gd[d] * inv16 * (d == 2 ? 0.5f : 1.f);
+                q[d] = max(-lim, min(lim, __float2int_rn(v)));
+            }
+            sval32[sb + (long long)k * 32 + ln] =
+                ((unsigned)q[0] & 0x7ffu) | (((unsigned)q[1] & 0x7ffu) << 11) | (((unsigned)q[2] & 0x3ffu) << 22);
+        } else {
+            unsigned h[3] = {0u, 0u, 0u};
+#pragma unroll
+            for (int d = 0; d < D; ++d) h[d] = __half_as_ushort(__float2half_rn(gd[d] * inv16));
+            reinterpret_cast<uint2*>(sval16)[sb + (long long)k * 32 + ln] = make_uint2(h[0] | (h[1] << 16), h[2]);
+        }
+    }
+    if (!row) return;   // warp-uniform
+    // b = - C p + inertia v (FP64), lambda C for the inner operator, and the
+    // C Lambda C^T diagonal, as k_pair_terms
+    double vi[3];
+    load_vec<D>(vel, i, vi);
+    double sumv[3] = {0.0, 0.0, 0.0};
+    const long long pb = nptrP[i];
+    const int np = ncp[i];
+    for (int a = lane; a < np; a += 32) {
+        const int k = nindP[pb + a];
+        const double pk = pvec[k];
+#pragma unroll
+        for (int r = 0; r < D; ++r) sumv[r] -= cval[(pb + a) * D + r] * pk;
+        const double lam = P.lambda[type[k]];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            const float cl = (float)(cval[(pb + a) * D + r] * lam);
+            cvl32[(pb + a) * D + r] = cl;
+            dpd[r] += cl * (float)cval[(pb + a) * D + r];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
+            tvd[r] += __shfl_xor_sync(0xffffffffu, tvd[r], o);
+            dpd[r] += __shfl_xor_sync(0xffffffffu, dpd[r], o);
+        }
+    if (lane == 0) {
+        const double inert = P.density[ti] * P.vol / P.vol / P.dt;   // as the assembly
+        const float in32 = P.inert32[ti];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
+            const float dg = in32 + tvd[r] + dpd[r];
+            dinv[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
         }
     }
 }
@@ -858,7 +1026,6 @@ k_visc_rc32(DevParams P, int Nf, const float4* __restrict__ pt32, const int* __r
 // operator, in FP16 scaled per slice (g / sigma, sigma = the slice's largest
 // |g| component / 2^15: relative rounding 2^-11, no overflow) into the first
 // D halves of the slot records (4 halves a slot).
-constexpr int kLtsK = 32;
 
 template <int D, bool PAIRS>
 __global__ void __launch_bounds__(256) k_list_to_slices(int rows, const long long* __restrict__ sptr, const int* __restrict__ cnt,
@@ -1608,6 +1775,54 @@ static int grow_pairs(mph_case* c, long long slots)
     return MPH_OK;
 }
 
+// The sliced pair-term arrays of this step's form, allocated before the
+// kernels that write them: FP32 g, the packed records and the block-local
+// indices, or the FP16 records, and the slices' scales.
+static int ensure_pair_records(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const int D = c->dim;
+    MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
+    const bool lrec = c->pair_recompute || c->pair_pack;   // records without the index half
+    if (c->pair_pack && !c->pair_recompute && c->nslots > d.cap_grec32) {   // packed g, a word a slot
+        if (d.grec32) cudaFree(d.grec32);
+        d.grec32 = nullptr;
+        d.cap_grec32 = 0;
+        const long long n = c->nslots + c->nslots / 8 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.grec32, (size_t)n * sizeof(unsigned)));
+        d.cap_grec32 = n;
+    }
+    if (lrec) {   // block-local indices, a half a slot
+        if (c->nslots > d.cap_lcol16) {
+            if (d.lcol16) cudaFree(d.lcol16);
+            d.lcol16 = nullptr;
+            d.cap_lcol16 = 0;
+            const long long n = c->nslots + c->nslots / 8 + 1024;
+            MPH_CUDA(cudaMalloc((void**)&d.lcol16, (size_t)n * sizeof(unsigned short)));
+            d.cap_lcol16 = n;
+        }
+    } else if (c->nslots * 4 > d.cap_grec16) {   // slot records, 4 halves a slot
+        if (d.grec16) cudaFree(d.grec16);
+        d.grec16 = nullptr;
+        d.cap_grec16 = 0;
+        const long long n = c->nslots * 4 + c->nslots / 2 + 1024;
+        MPH_CUDA(cudaMalloc((void**)&d.grec16, (size_t)n * sizeof(unsigned short)));
+        d.cap_grec16 = n;
+    }
+    if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)(c->nslices + 1) * sizeof(float)));
+    return MPH_OK;
+}
+
+// Option pair_fuse: k_pair_slices writes the sliced pair terms itself (no
+// pair-term list in between: 16 bytes a neighbour slot less device memory,
+// 3.7 GB on the config-1 workload) where nothing else reads that list, the
+// point-Jacobi mixed form on the pair path with slot records.  Off by
+// default: measured slower (assembly 9.6 against 8.2 ms on the config-1
+// workload; a block of 32 warps per slice with a barrier per chunk hides
+// the neighbours' position gathers worse than k_pair_terms' grid-stride
+// warps).
+static bool pair_fused(const mph_case* c) { return c->pair_fuse && c->step_pairs && mixed_jacobi(c) && !c->pair_recompute; }
+
 // The factored operator equals the assembled one when 2 RadiusP < MaxRadius;
 // its FP32 viscous part is accurate enough while FP32 rounding of that part
 // (about 1e-7 of it, the part being visc_ratio of the inertia) stays below
@@ -1628,14 +1843,34 @@ bool factored_applies(const mph_case* c)
     return pair_path || pert < 1.0e-2 * c->tol_outer;
 }
 
+template <int D>
+static void pair_slices_launch(mph_case* c)
+{
+    DeviceState& d = c->d;
+    const DevParams& P = c->dp;
+    if (c->nslices == 0) return;
+    if (c->pair_pack)
+        k_pair_slices<D, true><<<c->nslices, 1024, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind,
+            d.nfc, d.ncp, d.nptrP, d.nindP, d.cval, d.pvec, d.sptr, d.acol, d.pes32, d.grec32, nullptr, d.pscale, d.bvec, d.cvl32,
+            d.wrap32, d.invDiag);
+    else
+        k_pair_slices<D, false><<<c->nslices, 1024, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind,
+            d.nfc, d.ncp, d.nptrP, d.nindP, d.cval, d.pvec, d.sptr, d.acol, d.pes32, nullptr, d.grec16, d.pscale, d.bvec, d.cvl32,
+            d.wrap32, d.invDiag);
+    MPH_COUNT_LAUNCH();
+}
+
 int launch_pair_terms(mph_case* c)
 {
     DeviceState& d = c->d;
     const DevParams& P = c->dp;
-    long long slots = 0;
-    MPH_CUDA(cudaMemcpyAsync(&slots, d.nptr + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    MPH_CUDA(cudaStreamSynchronize(c->stream));
-    MPH_TRY(grow_pairs(c, slots));
+    const bool fused = pair_fused(c);
+    if (!fused) {   // the pair-term list, a record per neighbour slot
+        long long slots = 0;
+        MPH_CUDA(cudaMemcpyAsync(&slots, d.nptr + P.Nf, sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+        MPH_CUDA(cudaStreamSynchronize(c->stream));
+        MPH_TRY(grow_pairs(c, slots));
+    }
     if (!d.tct) MPH_CUDA(cudaMalloc((void**)&d.tct, (size_t)(P.N + 1) * sizeof(double)));
     // FP32 copy of x and, after it, the FP32 remainders x - hi (two-float x
     // of the pair-path residual)
@@ -1665,22 +1900,27 @@ int launch_pair_terms(mph_case* c)
         sdiag = d.sdiag32;
         cvl = d.cvl32;
         if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float)));
-        MPH_CUDA(cudaMemsetAsync(d.pscale, 0, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float), c->stream));
-        if (!c->pair_recompute)
-            gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
+        if (!fused) {
+            MPH_CUDA(cudaMemsetAsync(d.pscale, 0, (size_t)((P.Nf + 31) / 32 + 1) * sizeof(float), c->stream));
+            if (!c->pair_recompute)
+                gmax = reinterpret_cast<unsigned*>(d.pscale);   // slice maxima, turned into scales by the slicing
+        }
     }
     MPH_CUDA(cudaMemsetAsync(d.wrap32, 0, sizeof(int), c->stream));
+    if (fused && c->nslices) MPH_TRY(ensure_pair_records(c));
     // the mixed form without grid levels takes D^-1 from here (no level-0 pass)
     double* dinv = c->step_pairs && mixed_jacobi(c) ? d.invDiag : nullptr;
     const unsigned g = std::min<long long>(((long long)P.Nf + kPtWarps - 1) / kPtWarps, 152LL * 128 / kPtWarps);
     const unsigned gw = grid_for((long long)P.Nf * 32, 256);
     if (c->dim == 2) {
-        { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
+        if (fused) pair_slices_launch<2>(c);
+        else { k_pair_terms<2><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+                                                                    d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<2><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
-                                                               d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
+        if (fused) pair_slices_launch<3>(c);
+        else { k_pair_terms<3><<<g, kPtWarps * 32, 0, c->stream>>>(P, d.type, d.pos, d.pos32, d.poslo32, d.vel, d.nc, d.nptr, d.nind, d.nfc, d.ncp, d.nptrP,
+                                                                    d.nindP, d.cval, d.pvec, d.pe32, d.bvec, cvl, gmax, d.wrap32, dinv); MPH_COUNT_LAUNCH(); }
         { k_wall_terms64<3><<<gw, 256, 0, c->stream>>>(P, d.type, d.pos, d.vel, d.nc, d.nfc, d.nptr, d.nind, d.bvec, sdiag, sdiag64); MPH_COUNT_LAUNCH(); }
     }
     return MPH_OK;
@@ -1797,34 +2037,8 @@ int launch_pairs_to_slices(mph_case* c)
     const DevParams& P = c->dp;
     const int D = c->dim;
     if (c->nslices == 0) return MPH_OK;
-    MPH_TRY(grow_f(&d.pes32, &d.cap_pes32, c->nslots * D));
+    MPH_TRY(ensure_pair_records(c));
     const bool lrec = c->pair_recompute || c->pair_pack;   // records without the index half
-    if (c->pair_pack && !c->pair_recompute && c->nslots > d.cap_grec32) {   // packed g, a word a slot
-        if (d.grec32) cudaFree(d.grec32);
-        d.grec32 = nullptr;
-        d.cap_grec32 = 0;
-        const long long n = c->nslots + c->nslots / 8 + 1024;
-        MPH_CUDA(cudaMalloc((void**)&d.grec32, (size_t)n * sizeof(unsigned)));
-        d.cap_grec32 = n;
-    }
-    if (lrec) {   // block-local indices, a half a slot
-        if (c->nslots > d.cap_lcol16) {
-            if (d.lcol16) cudaFree(d.lcol16);
-            d.lcol16 = nullptr;
-            d.cap_lcol16 = 0;
-            const long long n = c->nslots + c->nslots / 8 + 1024;
-            MPH_CUDA(cudaMalloc((void**)&d.lcol16, (size_t)n * sizeof(unsigned short)));
-            d.cap_lcol16 = n;
-        }
-    } else if (c->nslots * 4 > d.cap_grec16) {   // slot records, 4 halves a slot
-        if (d.grec16) cudaFree(d.grec16);
-        d.grec16 = nullptr;
-        d.cap_grec16 = 0;
-        const long long n = c->nslots * 4 + c->nslots / 2 + 1024;
-        MPH_CUDA(cudaMalloc((void**)&d.grec16, (size_t)n * sizeof(unsigned short)));
-        d.cap_grec16 = n;
-    }
-    if (!d.pscale) MPH_CUDA(cudaMalloc((void**)&d.pscale, (size_t)(c->nslices + 1) * sizeof(float)));
     if (!d.psptr) {
         MPH_CUDA(cudaMalloc((void**)&d.psptr, (size_t)(c->nslices + 1) * sizeof(long long)));
         MPH_CUDA(cudaMalloc((void**)&d.pswidth, (size_t)(c->nslices + 1) * sizeof(int)));
@@ -1835,13 +2049,15 @@ int launch_pairs_to_slices(mph_case* c)
     unsigned short* rec16 = lrec ? nullptr : d.grec16;
     unsigned* rec32 = c->pair_pack && !c->pair_recompute ? d.grec32 : nullptr;
     if (D == 2) {
-        { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
+        if (!pair_fused(c))
+            { k_list_to_slices<2, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
+                                                                          d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<2, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
                                                                        nullptr, d.psval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     } else {
-        { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
-                                                                      d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
+        if (!pair_fused(c))
+            { k_list_to_slices<3, true><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.sptr, d.nfc, d.nptr, d.nind, d.pe32, nullptr, d.acol,
+                                                                          d.pes32, rec16, d.pscale, rec32); MPH_COUNT_LAUNCH(); }
         { k_list_to_slices<3, false><<<c->nslices, 256, 0, c->stream>>>(P.Nf, d.psptr, d.ncp, d.nptrP, d.nindP, nullptr, d.cvl32,
                                                                        nullptr, d.psval, nullptr, nullptr, nullptr); MPH_COUNT_LAUNCH(); }
     }

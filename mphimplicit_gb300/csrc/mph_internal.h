@@ -252,6 +252,7 @@ struct mph_case {
     bool inner_local = true;            // pair-term operator: stage neighbours' s in shared memory where a block fits
     bool pair_recompute = false;        // pair-term operator: evaluate g from the FP32 positions per slot (else slot records)
     bool pair_pack = true;              // pair-term operator: 6-byte slot records (packed g, 2-byte index; else FP16, 8 bytes)
+    bool pair_fuse = false;             // point-Jacobi pair path: pair terms written sliced by one kernel (no pair-term list)
     bool split_apply = false;           // pair-term operator: transposed apply beside the viscous kernel (fork / join;
                                         // measured slower: the viscous kernel fills every SM)
     cudaStream_t fork_stream = nullptr; // its side stream and events

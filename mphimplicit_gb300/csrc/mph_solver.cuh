@@ -130,7 +130,7 @@ inline unsigned long long graph_signature(const mph_case* c, double tol, int cap
     h = fnv1a(h, &d, sizeof(d));
     h = fnv1a(h, &c->dp, sizeof(c->dp));
     if (!c->lv.empty()) h = fnv1a(h, c->lv.data(), c->lv.size() * sizeof(c->lv[0]));
-    const long long misc[] = {c->depth, c->nslices, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level, c->pair_block, c->ct_block, c->chunk, c->mg_pre, c->mg_post, c->mg_depth, c->mg_coarsest, c->pair_recompute, c->pair_pack, c->split_apply, c->fork_stream != nullptr, c->loc_cap,
+    const long long misc[] = {c->depth, c->nslices, c->precision, c->step_factored, c->step_pairs, c->loc_smem, c->loc_ct_smem, c->prof.on, c->mixed_extra_sweeps, c->dense_level, c->pair_block, c->ct_block, c->chunk, c->mg_pre, c->mg_post, c->mg_depth, c->mg_coarsest, c->pair_recompute, c->pair_pack, c->pair_fuse, c->split_apply, c->fork_stream != nullptr, c->loc_cap,
                               cap, c->mg_rows_total, c->mg_cof_total};
     h = fnv1a(h, misc, sizeof(misc));
     h = fnv1a(h, &tol, sizeof(tol));

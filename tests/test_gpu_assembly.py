@@ -277,3 +277,30 @@ def test_point_jacobi_diagonal_and_solution(engine_lib, case):
     (dj, vj), (dm, vm) = res[-1], res[0]
     assert rel(dj, dm) <= 1e-6
     assert np.linalg.norm(vj - vm) / np.linalg.norm(vm) <= 1e-8
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_fused_pair_slices_give_the_same_bits(engine_lib, case):
+    """Option pair_fuse writes the sliced pair terms, the slot records and
+    the slice scales in one kernel (no pair-term list) with the same pair
+    evaluation and expressions as the two-kernel path: whole point-Jacobi
+    mixed steps agree bit for bit except for D^-1, whose wall-slot terms it
+    sums in another order (so the steps are compared to the refinement's
+    tolerance, and b and the records bit for bit)."""
+    name, dim, params, parts = case
+    out = {}
+    for fuse in (0, 1):
+        g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+        g.set_solver(1e-10, 1e-3, 50)
+        g.set_option("pair_fuse", fuse)
+        for st in ("step_begin", "cellsort", "neighbors", "explicit", "assemble"):
+            g.stage(st)
+        b, dinv = g.export("VectorB"), g.export("InvDiagA")
+        g.stage("mg_build")
+        g.stage("solve")
+        assert g.solve_stats()["status"] == 0
+        out[fuse] = (b, dinv, vec_proj(g.export("Velocity"), dim)[:g.fluid_count])
+    (b0, d0, v0), (b1, d1, v1) = out[0], out[1]
+    assert np.array_equal(b0, b1)
+    assert rel(d1, d0) <= 1e-6
+    assert np.linalg.norm(v1 - v0) / np.linalg.norm(v0) <= 1e-8
