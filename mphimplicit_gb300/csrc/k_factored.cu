@@ -105,7 +105,15 @@ __device__ __forceinline__ void pair_ef(const DevParams& P, int i, int j, int ti
 {
     if (j != i) {
         float hj[3], lj[3];
-        load_f32<D>(pos32, j, hj);
+        int tj;
+        if (D == 3) {   // the high part's w holds the type bits (k_permute)
+            const float4 h4 = reinterpret_cast<const float4*>(pos32)[j];
+            hj[0] = h4.x; hj[1] = h4.y; hj[2] = h4.z;
+            tj = __float_as_int(h4.w);
+        } else {
+            load_f32<D>(pos32, j, hj);
+            tj = type[j];
+        }
         load_f32<D>(poslo32, j, lj);
         float q32[3] = {0.f, 0.f, 0.f};
         bool inner = true;
@@ -127,7 +135,7 @@ __device__ __forceinline__ void pair_ef(const DevParams& P, int i, int j, int ti
         if (r2 != 0.f && P.rV2_32 - r2 > 0.f) {
             const float inv = rsqrtf(r2);
             const float wd = P.wdA32 * (1.f - (r2 * inv) * P.inv_rv32);
-            f = P.vm32[ti][type[j]] * wd * inv;
+            f = P.vm32[ti][tj] * wd * inv;
 #pragma unroll
             for (int d = 0; d < D; ++d) e[d] = q32[d] * inv;
         }
