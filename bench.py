@@ -452,6 +452,7 @@ def run_ensemble(args, line_base):
         g.set_option("dense_coarse", args.dense_coarse)
         g.set_option("device_loop", args.device_loop)
         g.set_option("mg_depth", args.mg_depth)
+        g.set_option("batch_solve", args.batch_solve)
 
     table = None
     if prec == PRECISION_MIXED and args.autotune:
@@ -657,6 +658,8 @@ def main():
                          "reads them as FP16 slot records (0)")
     ap.add_argument("--pair-pack", type=int, default=1, choices=[0, 1],
                     help="mixed form: 6-byte slot records of the pair-term operator (packed g + 2-byte index; 0: FP16, 8 bytes)")
+    ap.add_argument("--batch-solve", type=int, default=0, choices=[0, 1],
+                    help="ensemble: the CR iterations of all cases in one launch per kernel (1) or each case's own (0)")
     ap.add_argument("--split-apply", type=int, default=0, choices=[0, 1],
                     help="mixed form: the operator's transposed apply beside its viscous kernel (1) or before it (0)")
     ap.add_argument("--no-fp64-leg", action="store_true", help="mixed form: skip the plain FP64 comparison run")

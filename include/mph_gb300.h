@@ -286,6 +286,12 @@ int mph_case_set_option(mph_case* c, const char* name, double value);
  *   2-byte block-local index) or 8 bytes (g in FP16 and the index).
  *   "pair_recompute" 0 (default) / 1: pair-term inner operator only; 1
  *   evaluates g per slot from the staged FP32 positions (2 bytes a slot).
+ *   "batch_solve" 0 (default) / 1: in mph_batch_step, the point-Jacobi
+ *   mixed cases on the pair path solve together: each refinement phase's CR
+ *   iterations are one launch per kernel over all of them (a block runs its
+ *   case's single-case kernel body with that case's block decomposition, so
+ *   every case keeps the bits of its own solve); the stages before the solve
+ *   then run for all cases before any solve starts.
  *   "pair_fuse" 0 (default) / 1: point-Jacobi mixed form on the pair path;
  *   1 writes the sliced pair terms in one kernel without the per-slot
  *   pair-term list (16 bytes a neighbour slot less device memory; slower).

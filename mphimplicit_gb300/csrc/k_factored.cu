@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <mutex>
 
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
@@ -580,7 +581,7 @@ __device__ __forceinline__ int rho32_slot_f(int it) { return 20 + (it & 1); }
 // hold ucount[b] >= 0 distinct fluid rows stages their s in shared memory;
 // its records carry each row's rank among them in place of the column.
 template <int D, bool LOC>
-__global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
+__device__ __forceinline__ void ct_apply32_body(int lb, int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
                                                     const float4* __restrict__ ctrec, const float* __restrict__ x, float* __restrict__ t,
                                                     const double* __restrict__ scal, int* __restrict__ flags, int cap,
                                                     const int* __restrict__ uniq, const int* __restrict__ ucount)
@@ -594,18 +595,18 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
     const double rr = it == 0 ? rr0 : scal[kSIn];
     const bool bad = !(rr == rr);
     if (it >= cap || rr / rr0 < tol2 || bad) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (lb == 0 && threadIdx.x == 0) {
             flags[kFlagDone] = 1;
             if (bad) flags[kFlagBad] = 1;
         }
         return;
     }
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = lb * blockDim.x + threadIdx.x;
     int U = -1;
     if (LOC) {   // block-uniform
-        U = ucount[blockIdx.x];
+        U = ucount[lb];
         if (U >= 0) {
-            const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+            const int* ul = uniq + (size_t)lb * kUMax;
 #pragma unroll 4
             for (int a = threadIdx.x; a < U; a += blockDim.x) {
                 const int j = ul[a];
@@ -652,6 +653,15 @@ __global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long l
         }
     }
     t[k] = s;
+}
+
+template <int D, bool LOC>
+__global__ void __launch_bounds__(MPH_CT_BLOCK) k_ct_apply32(int N, const long long* __restrict__ ctsptr, const int* __restrict__ ctcnt,
+                                                    const float4* __restrict__ ctrec, const float* __restrict__ x, float* __restrict__ t,
+                                                    const double* __restrict__ scal, int* __restrict__ flags, int cap,
+                                                    const int* __restrict__ uniq, const int* __restrict__ ucount)
+{
+    ct_apply32_body<D, LOC>((int)blockIdx.x, N, ctsptr, ctcnt, ctrec, x, t, scal, flags, cap, uniq, ucount);
 }
 
 // C Lambda t over the row's P-neighbours: 16-byte records (lambda C, column)
@@ -798,8 +808,7 @@ __device__ __forceinline__ void visc_row32(int i, int lane, const float* xi, con
 // the dot; k_ppart32 adds lambda C t and forms the dot (the split operator,
 // whose transposed apply runs beside this kernel)
 template <int D, bool LOC, bool PACK, bool PPART>
-__global__ void __launch_bounds__(MPH_PAIR_BLOCK, 2)   // two 512-row blocks an SM
-k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
+__device__ __forceinline__ void visc_pen32_body(int lb, int nb, int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
              const unsigned short* __restrict__ grec, const unsigned* __restrict__ grec32, const unsigned short* __restrict__ lcol,
              const float* __restrict__ pscale, const float* __restrict__ sdiag,
              const int* __restrict__ ncp, const long long* __restrict__ psptr, const float4* __restrict__ psrec,
@@ -813,7 +822,7 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
     constexpr int XS = D == 3 ? kXs3 : 2;
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = lb * blockDim.x + threadIdx.x;
     const uint2* r16 = reinterpret_cast<const uint2*>(grec);
     uint2 pre[kPairUnroll];   // the row's first slot records, in flight while s is staged
     {
@@ -825,9 +834,9 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
     }
     int U = -1;
     if (LOC) {   // stage s of the block's distinct neighbours once (block-uniform)
-        U = ucount[blockIdx.x];
+        U = ucount[lb];
         if (U >= 0) {
-            const int* ul = uniq + (size_t)blockIdx.x * kUMax;
+            const int* ul = uniq + (size_t)lb * kUMax;
 #pragma unroll 4
             for (int k = threadIdx.x; k < U; k += blockDim.x) {
                 const int j = ul[k];
@@ -860,7 +869,21 @@ k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ 
         }
         acc = (double)dot;
     }
-    if (PPART) reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
+    if (PPART) reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it), lb, nb);
+}
+
+template <int D, bool LOC, bool PACK, bool PPART>
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK, 2)   // two 512-row blocks an SM
+k_visc_pen32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr, const int* __restrict__ acol,
+             const unsigned short* __restrict__ grec, const unsigned* __restrict__ grec32, const unsigned short* __restrict__ lcol,
+             const float* __restrict__ pscale, const float* __restrict__ sdiag,
+             const int* __restrict__ ncp, const long long* __restrict__ psptr, const float4* __restrict__ psrec,
+             const float* __restrict__ t, const float* __restrict__ x, float* __restrict__ y, double* __restrict__ scal,
+             const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter,
+             const int* __restrict__ uniq, const int* __restrict__ ucount)
+{
+    visc_pen32_body<D, LOC, PACK, PPART>((int)blockIdx.x, (int)gridDim.x, Nf, nfc, sptr, acol, grec, grec32, lcol, pscale, sdiag, ncp,
+                                         psptr, psrec, t, x, y, scal, flags, partials, counter, uniq, ucount);
 }
 
 // The second half of the split operator: y_i += sum_k lambda_k C_ik t_k, then
@@ -1313,6 +1336,66 @@ void launch_apply32(mph_case* c, const float* x, float* y, int cap)
 {
     if (c->dim == 2) apply32<2>(c, x, y, cap);
     else apply32<3>(c, x, y, cap);
+}
+
+// ---- the operator over the cases of a batch ------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(MPH_CT_BLOCK) k_batch_ct32(const BatchCase* __restrict__ cs, const int* __restrict__ b0, int nc)
+{
+    const int c = batch_case_of(b0, nc, (int)blockIdx.x);
+    const BatchCase& B = cs[c];
+    const int lb = (int)blockIdx.x - b0[c];
+    if (B.ct_loc)
+        ct_apply32_body<D, true>(lb, B.N, B.ctsptr, B.ct_cnt, B.ctsval, B.s32, B.tct32, B.scal, B.flags, B.cap, B.ctuniq, B.ctucount);
+    else
+        ct_apply32_body<D, false>(lb, B.N, B.ctsptr, B.ct_cnt, B.ctsval, B.s32, B.tct32, B.scal, B.flags, B.cap, nullptr, nullptr);
+}
+
+template <int D, bool PACK>
+__global__ void __launch_bounds__(MPH_PAIR_BLOCK, 2) k_batch_visc32(const BatchCase* __restrict__ cs, const int* __restrict__ b0, int nc)
+{
+    const int c = batch_case_of(b0, nc, (int)blockIdx.x);
+    const BatchCase& B = cs[c];
+    const int lb = (int)blockIdx.x - b0[c];
+    if (B.vp_loc)
+        visc_pen32_body<D, true, PACK, true>(lb, B.vp_nb, B.Nf, B.nfc, B.sptr, B.acol, B.grec16, B.grec32, B.lcol16, B.pscale, B.sdiag32,
+                                             B.ncp, B.psptr, B.psval, B.tct32, B.s32, B.y32, B.scal, B.flags, B.partials, B.counter,
+                                             B.uniq, B.ucount);
+    else
+        visc_pen32_body<D, false, PACK, true>(lb, B.vp_nb, B.Nf, B.nfc, B.sptr, B.acol, B.grec16, B.grec32, B.lcol16, B.pscale,
+                                              B.sdiag32, B.ncp, B.psptr, B.psval, B.tct32, B.s32, B.y32, B.scal, B.flags, B.partials,
+                                              B.counter, nullptr, nullptr);
+}
+
+// the transposed apply and the viscous kernel of one batched CR iteration
+// (ct_b0 / vp_b0: their block starts; shared memory: the batch's largest)
+void launch_batch_operator(const BatchCase* cs, const int* ct_b0, const int* vp_b0, int nc, int dim, bool pack, int pair_block,
+                           int ct_block, int vp_smem, int ct_smem, int ct_blocks, int vp_blocks, cudaStream_t st)
+{
+    static std::once_flag once;
+    std::call_once(once, [] {   // fixed maxima (host threads of other batches would race on per-launch values)
+        cudaFuncSetAttribute(k_batch_ct32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float));
+        cudaFuncSetAttribute(k_batch_ct32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float));
+        cudaFuncSetAttribute(k_batch_visc32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float));
+        cudaFuncSetAttribute(k_batch_visc32<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 2 * (int)sizeof(float));
+        cudaFuncSetAttribute(k_batch_visc32<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float));
+        cudaFuncSetAttribute(k_batch_visc32<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUMax * 4 * (int)sizeof(float));
+    });
+    if (ct_blocks > 0) {
+        if (dim == 2) k_batch_ct32<2><<<ct_blocks, ct_block, ct_smem, st>>>(cs, ct_b0, nc);
+        else k_batch_ct32<3><<<ct_blocks, ct_block, ct_smem, st>>>(cs, ct_b0, nc);
+        MPH_COUNT_LAUNCH();
+    }
+    if (vp_blocks > 0) {
+        if (dim == 2) {
+            if (pack) k_batch_visc32<2, true><<<vp_blocks, pair_block, vp_smem, st>>>(cs, vp_b0, nc);
+            else k_batch_visc32<2, false><<<vp_blocks, pair_block, vp_smem, st>>>(cs, vp_b0, nc);
+        } else {
+            if (pack) k_batch_visc32<3, true><<<vp_blocks, pair_block, vp_smem, st>>>(cs, vp_b0, nc);
+            else k_batch_visc32<3, false><<<vp_blocks, pair_block, vp_smem, st>>>(cs, vp_b0, nc);
+        }
+        MPH_COUNT_LAUNCH();
+    }
 }
 
 // ---- level-0 multigrid stencils and D^-1 on the pair-term path --------------------

@@ -16,6 +16,8 @@
 // tests.  The CR recurrences are the reference's (main.cpp:4344-4377).  The
 // default outer tolerance is the reference's ||r||/||b|| < 1e-6;
 // mph_case_set_solver tightens it (e.g. 1e-10).
+#include <algorithm>
+
 #include "mph_device.cuh"
 #include "mph_solver.cuh"
 
@@ -105,7 +107,7 @@ __global__ void k_pq32(int n, const V* __restrict__ s, const V* __restrict__ y, 
 // The same update fused with the point-Jacobi preconditioner of the mixed
 // form: u = D^-1 q and (q, u) -> kSQU32 in the same pass.
 template <typename V>
-__global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restrict__ y, V* __restrict__ p, V* __restrict__ q,
+__device__ __forceinline__ void pq_jacobi32_body(int lb, int nb, int n, const V* __restrict__ s, const V* __restrict__ y, V* __restrict__ p, V* __restrict__ q,
                               const V* __restrict__ invD, V* __restrict__ u, double* __restrict__ scal,
                               const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
@@ -114,7 +116,7 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
     const V beta = it == 0 ? (V)0 : (V)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
     // a thread's few terms (q u = q^2 / d >= 0) in FP32, the threads in FP64
     float acc = 0.f;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
         const V pk = it == 0 ? s[k] : beta * p[k] + s[k];
         const V qk = it == 0 ? y[k] : beta * q[k] + y[k];
         p[k] = pk;
@@ -123,7 +125,15 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
         u[k] = uk;
         acc += qk * uk;
     }
-    reduce_finalize((double)acc, partials, counter, scal + kSQU32);
+    reduce_finalize((double)acc, partials, counter, scal + kSQU32, lb, nb);
+}
+
+template <typename V>
+__global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restrict__ y, V* __restrict__ p, V* __restrict__ q,
+                              const V* __restrict__ invD, V* __restrict__ u, double* __restrict__ scal,
+                              const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
+{
+    pq_jacobi32_body<V>((int)blockIdx.x, (int)gridDim.x, n, s, y, p, q, invD, u, scal, flags, partials, counter);
 }
 
 // z += alpha p, r -= alpha q, s -= alpha u, (r,r) -> kSIn; the last block
@@ -136,27 +146,27 @@ __global__ void k_pq_jacobi32(int n, const V* __restrict__ s, const V* __restric
 // condition; the host-driven solve's variant holds no device graph call (a
 // kernel with one is not profiled by ncu).
 template <typename V, bool COND>
-__global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
+__device__ __forceinline__ void xrs32_body(int lb, int nb, int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
                         const V* __restrict__ p, const V* __restrict__ q, const V* __restrict__ u,
                         double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                         unsigned* __restrict__ counter, int cap = 0, int use_cond = 0, cudaGraphConditionalHandle cond = 0)
 {
     if (flags[kFlagDone]) {
         if constexpr (COND)
-            if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+            if (use_cond && lb == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
         return;
     }
     const int it = flags[kFlagIter];
     const V alpha = (V)(scal[rho32_slot(it)] / scal[kSQU32]);
     float acc = 0.f;   // a thread's few squares in FP32, the threads in FP64
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
         z[k] += alpha * p[k];
         const V rk = r[k] - alpha * q[k];
         r[k] = rk;
         s[k] -= alpha * u[k];
         acc += rk * rk;
     }
-    const bool last = reduce_finalize_step((double)acc, partials, counter, scal + kSIn, flags + kFlagIter);
+    const bool last = reduce_finalize_step((double)acc, partials, counter, scal + kSIn, flags + kFlagIter, lb, nb);
     if constexpr (COND) {
         if (use_cond && last) {
             const int it1 = flags[kFlagIter];
@@ -170,6 +180,15 @@ __global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restri
             cudaGraphSetConditional(cond, stop ? 0u : 1u);
         }
     }
+}
+
+template <typename V, bool COND>
+__global__ void k_xrs32(int n, V* __restrict__ z, V* __restrict__ r, V* __restrict__ s,
+                        const V* __restrict__ p, const V* __restrict__ q, const V* __restrict__ u,
+                        double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
+                        unsigned* __restrict__ counter, int cap = 0, int use_cond = 0, cudaGraphConditionalHandle cond = 0)
+{
+    xrs32_body<V, COND>((int)blockIdx.x, (int)gridDim.x, n, z, r, s, p, q, u, scal, flags, partials, counter, cap, use_cond, cond);
 }
 
 // r32 = r * inv_scale, z = 0, and the inner reference norm (r32, r32) -> kSIn0
@@ -598,6 +617,142 @@ static int device_solve(mph_case* c, double* hs, int* hflags)
     return MPH_OK;
 }
 
+// The host side of one mixed solve in the parts the single-case solve and
+// the batched solve share: the start (start value, FP64 residual), the test
+// before each refinement phase and the phase's first kernels, the update and
+// FP64 residual after its CR iterations, and the end (velocity, statistics).
+// One FP32 CR run; at every refinement step the FP64 residual replaces the
+// recursive FP32 one (and s = M r is recomputed), while the search
+// directions p, q and the iteration count carry on, so the Krylov space is
+// not thrown away.  All FP32 vectors share one scale, fixed at the start.
+template <int D>
+struct MixedRun {
+    using V = float;
+    mph_case* c = nullptr;
+    int Nf = 0, n = 0, rb = 0, cap = 0;
+    unsigned gs = 0;
+    double* scal = nullptr;
+    double* part = nullptr;
+    int* flags = nullptr;
+    unsigned* counter = nullptr;
+    V *r32 = nullptr, *z32 = nullptr, *s32 = nullptr, *y32 = nullptr, *p32 = nullptr, *q32 = nullptr, *u32 = nullptr;
+    double tol_out2 = 0.0, tol_in2 = 0.0, scale = 1.0;
+    int outer = 0;
+    long long launched = 0;           // CR iterations launched (the runaway bound)
+    int host_flags[kFlagCount] = {};
+    double hs[32] = {};
+    bool bad = false;
+
+    void init(mph_case* c_)
+    {
+        c = c_;
+        DeviceState& d = c->d;
+        Nf = c->dp.Nf;
+        n = Nf * D;
+        scal = d.scal;
+        flags = d.flags;
+        counter = (unsigned*)(flags + kFlagCounter);
+        part = d.partials;
+        rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
+        gs = grid_for(Nf, 128);
+        V* vec = d.v32;
+        r32 = vec;
+        z32 = vec + (size_t)n;
+        s32 = vec + 2 * (size_t)n;
+        y32 = vec + 3 * (size_t)n;
+        p32 = vec + 4 * (size_t)n;
+        q32 = vec + 5 * (size_t)n;
+        u32 = vec + 6 * (size_t)n;
+        tol_out2 = c->tol_outer * c->tol_outer;
+        tol_in2 = c->tol_inner * c->tol_inner;
+        cap = n;
+    }
+
+    // FP64 residual: from the assembled FP64 blocks, or in factored form
+    void residual()
+    {
+        DeviceState& d = c->d;
+        if (c->step_factored) {
+            launch_resid_factored(c, d.x, d.r, scal + kSRR);
+        } else {
+            k_resid64<D><<<gs, 128, 0, c->stream>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR);
+            MPH_COUNT_LAUNCH();
+        }
+    }
+
+    int start()
+    {
+        DeviceState& d = c->d;
+        cudaStream_t st = c->stream;
+        MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
+        MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
+        const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
+        if (c->extrapolate && !d.vprev) {
+            MPH_CUDA(cudaMalloc((void**)&d.vprev, 2 * nvs * sizeof(double)));
+            MPH_CUDA(cudaMalloc((void**)&d.vprev_alt, 2 * nvs * sizeof(double)));
+            c->prev_valid = 0;
+        }
+        double* vprev = c->extrapolate ? d.vprev : nullptr;
+        const int have = std::min(c->prev_valid, c->extrapolate);
+        { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, nvs, have, c->extrapolate,
+                                                 part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
+        c->prev_valid = vprev ? std::min(c->prev_valid + 1, c->extrapolate) : 0;
+        residual();
+        return MPH_OK;
+    }
+
+    // The test before a refinement phase (reads the solve's state: syncs the
+    // case stream).  *go: a phase follows, its first kernels launched.
+    int phase(bool* go)
+    {
+        *go = false;
+        cudaStream_t st = c->stream;
+        MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
+        MPH_CUDA(cudaStreamSynchronize(st));
+        if (!(hs[kSRR] == hs[kSRR])) {
+            bad = true;
+            return MPH_OK;
+        }
+        if (hs[kSRR] / hs[kSRR0] < tol_out2 || outer >= c->max_outer || hs[kSRR] == 0.0) return MPH_OK;
+        if (outer > 0 && host_flags[kFlagIter] >= cap) return MPH_OK;
+        if (outer == 0) scale = std::sqrt(hs[kSRR]);
+        else MPH_CUDA(cudaMemsetAsync(flags + kFlagDone, 0, sizeof(int), st));
+        ++outer;
+        { k_to32<V><<<rb, kReduceThreads, 0, st>>>(n, c->d.r, r32, z32, 1.0 / scale, scal, part, counter); MPH_COUNT_LAUNCH(); }
+        { k_phase_tol<<<1, 32, 0, st>>>(scal, tol_in2, tol_out2); MPH_COUNT_LAUNCH(); }
+        vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
+        *go = true;
+        return MPH_OK;
+    }
+
+    // After a phase's CR iterations (host_flags read after them): a bad
+    // solve stops; else x += scale z and the FP64 residual.
+    int refine(bool* go)
+    {
+        *go = false;
+        if (host_flags[kFlagBad]) {
+            bad = true;
+            return MPH_OK;
+        }
+        { k_refine<V><<<rb, kReduceThreads, 0, c->stream>>>(n, c->d.x, z32, scale); MPH_COUNT_LAUNCH(); }
+        residual();
+        *go = true;
+        return MPH_OK;
+    }
+
+    int finish()
+    {
+        cudaStream_t st = c->stream;
+        const int total_inner = host_flags[kFlagIter];
+        { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, c->d.x, c->d.vel); MPH_COUNT_LAUNCH(); }
+        MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        MPH_CUDA(cudaStreamSynchronize(st));
+        fill_mixed_stats(c, total_inner, outer, hs, bad, tol_out2);
+        return MPH_OK;
+    }
+};
+
 template <int D>
 static int mixed_solve_t(mph_case* c)
 {
@@ -619,53 +774,18 @@ static int mixed_solve_t(mph_case* c)
         return MPH_OK;
     }
     DeviceState& d = c->d;
-    const int Nf = c->dp.Nf;
-    const int n = Nf * D;
-    cudaStream_t st = c->stream;
-    double* scal = d.scal;
-    int* flags = d.flags;
-    unsigned* counter = (unsigned*)(flags + kFlagCounter);
-    double* part = d.partials;
-    const int rb = std::min<int>(grid_for(n, kReduceThreads), kReduceBlocks);
-    const unsigned gs = grid_for(Nf, 128);
-    V* vec = d.v32;
-    V* r32 = vec;
-    V* z32 = vec + (size_t)n;
-    V* s32 = vec + 2 * (size_t)n;
-    V* y32 = vec + 3 * (size_t)n;
-    V* p32 = vec + 4 * (size_t)n;
-    V* q32 = vec + 5 * (size_t)n;
-    V* u32 = vec + 6 * (size_t)n;
-    MPH_CUDA(cudaMemsetAsync(scal, 0, 32 * sizeof(double), st));
-    MPH_CUDA(cudaMemsetAsync(flags, 0, kFlagCount * sizeof(int), st));
-    const size_t nvs = (size_t)c->dp.N * (D == 2 ? 2 : 4);
-    if (c->extrapolate && !d.vprev) {
-        MPH_CUDA(cudaMalloc((void**)&d.vprev, 2 * nvs * sizeof(double)));
-        MPH_CUDA(cudaMalloc((void**)&d.vprev_alt, 2 * nvs * sizeof(double)));
-        c->prev_valid = 0;
-    }
-    double* vprev = c->extrapolate ? d.vprev : nullptr;
-    const int have = std::min(c->prev_valid, c->extrapolate);
-    { k_x0<D><<<rb, kReduceThreads, 0, st>>>(Nf, d.type, d.vel, d.force, d.bvec, d.x, c->dp, vprev, nvs, have, c->extrapolate,
-                                             part, counter, scal + kSRR0); MPH_COUNT_LAUNCH(); }
-    c->prev_valid = vprev ? std::min(c->prev_valid + 1, c->extrapolate) : 0;
-    // FP64 residual: from the assembled FP64 blocks, or in factored form
-    auto residual = [&]() {
-        if (c->step_factored) {
-            launch_resid_factored(c, d.x, d.r, scal + kSRR);
-        } else {
-            k_resid64<D><<<gs, 128, 0, st>>>(Nf, d.nfc, d.sptr, d.acol, d.aval, d.x, d.bvec, d.r, part, counter, scal + kSRR);
-            MPH_COUNT_LAUNCH();
-        }
-    };
-    residual();
-    const double tol_out2 = c->tol_outer * c->tol_outer;
-    const double tol_in2 = c->tol_inner * c->tol_inner;
-    const int cap = n;
-    int total_inner = 0, outer = 0;
-    int host_flags[kFlagCount];
-    double hs[32];
-    bool bad = false;
+    MixedRun<D> run;
+    run.init(c);
+    MPH_TRY(run.start());
+    const int Nf = run.Nf, n = run.n, rb = run.rb, cap = run.cap;
+    const unsigned gs = run.gs;
+    double* scal = run.scal;
+    int* flags = run.flags;
+    unsigned* counter = run.counter;
+    double* part = run.part;
+    V *r32 = run.r32, *z32 = run.z32, *s32 = run.s32, *y32 = run.y32, *p32 = run.p32, *q32 = run.q32, *u32 = run.u32;
+    (void)r32;
+    int* host_flags = run.host_flags;
     // One FP32 CR iteration; its index lives in flags[kFlagIter] (it runs on
     // across refinement steps), so one launch sequence serves every iteration
     // and replays as a graph.  Iterations after a stop return at once.
@@ -701,7 +821,7 @@ static int mixed_solve_t(mph_case* c)
     if (gprof && !c->gev[0])
         for (int k = 0; k < 4 * kMaxGraphChunk; ++k) MPH_CUDA(cudaEventCreate(&c->gev[k]));
     if (graphs) {
-        MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, tol_in2, cap), [&] {
+        MPH_TRY(capture_graph(c, &c->mx_exec, &c->mx_sig, graph_signature(c, run.tol_in2, cap), [&] {
             for (int k = 0; k < chunk; ++k) {
                 if (gprof) cudaEventRecordWithFlags(c->gev[2 * k], c->stream, cudaEventRecordExternal);   // a record node
                 iteration(nullptr, gprof ? c->gev[2 * k + 1] : nullptr, gprof ? c->gev[kVcycleEvents + 2 * k] : nullptr,
@@ -710,42 +830,28 @@ static int mixed_solve_t(mph_case* c)
         }, &c->mx_launches));
     }
     const long long chunk_launches = c->mx_launches;
-    // One FP32 CR run; at every refinement step the FP64 residual replaces the
-    // recursive FP32 one (and s = M r is recomputed), while the search
-    // directions p, q and the iteration count carry on, so the Krylov space is
-    // not thrown away.  All FP32 vectors share one scale, fixed at the start.
-    double scale = 1.0;
-    int launched = 0;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
     for (;;) {
-        MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
-        MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
-        MPH_CUDA(cudaStreamSynchronize(st));
-        if (!(hs[kSRR] == hs[kSRR])) { bad = true; break; }
-        if (hs[kSRR] / hs[kSRR0] < tol_out2 || outer >= c->max_outer || hs[kSRR] == 0.0) break;
-        if (outer > 0 && host_flags[kFlagIter] >= cap) break;
-        if (outer == 0) scale = std::sqrt(hs[kSRR]);
-        else MPH_CUDA(cudaMemsetAsync(flags + kFlagDone, 0, sizeof(int), st));
-        ++outer;
-        { k_to32<V><<<rb, kReduceThreads, 0, st>>>(n, d.r, r32, z32, 1.0 / scale, scal, part, counter); MPH_COUNT_LAUNCH(); }
-        { k_phase_tol<<<1, 32, 0, st>>>(scal, tol_in2, tol_out2); MPH_COUNT_LAUNCH(); }
-        vcycle_mixed(c, r32, s32, scal + kSQU32);   // s = M r
+        bool go = false;
+        MPH_TRY(run.phase(&go));
+        if (!go) break;
+        cudaStream_t st = c->stream;
         bool done = false;
         while (!done) {
             const int it_before = host_flags[kFlagIter];
             if (graphs) {
                 MPH_CUDA(cudaGraphLaunch(c->mx_exec, st));
                 g_launch_count += chunk_launches;
-                launched += chunk;
+                run.launched += chunk;
             } else {
-                for (int k = 0; k < chunk; ++k, ++launched) {
+                for (int k = 0; k < chunk; ++k, ++run.launched) {
                     cudaEvent_t e[2] = {nullptr, nullptr};
                     const bool pon = prof_begin(c, 0, &e[0]) != 0;
                     iteration(pon ? e : nullptr, nullptr);
-                    if (pon) timed.push_back({launched, {e[0], e[1]}});
+                    if (pon) timed.push_back({(int)run.launched, {e[0], e[1]}});
                 }
             }
-            MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(host_flags), cudaMemcpyDeviceToHost, st));
+            MPH_CUDA(cudaMemcpyAsync(host_flags, flags, sizeof(run.host_flags), cudaMemcpyDeviceToHost, st));
             MPH_CUDA(cudaStreamSynchronize(st));
             if (gprof) {   // the operators of the iterations this chunk ran
                 const int ran = std::min(chunk, std::max(0, host_flags[kFlagIter] - it_before));
@@ -759,13 +865,12 @@ static int mixed_solve_t(mph_case* c)
                     c->prof.kern_n[1] += 1;
                 }
             }
-            done = host_flags[kFlagDone] != 0 || launched > cap + chunk;
+            done = host_flags[kFlagDone] != 0 || run.launched > cap + chunk;
         }
-        if (host_flags[kFlagBad]) { bad = true; break; }
-        { k_refine<V><<<rb, kReduceThreads, 0, st>>>(n, d.x, z32, scale); MPH_COUNT_LAUNCH(); }
-        residual();
+        MPH_TRY(run.refine(&go));
+        if (!go) break;
     }
-    total_inner = host_flags[kFlagIter];
+    const int total_inner = host_flags[kFlagIter];
     for (auto& t : timed) {   // keep the SpMV launches of iterations that ran
         if (t.first < total_inner) {
             c->prof.pending.push_back({0, t.second});
@@ -774,10 +879,258 @@ static int mixed_solve_t(mph_case* c)
             c->prof.pool.push_back(t.second.second);
         }
     }
-    { k_store_velocity_m<D><<<grid_for(n, 256), 256, 0, st>>>(Nf, d.x, d.vel); MPH_COUNT_LAUNCH(); }
-    MPH_CUDA(cudaMemcpyAsync(hs, scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
-    MPH_CUDA(cudaStreamSynchronize(st));
-    fill_mixed_stats(c, total_inner, outer, hs, bad, tol_out2);
+    return run.finish();
+}
+
+// ---- the batched solve ---------------------------------------------------------------
+// The cases of mph_batch_step that run the point-Jacobi mixed form on the pair
+// path solve together: each case's start, phase tests, updates and FP64
+// residuals are its own (MixedRun, on its stream), while the CR iterations of
+// a refinement phase are four launches over all the cases still iterating
+// (each block runs the single-case kernel body on its case, with the
+// single-case block decomposition), so a case's bits are those it gets alone.
+__global__ void k_batch_pq32(const BatchCase* __restrict__ cs, const int* __restrict__ b0, int nc)
+{
+    const int c = batch_case_of(b0, nc, (int)blockIdx.x);
+    const BatchCase& B = cs[c];
+    pq_jacobi32_body<float>((int)blockIdx.x - b0[c], B.el_nb, B.n, B.s32, B.y32, B.p32, B.q32, B.invD, B.u32, B.scal, B.flags,
+                            B.partials, B.counter);
+}
+
+__global__ void k_batch_xrs32(const BatchCase* __restrict__ cs, const int* __restrict__ b0, int nc)
+{
+    const int c = batch_case_of(b0, nc, (int)blockIdx.x);
+    const BatchCase& B = cs[c];
+    xrs32_body<float, false>((int)blockIdx.x - b0[c], B.el_nb, B.n, B.z32, B.r32, B.s32, B.p32, B.q32, B.u32, B.scal, B.flags,
+                             B.partials, B.counter);
+}
+
+// the cases' solver flags, gathered for one read
+__global__ void k_batch_flags(const BatchCase* __restrict__ cs, int nc, int* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nc * kFlagCount) out[t] = cs[t / kFlagCount].flags[t % kFlagCount];
+}
+
+void launch_batch_iteration(const BatchCase* cs, const int* b0, int nc, int dim, bool pack, int pair_block, int ct_block,
+                            int vp_smem, int ct_smem, const int* nblocks, cudaStream_t st)
+{
+    launch_batch_operator(cs, b0, b0 + (nc + 1), nc, dim, pack, pair_block, ct_block, vp_smem, ct_smem, nblocks[0], nblocks[1], st);
+    if (nblocks[2] > 0) {
+        { k_batch_pq32<<<nblocks[2], kReduceThreads, 0, st>>>(cs, b0 + 2 * (nc + 1), nc); MPH_COUNT_LAUNCH(); }
+        { k_batch_xrs32<<<nblocks[2], kReduceThreads, 0, st>>>(cs, b0 + 2 * (nc + 1), nc); MPH_COUNT_LAUNCH(); }
+    }
+}
+
+bool batch_solve_eligible(const mph_case* c)
+{
+    return c->batch_solve && c->precision == MPH_PRECISION_MIXED && c->stage == 6 && c->step_pairs && mixed_jacobi(c) &&
+           !c->pair_recompute && !c->split_apply && !c->device_loop && !c->prof.on && c->dp.Nf > 0 && c->nslices > 0;
+}
+
+// The batched solve's device table, flag buffers, stream and events, per
+// host thread (one batch at a time per thread).
+struct BatchBuffers {
+    BatchCase* tab = nullptr;
+    int* b0 = nullptr;
+    int* flags = nullptr;
+    int* hflags = nullptr;
+    int cap = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::vector<cudaEvent_t> evs;
+    int ensure(int nc)
+    {
+        if (!st) {
+            MPH_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            MPH_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        }
+        while ((int)evs.size() < nc) {
+            cudaEvent_t e = nullptr;
+            MPH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            evs.push_back(e);
+        }
+        if (nc <= cap) return MPH_OK;
+        if (tab) cudaFree(tab);
+        if (b0) cudaFree(b0);
+        if (flags) cudaFree(flags);
+        if (hflags) cudaFreeHost(hflags);
+        tab = nullptr;
+        b0 = flags = hflags = nullptr;
+        cap = 0;
+        MPH_CUDA(cudaMalloc((void**)&tab, (size_t)nc * sizeof(BatchCase)));
+        MPH_CUDA(cudaMalloc((void**)&b0, (size_t)3 * (nc + 1) * sizeof(int)));
+        MPH_CUDA(cudaMalloc((void**)&flags, (size_t)nc * kFlagCount * sizeof(int)));
+        MPH_CUDA(cudaMallocHost((void**)&hflags, (size_t)nc * kFlagCount * sizeof(int)));
+        cap = nc;
+        return MPH_OK;
+    }
+};
+static thread_local BatchBuffers t_batch;
+
+using ParFor = std::function<void(int, const std::function<int(int)>&)>;
+
+template <int D>
+static int batched_solve_t(std::vector<mph_case*>& cs, bool pack, int pair_block, int ct_block, const ParFor& par)
+{
+    const int nc = (int)cs.size();
+    BatchBuffers& tb = t_batch;
+    MPH_TRY(tb.ensure(nc));
+    std::vector<MixedRun<D>> runs(nc);
+    std::vector<int> st(nc, MPH_OK);
+    auto each = [&](const std::function<int(int)>& f) {   // f on every case, in parallel; the first failure
+        par(nc, [&](int k) { return st[k] = f(k); });
+        for (int k = 0; k < nc; ++k)
+            if (st[k] != MPH_OK) return st[k];
+        return (int)MPH_OK;
+    };
+    int chunk = 1;
+    MPH_TRY(each([&](int k) {
+        MPH_TRY(mixed_prepare(cs[k]));
+        runs[k].init(cs[k]);
+        return runs[k].start();
+    }));
+    for (int k = 0; k < nc; ++k) chunk = std::max(chunk, cs[k]->chunk);
+    std::vector<BatchCase> tab(nc);
+    int vp_smem = 0, ct_smem = 0;
+    for (int k = 0; k < nc; ++k) {
+        mph_case* c = cs[k];
+        DeviceState& d = c->d;
+        MixedRun<D>& R = runs[k];
+        BatchCase& B = tab[k];
+        B.N = c->dp.N;
+        B.Nf = c->dp.Nf;
+        B.n = R.n;
+        B.cap = R.cap;
+        B.ct_loc = c->loc_ct_smem != 0;
+        B.vp_loc = c->loc_smem != 0;
+        B.ct_nb = (int)grid_for(c->dp.N, ct_block);
+        B.vp_nb = (int)grid_for(c->dp.Nf, pair_block);
+        B.el_nb = R.rb;
+        B.ctsptr = d.ctsptr;
+        B.ct_cnt = d.ct_cnt;
+        B.ctsval = (const float4*)d.ctsval;
+        B.tct32 = d.tct32;
+        B.ctuniq = d.ctuniq;
+        B.ctucount = d.ctucount;
+        B.nfc = d.nfc;
+        B.sptr = d.sptr;
+        B.acol = d.acol;
+        B.grec16 = d.grec16;
+        B.grec32 = d.grec32;
+        B.lcol16 = d.lcol16;
+        B.pscale = d.pscale;
+        B.sdiag32 = d.sdiag32;
+        B.ncp = d.ncp;
+        B.psptr = d.psptr;
+        B.psval = (const float4*)d.psval;
+        B.uniq = d.uniq;
+        B.ucount = d.ucount;
+        B.s32 = R.s32;
+        B.y32 = R.y32;
+        B.p32 = R.p32;
+        B.q32 = R.q32;
+        B.u32 = R.u32;
+        B.z32 = R.z32;
+        B.r32 = R.r32;
+        B.invD = d.v32 + 7 * (size_t)R.n;
+        B.scal = R.scal;
+        B.flags = R.flags;
+        B.partials = R.part;
+        B.counter = R.counter;
+        vp_smem = std::max(vp_smem, c->loc_smem);
+        ct_smem = std::max(ct_smem, c->loc_ct_smem);
+    }
+    MPH_CUDA(cudaMemcpyAsync(tb.tab, tab.data(), (size_t)nc * sizeof(BatchCase), cudaMemcpyHostToDevice, tb.st));
+    std::vector<char> active(nc, 1);
+    std::vector<int> b0(3 * (nc + 1));
+    for (;;) {
+        MPH_TRY(each([&](int k) {
+            if (!active[k]) return (int)MPH_OK;
+            bool go = false;
+            MPH_TRY(runs[k].phase(&go));
+            if (!go) active[k] = 0;
+            return (int)MPH_OK;
+        }));
+        int nact = 0;
+        for (int k = 0; k < nc; ++k) nact += active[k] ? 1 : 0;
+        if (nact == 0) break;
+        // this phase's block starts: the cases still iterating, the others none
+        int nb[3] = {0, 0, 0};
+        for (int k = 0; k < nc; ++k) {
+            b0[k] = nb[0];
+            b0[(nc + 1) + k] = nb[1];
+            b0[2 * (nc + 1) + k] = nb[2];
+            if (active[k]) {
+                nb[0] += tab[k].ct_nb;
+                nb[1] += tab[k].vp_nb;
+                nb[2] += tab[k].el_nb;
+            }
+        }
+        b0[nc] = nb[0];
+        b0[2 * nc + 1] = nb[1];
+        b0[3 * nc + 2] = nb[2];
+        // the batch stream after the active cases' phase kernels
+        for (int k = 0; k < nc; ++k) {
+            if (!active[k]) continue;
+            MPH_CUDA(cudaEventRecord(tb.evs[k], cs[k]->stream));
+            MPH_CUDA(cudaStreamWaitEvent(tb.st, tb.evs[k], 0));
+        }
+        MPH_CUDA(cudaMemcpyAsync(tb.b0, b0.data(), b0.size() * sizeof(int), cudaMemcpyHostToDevice, tb.st));
+        bool all = false;
+        while (!all) {
+            for (int it = 0; it < chunk; ++it)
+                launch_batch_iteration(tb.tab, tb.b0, nc, D, pack, pair_block, ct_block, vp_smem, ct_smem, nb, tb.st);
+            { k_batch_flags<<<grid_for((long long)nc * kFlagCount, 256), 256, 0, tb.st>>>(tb.tab, nc, tb.flags); MPH_COUNT_LAUNCH(); }
+            MPH_CUDA(cudaMemcpyAsync(tb.hflags, tb.flags, (size_t)nc * kFlagCount * sizeof(int), cudaMemcpyDeviceToHost, tb.st));
+            MPH_CUDA(cudaStreamSynchronize(tb.st));
+            all = true;
+            for (int k = 0; k < nc; ++k) {
+                if (!active[k]) continue;
+                std::copy(tb.hflags + (size_t)k * kFlagCount, tb.hflags + (size_t)(k + 1) * kFlagCount, runs[k].host_flags);
+                runs[k].launched += chunk;
+                if (!(runs[k].host_flags[kFlagDone] != 0 || runs[k].launched > runs[k].cap + chunk)) all = false;
+            }
+        }
+        // the cases' streams after the batch's iterations: updates and FP64 residuals
+        MPH_CUDA(cudaEventRecord(tb.ev, tb.st));
+        MPH_TRY(each([&](int k) {
+            if (!active[k]) return (int)MPH_OK;
+            MPH_CUDA(cudaStreamWaitEvent(cs[k]->stream, tb.ev, 0));
+            bool go = false;
+            MPH_TRY(runs[k].refine(&go));
+            if (!go) active[k] = 0;
+            return (int)MPH_OK;
+        }));
+    }
+    return each([&](int k) {
+        MPH_TRY(runs[k].finish());
+        MPH_CUDA(cudaGetLastError());
+        cs[k]->stage = 7;
+        return (int)MPH_OK;
+    });
+}
+
+// Solve the eligible cases of a batch together, in groups of one dimension,
+// record format and block widths (the cases' stage must be 6).
+int batched_mixed_solve(std::vector<mph_case*>& cases, const ParFor& par)
+{
+    std::vector<char> taken(cases.size(), 0);
+    for (size_t a = 0; a < cases.size(); ++a) {
+        if (taken[a]) continue;
+        mph_case* c0 = cases[a];
+        std::vector<mph_case*> g;
+        for (size_t b = a; b < cases.size(); ++b) {
+            mph_case* c = cases[b];
+            if (taken[b] || c->dim != c0->dim || c->pair_pack != c0->pair_pack || c->pair_block != c0->pair_block ||
+                c->ct_block != c0->ct_block)
+                continue;
+            taken[b] = 1;
+            g.push_back(c);
+        }
+        if (c0->dim == 2) MPH_TRY(batched_solve_t<2>(g, c0->pair_pack, c0->pair_block, c0->ct_block, par));
+        else MPH_TRY(batched_solve_t<3>(g, c0->pair_pack, c0->pair_block, c0->ct_block, par));
+    }
     return MPH_OK;
 }
 

@@ -113,26 +113,96 @@ int batch_step(mph_case** cases, int ncases, int nsteps, int workers)
     const int nw = workers > 0 ? std::min(workers, ncases) : default_workers(ncases);
     std::vector<int> status(ncases, MPH_OK);
     std::vector<std::string> msg(ncases);
-    std::atomic<int> next{0};
-    auto work = [&]() {
-        int k;
-        while ((k = next.fetch_add(1)) < ncases) {
-            mph_case* c = cases[k];
-            cudaSetDevice(c->device);
-            int st;
-            try {
-                st = case_step(c, nsteps);
-            } catch (...) {
-                st = fail(MPH_ERR_STATE, "exception in a batched step");
+    // run f(k) for every case k on the worker pool (a case's failure is kept,
+    // and the case skipped afterwards)
+    auto parallel = [&](auto&& f) {
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            int k;
+            while ((k = next.fetch_add(1)) < ncases) {
+                if (status[k] != MPH_OK) continue;
+                mph_case* c = cases[k];
+                cudaSetDevice(c->device);
+                int st;
+                try {
+                    st = f(k);
+                } catch (...) {
+                    st = fail(MPH_ERR_STATE, "exception in a batched step");
+                }
+                status[k] = st;
+                if (st != MPH_OK) msg[k] = last_error();
             }
-            status[k] = st;
-            if (st != MPH_OK) msg[k] = last_error();
-        }
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nw; ++w) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
     };
-    std::vector<std::thread> pool;
-    for (int w = 1; w < nw; ++w) pool.emplace_back(work);
-    work();
-    for (auto& t : pool) t.join();
+    bool batched = false;   // some case may solve in the batched solve (option batch_solve, mixed form)
+    for (int k = 0; k < ncases; ++k)
+        if (cases[k]->batch_solve && cases[k]->precision == MPH_PRECISION_MIXED && !cases[k]->prof.on) batched = true;
+    if (!batched) {
+        parallel([&](int k) -> int { return case_step(cases[k], nsteps); });
+    } else {
+        // step by step: the stages before the solve on the worker pool; the
+        // eligible cases' solve batched on this thread (the CR iterations of
+        // every case in one launch per kernel), the others' on the pool; the
+        // step's end for all
+        std::vector<int> last(ncases, MPH_OK);
+        for (int s = 0; s < nsteps; ++s) {
+            parallel([&](int k) -> int {
+                mph_case* c = cases[k];
+                MPH_TRY(stage_step_begin(c));
+                MPH_TRY(stage_cellsort(c));
+                MPH_TRY(stage_neighbors(c));
+                MPH_TRY(stage_explicit(c));
+                MPH_TRY(stage_assemble(c));
+                return stage_mg_build(c);
+            });
+            std::vector<mph_case*> group;
+            std::vector<int> group_k;
+            for (int k = 0; k < ncases; ++k)
+                if (status[k] == MPH_OK && batch_solve_eligible(cases[k])) {
+                    group.push_back(cases[k]);
+                    group_k.push_back(k);
+                }
+            if (!group.empty()) {
+                cudaSetDevice(group[0]->device);
+                const int dev = group[0]->device;
+                // the per-case host parts on the worker pool
+                auto par = [&](int n, const std::function<int(int)>& f) {
+                    std::atomic<int> next{0};
+                    auto work = [&]() {
+                        cudaSetDevice(dev);
+                        int k;
+                        while ((k = next.fetch_add(1)) < n) f(k);
+                    };
+                    std::vector<std::thread> pool;
+                    for (int w = 1; w < std::min(nw, n); ++w) pool.emplace_back(work);
+                    work();
+                    for (auto& t : pool) t.join();
+                };
+                const int st = batched_mixed_solve(group, par);
+                if (st != MPH_OK)
+                    for (int k : group_k) {
+                        status[k] = st;
+                        msg[k] = last_error();
+                    }
+            }
+            parallel([&](int k) -> int {
+                mph_case* c = cases[k];
+                if (c->stage == 6) MPH_TRY(stage_solve(c));   // not in the batched solve
+                MPH_TRY(stage_step_end(c));
+                if (c->stats.status != MPH_OK) last[k] = c->stats.status;
+                return MPH_OK;
+            });
+        }
+        for (int k = 0; k < ncases; ++k)
+            if (status[k] == MPH_OK && last[k] != MPH_OK) {
+                status[k] = last[k];
+                msg[k] = "the solve did not converge";
+            }
+    }
     for (int k = 0; k < ncases; ++k)
         if (borrowed[k]) cases[k]->stream = nullptr;
     int last = MPH_OK;

@@ -190,6 +190,10 @@ int mph_case_set_option(mph_case* c, const char* name, double value)
         c->mg_coarsest = v;
         return MPH_OK;
     }
+    if (std::string(name) == "batch_solve") {
+        c->batch_solve = value != 0.0;
+        return MPH_OK;
+    }
     if (std::string(name) == "pair_fuse") {
         c->pair_fuse = value != 0.0;
         return MPH_OK;

@@ -27,6 +27,7 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/mph_gb300.h"
@@ -253,6 +254,9 @@ struct mph_case {
     bool pair_recompute = false;        // pair-term operator: evaluate g from the FP32 positions per slot (else slot records)
     bool pair_pack = true;              // pair-term operator: 6-byte slot records (packed g, 2-byte index; else FP16, 8 bytes)
     bool pair_fuse = false;             // point-Jacobi pair path: pair terms written sliced by one kernel (no pair-term list)
+    bool batch_solve = false;           // in mph_batch_step: the CR iterations launched over the batch's cases together
+                                        // (measured slower on the 512-case ensemble: the step-wide barriers cost more
+                                        // than the launches saved)
     bool split_apply = false;           // pair-term operator: transposed apply beside the viscous kernel (fork / join;
                                         // measured slower: the viscous kernel fills every SM)
     cudaStream_t fork_stream = nullptr; // its side stream and events
@@ -380,6 +384,36 @@ int launch_assemble(mph_case* c);
 int launch_assemble_cells(mph_case* c, int kmax_rows, bool mix, bool* done);
 int build_ct(mph_case* c);
 bool factored_applies(const mph_case* c);
+// One case of a CR iteration launched over several cases (the batched
+// solve): the case's arrays and its share of each launch.  A block finds its
+// case from the launches' block starts and runs the single-case kernel body
+// with its block index inside the case, so each case's arithmetic, and its
+// reductions' order, are the single-case launch's.
+struct BatchCase {
+    int N, Nf, n, cap;                 // particles, fluid rows, vector length, iteration cap
+    int ct_loc, vp_loc;                // the case's blocks stage s (shared memory of the transposed / viscous kernel)
+    int ct_nb, vp_nb, el_nb;           // the case's block counts: transposed apply, viscous kernel, vector kernels
+    const long long* ctsptr; const int* ct_cnt; const float4* ctsval; float* tct32; const int* ctuniq; const int* ctucount;
+    const int* nfc; const long long* sptr; const int* acol; const unsigned short* grec16; const unsigned* grec32;
+    const unsigned short* lcol16; const float* pscale; const float* sdiag32; const int* ncp; const long long* psptr;
+    const float4* psval; const int* uniq; const int* ucount;
+    float *s32, *y32, *p32, *q32, *u32, *z32, *r32;
+    const float* invD;
+    double* scal; int* flags; double* partials; unsigned* counter;
+};
+// one FP32 CR iteration over the cases of a batch (all in the point-Jacobi
+// mixed form on the pair path, one dimension, one record format and one
+// pair / transposed block width): four launches on `st`; b0 holds the three
+// launches' block starts per case (3 x (ncases + 1) ints, device)
+void launch_batch_iteration(const BatchCase* cases_dev, const int* b0_dev, int ncases, int dim, bool pack, int pair_block,
+                            int ct_block, int vp_smem, int ct_smem, const int* nblocks, cudaStream_t st);
+void launch_batch_operator(const BatchCase* cs, const int* ct_b0, const int* vp_b0, int nc, int dim, bool pack, int pair_block,
+                           int ct_block, int vp_smem, int ct_smem, int ct_blocks, int vp_blocks, cudaStream_t st);
+// par(n, f): run f(0) .. f(n-1) (the batch's host worker pool); the per-case
+// host parts of the batched solve (phase tests, updates) run through it
+int batched_mixed_solve(std::vector<mph_case*>& cases, const std::function<void(int, const std::function<int(int)>&)>& par);
+bool batch_solve_eligible(const mph_case* c);
+
 // the mixed form preconditioned by point Jacobi (option mg_depth -1): no
 // multigrid levels are built or used
 inline bool mixed_jacobi(const mph_case* c) { return c->precision == MPH_PRECISION_MIXED && c->mg_depth < 0; }

@@ -44,49 +44,56 @@ __device__ __forceinline__ double block_sum(double v)
 }
 
 // Store this block's partial; the last block reduces all partials in block
-// order into *out.  Every thread of every block must call it.
+// order into *out.  Every thread of every block must call it.  lb / nb: the
+// block's index and the block count of its reduction (a launch's own, or one
+// case's share of a launch over several cases).
 __device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
-                                                double* __restrict__ out)
+                                                double* __restrict__ out, int lb, int nb)
 {
     __shared__ bool last;
     const double bs = block_sum(v);
     if (threadIdx.x == 0) {
-        partials[blockIdx.x] = bs;
+        partials[lb] = bs;
         __threadfence();
         const unsigned ticket = atomicAdd(counter, 1u);
-        last = (ticket == gridDim.x - 1);
+        last = (ticket == (unsigned)nb - 1);
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
     double s = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ((volatile double*)partials)[b];
     s = block_sum(s);
     if (threadIdx.x == 0) {
         *out = s;
         *counter = 0u;
     }
 }
+__device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+                                                double* __restrict__ out)
+{
+    reduce_finalize(v, partials, counter, out, (int)blockIdx.x, (int)gridDim.x);
+}
 
 // As reduce_finalize; the last block also advances the device iteration
 // counter *it (every block read it before taking its ticket).  Returns true
 // in thread 0 of the last block, after the stores.
 __device__ __forceinline__ bool reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
-                                                     double* __restrict__ out, int* __restrict__ it)
+                                                     double* __restrict__ out, int* __restrict__ it, int lb, int nb)
 {
     __shared__ bool last;
     const double bs = block_sum(v);
     if (threadIdx.x == 0) {
-        partials[blockIdx.x] = bs;
+        partials[lb] = bs;
         __threadfence();
         const unsigned ticket = atomicAdd(counter, 1u);
-        last = (ticket == gridDim.x - 1);
+        last = (ticket == (unsigned)nb - 1);
     }
     __syncthreads();
     if (!last) return false;
     __threadfence();
     double s = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += ((volatile double*)partials)[b];
     s = block_sum(s);
     if (threadIdx.x == 0) {
         *out = s;
@@ -94,6 +101,24 @@ __device__ __forceinline__ bool reduce_finalize_step(double v, double* __restric
         *it = *it + 1;
     }
     return threadIdx.x == 0;
+}
+__device__ __forceinline__ bool reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+                                                     double* __restrict__ out, int* __restrict__ it)
+{
+    return reduce_finalize_step(v, partials, counter, out, it, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// The case of launch block b: the last case whose first block is <= b (b0:
+// ncases + 1 block starts; a case without blocks is never found).
+__device__ __forceinline__ int batch_case_of(const int* __restrict__ b0, int ncases, int b)
+{
+    int lo = 0, hi = ncases - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b0[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Capture `body` (a fixed launch sequence on c->stream) into a CUDA graph and

@@ -47,6 +47,37 @@ def test_batch_step_matches_alone(engine_lib):
         g.close()
 
 
+def test_batched_solve_matches_per_case_solve(engine_lib):
+    """With option batch_solve, mph_batch_step solves its point-Jacobi mixed
+    cases together (the CR iterations of all of them in one launch per
+    kernel, each block on its case with the case's own block decomposition),
+    so every case gets the bits and the iteration counts of its own solve:
+    the batch with the option off is the reference.  Cases of
+    several sizes and both dimensions, so the batch forms groups and its
+    cases finish their refinement phases at different times."""
+    ens = casegen.ensemble_2d(10, seed=3)
+    picked = [(2, params, parts) for params, parts in ens if parts.count < 20000][:6]
+    for name, dim, params, parts in CASES:
+        picked.append((dim, params, parts))
+    runs = {}
+    for on in (0, 1):
+        cases = []
+        for dim, params, parts in picked:
+            g = engine.Case(params, parts, dim, precision=PRECISION_MIXED)
+            g.set_solver(1e-8, 1e-3, 50)
+            g.set_option("extrapolate", 2)
+            g.set_option("batch_solve", on)
+            cases.append(g)
+        assert serving.batch_step(cases, 3) in (0, 7)
+        runs[on] = [(g.fields(("id", "pos", "vel")), g.solve_stats()) for g in cases]
+        for g in cases:
+            g.close()
+    for (fa, sa), (fb, sb) in zip(runs[0], runs[1]):
+        assert sa["iter"] == sb["iter"] and sa["outer"] == sb["outer"] and sa["status"] == sb["status"]
+        for k in ("id", "pos", "vel"):
+            assert np.array_equal(fa[k], fb[k]), k
+
+
 def test_batch_rejects_duplicates(engine_lib):
     name, dim, params, parts = CASES[0]
     g = engine.Case(params, parts, dim)
