@@ -564,11 +564,13 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 //   k_visc_pen32   y_i = (inertia + sum_{wall j} f e (x) e) s_i
 //                        + sum_{fluid j} g (g . (s_i - s_j)) + sum_k lambda_k C_ik t_k
 //                  with g = sqrt(f) e (f >= 0, so a fluid pair's terms
-//                  f e (x) e are g (x) g), read as FP16 scaled per slice: 6
-//                  bytes a slot in 3-D against 36 for an FP32 block (the
-//                  viscous part is a few 1e-3 of the operator, so the 2^-11
+//                  f e (x) e are g (x) g), read from the packed slot records
+//                  (11/11/10-bit fixed point of the slice's scale and a
+//                  2-byte index: 6 bytes a slot, against 36 for an FP32
+//                  block; option pair_pack 0: FP16, 8 bytes) — the viscous
+//                  part is a few 1e-3 of the operator, so the 2^-11
 //                  rounding of g moves the inner operator by ~1e-5 of itself;
-//                  the FP64 outer residual takes the FP32 g).  (s, y) goes
+//                  the FP64 outer residual takes the FP32 g.  (s, y) goes
 //                  into the iteration's rho slot.  The pairs act on
 //                  differences s_i - s_j, so the viscous sum has no
 //                  cancellation between a large diagonal and its row.

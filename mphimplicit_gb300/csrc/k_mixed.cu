@@ -1,6 +1,7 @@
 // k_mixed.cu - mixed-precision solve of the step's system: FP32 conjugate
-// residual + FP32 V-cycle, with the FP64 residual replacing the recursive one
-// at every refinement step.
+// residual preconditioned by point Jacobi (option mg_depth -1, the default)
+// or the FP32 V-cycle, with the FP64 residual replacing the recursive one at
+// every refinement step.
 //
 //   x = v* - F/m dt ; r = b - A x                 (FP64, as the reference)
 //   r32 = r / ||r_0|| ; s = M r32                  (one scale for the whole solve)
@@ -27,8 +28,8 @@ bool mixed_available() { return true; }
 
 __host__ __device__ __forceinline__ int rho32_slot(int it) { return 20 + (it & 1); }
 enum { kSIn0 = 16, kSIn = 17, kSQU32 = 18, kSTol2 = 23, kSScale = 24 };   // kSTol2: this phase's inner target
-constexpr int kDeviceLoopMax = 100000;
-constexpr int kVcycleEvents = 2 * kMaxGraphChunk;   // gev: operator pairs first, then V-cycle pairs   // bound on the device-driven solve's inner iterations
+constexpr int kDeviceLoopMax = 100000;   // bound on the device-driven solve's inner iterations
+constexpr int kVcycleEvents = 2 * kMaxGraphChunk;   // gev: operator pairs first, then preconditioner pairs
 
 template <int D, int MODE, typename V>
 __global__ void __launch_bounds__(128) k_spmv32(int Nf, const int* __restrict__ nfc, const long long* __restrict__ sptr,
