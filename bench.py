@@ -491,6 +491,45 @@ def run_ensemble(args, line_base):
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     total_s = sum(step_ms) / 1000.0
     value = N * args.steps / total_s
+    # end to end: the same cases go on for K more steps, each step uploading
+    # every case's state from pinned host buffers (the state continuing the
+    # case's own steps) and reading it back after the batched step; the
+    # per-case copies on a host thread pool (ctypes releases the GIL)
+    e2e_value, e2e_bytes = None, 0
+    e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
+    if e2e_steps > 0:
+        from concurrent.futures import ThreadPoolExecutor
+
+        def pinned(shape, dt):
+            return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+        bufs = []
+        for g in cases:
+            n = g.count
+            f = {"id": pinned((n,), torch.int32), "type": pinned((n,), torch.int32), "pos": pinned((n, 3), torch.float64),
+                 "vel": pinned((n, 3), torch.float64)}
+            g.fields(out=f)
+            if prec == PRECISION_MIXED:
+                g.set_option("keep_history", 1)
+            bufs.append(f)
+
+        def up(k):
+            g, f, parts = cases[k], bufs[k], ens[k][1]
+            g.set_state(casegen.Particles(g.time(), parts.spacing, parts.domain_min, parts.domain_max, f["type"], f["pos"],
+                                          f["vel"]), f["id"])
+
+        def down(k):
+            cases[k].fields(out=bufs[k])
+        with ThreadPoolExecutor(max_workers=args.workers) as pool:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                list(pool.map(up, range(len(cases))))
+                serving.batch_step(cases, 1, args.workers)
+                list(pool.map(down, range(len(cases))))
+            torch.cuda.synchronize()
+            e2e_s = time.perf_counter() - t0
+        e2e_value = N * e2e_steps / e2e_s
+        e2e_bytes = N * (3 * 8 * 2 + 4 + 4)
     for g in cases:
         g.close()
     # plain FP64 form, one case after the other, on an evenly spaced sample
@@ -523,7 +562,8 @@ def run_ensemble(args, line_base):
                    "speedup_vs_plain_fp64_sequential": value / plain,
                    "vel_rel_err_vs_fp64_per_step": errs},
         "gpu_launches": launches, "clocks": clk.summary(),
-        "e2e": {"value": None, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": e2e_bytes, "d2h_bytes_per_step": e2e_bytes,
+                "steps": e2e_steps, "note": "every case's state uploaded from and read back into pinned host buffers each step"},
     })
     print(json.dumps(line), flush=True)
     return 0
