@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(128) k_matrix_c(DevParams P, const double* __r
             load_vec<D>(pos, j, xj);
             sep_vec<D>(P, xj, xi, q);
             const double r2 = norm2_exact<D>(q);
-            if (r2 != 0.0 && rP2 - r2 > 0) {
+            if (r2_pos_below(r2, rP2)) {
                 const double inv = rsqrt(r2);
                 const double wd = -P.kfp * (P.m2h_rp * (1.0 - (r2 * inv) * P.inv_rp));
 #pragma unroll
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128) k_vector_p(DevParams P, const int* __rest
         load_vec<D>(pos, j, xj);
         sep_vec<D>(P, xj, xi, q);
         const double r2 = norm2_exact<D>(q);
-        if (r2 == 0.0 || !(rP2 - r2 > 0)) continue;
+        if (!r2_pos_below(r2, rP2)) continue;
         const double inv = rsqrt(r2);
         const double wd = -P.kfp * (P.m2h_rp * (1.0 - (r2 * inv) * P.inv_rp));
         double vj[3];
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
         sep_vec<D>(P, xj, xi, q);
         const double r2 = norm2_exact<D>(q);
         const bool fluid = k < nf;
-        if (r2 != 0.0 && rV2 - r2 > 0) {
+        if (r2_pos_below(r2, rV2)) {
             // one reciprocal square root per pair (FP64 divide and sqrt are
             // slow on this part); -dw/dr = -kf (-2/h) (1 - r/h)
             const double inv = rsqrt(r2);
@@ -308,8 +308,7 @@ __global__ void __launch_bounds__(128) k_matrix_a(DevParams P, Level0Map M, cons
         touched |= 1ull << run_slot;
     }
     // self block: viscous sum, inertia, C Lambda C^T(i, i)
-    const double m = P.density[ti] * P.vol;
-    const double inert = m / P.vol / P.dt;
+    const double inert = P.inert64[ti];   // (rho vol) / vol / dt, formed on the host
     {
         double cc[D][D];
 #pragma unroll

@@ -233,7 +233,7 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
             load_vec<D>(pos, j, xj);
             sep_vec<D>(P, xj, xi, q);
             const double r2 = norm2_exact<D>(q);
-            if (!(r2 != 0.0 && rV2 - r2 > 0)) continue;
+            if (!r2_pos_below(r2, rV2)) continue;
             const double inv = rsqrt(r2);
             const double wd = -P.kfv * (P.m2h_rv * (1.0 - (r2 * inv) * P.inv_rv));
             const double f = P.visc * P.muij[ti][type[j]] * wd * inv;
@@ -283,9 +283,9 @@ k_assemble_cells(DevParams P, CellMap M, int rx, int ry, int rz, int mwords, int
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
         const int self = __reduce_max_sync(0xffffffffu, myself);
-        // inertia density/dt as the reference forms it, (rho*vol)/vol/dt; the
-        // FP32 form takes its host-rounded FP32 value (no FP64 on the device)
-        const T inert = MIX ? (T)P.inert32[ti] : (T)(P.density[ti] * P.vol / P.vol / P.dt);
+        // inertia density/dt as the reference forms it, (rho*vol)/vol/dt,
+        // formed once on the host (its FP32 rounding for the FP32 form)
+        const T inert = MIX ? (T)P.inert32[ti] : (T)P.inert64[ti];
         __syncwarp();
         if (lane == 0) {
 #pragma unroll

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(128) k_density_p(DevParams P, const double* __
         load_vec<D>(pos, j, xj);
         sep_vec<D>(P, xj, xi, q);
         const double r2 = norm2_exact<D>(q);
-        if (rP2 - r2 >= 0) sp = DADD(sp, w_quad(P.kfp, __dsqrt_rn(r2), P.rP));
+        if (r2_within(r2, rP2)) sp = DADD(sp, w_quad(P.kfp, __dsqrt_rn(r2), P.rP));
     }
     vsp[i] = DSUB(sp, P.N0p);
 }

@@ -143,6 +143,40 @@ __device__ __forceinline__ void pair_ef(const DevParams& P, int i, int j, int ti
     }
 }
 
+// The end of a fluid row in the pair-term kernels, from its warp's per-lane
+// partial sums: b_i = - C p + inertia v in FP64 (the lanes' sums by
+// reduce-scatter; lane 8 r in 3-D, 16 r in 2-D, writes component r) and, with
+// dinv, the inverse diagonal of A from FP32 sums (the mixed form's
+// point-Jacobi preconditioner; lane r writes component r).
+template <int D>
+__device__ __forceinline__ void pair_row_end(const DevParams& P, int i, int ti, int lane, const double* sumv,
+                                             const double* vi, float* tvd, float* dpd, double* __restrict__ bvec,
+                                             double* __restrict__ dinv)
+{
+    const double sr = warp_sum_scatter<D>(sumv, lane);
+    constexpr int kStep = D == 3 ? 8 : 16;
+    const int r = lane / kStep;
+    if (lane % kStep == 0 && r < D) {
+        const double vr = r == 0 ? vi[0] : (r == 1 || D == 2 ? vi[1] : vi[2]);
+        bvec[(size_t)i * D + r] = sr + P.inert64[ti] * vr;   // inertia as the assembly forms it
+    }
+    if (dinv) {
+#pragma unroll
+        for (int c = 0; c < D; ++c)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                tvd[c] += __shfl_xor_sync(0xffffffffu, tvd[c], o);
+                dpd[c] += __shfl_xor_sync(0xffffffffu, dpd[c], o);
+            }
+        if (lane < D) {
+            const float tv = lane == 0 ? tvd[0] : (lane == 1 ? tvd[1] : tvd[2]);
+            const float dp = lane == 0 ? dpd[0] : (lane == 1 ? dpd[1] : dpd[2]);
+            const float dg = P.inert32[ti] + tv + dp;
+            dinv[(size_t)i * D + lane] = (double)(dg != 0.f ? 1.f / dg : 0.f);
+        }
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(kPtWarps * 32)
 k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict__ pos, const float* __restrict__ pos32,
@@ -204,32 +238,7 @@ k_pair_terms(DevParams P, const int* __restrict__ type, const double* __restrict
                 }
             }
         }
-#pragma unroll
-        for (int r = 0; r < D; ++r)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
-        if (lane == 0) {
-            const double inert = P.density[ti] * P.vol / P.vol / P.dt;   // as the assembly
-#pragma unroll
-            for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
-        }
-        if (dinv) {   // the inverse diagonal of A, FP32 sums (the mixed form's point-Jacobi preconditioner)
-#pragma unroll
-            for (int r = 0; r < D; ++r)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    tvd[r] += __shfl_xor_sync(0xffffffffu, tvd[r], o);
-                    dpd[r] += __shfl_xor_sync(0xffffffffu, dpd[r], o);
-                }
-            if (lane == 0) {
-                const float in32 = P.inert32[ti];
-#pragma unroll
-                for (int r = 0; r < D; ++r) {
-                    const float dg = in32 + tvd[r] + dpd[r];
-                    dinv[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
-                }
-            }
-        }
+        pair_row_end<D>(P, i, ti, lane, sumv, vi, tvd, dpd, bvec, dinv);
     }
 }
 
@@ -369,24 +378,7 @@ k_pair_slices(DevParams P, const int* __restrict__ type, const double* __restric
             dpd[r] += cl * (float)cval[(pb + a) * D + r];
         }
     }
-#pragma unroll
-    for (int r = 0; r < D; ++r)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sumv[r] += __shfl_xor_sync(0xffffffffu, sumv[r], o);
-            tvd[r] += __shfl_xor_sync(0xffffffffu, tvd[r], o);
-            dpd[r] += __shfl_xor_sync(0xffffffffu, dpd[r], o);
-        }
-    if (lane == 0) {
-        const double inert = P.density[ti] * P.vol / P.vol / P.dt;   // as the assembly
-        const float in32 = P.inert32[ti];
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            bvec[(size_t)i * D + r] = sumv[r] + inert * vi[r];
-            const float dg = in32 + tvd[r] + dpd[r];
-            dinv[(size_t)i * D + r] = (double)(dg != 0.f ? 1.f / dg : 0.f);
-        }
-    }
+    pair_row_end<D>(P, i, ti, lane, sumv, vi, tvd, dpd, bvec, dinv);
 }
 
 // The wall neighbours of every fluid row in FP64 (after k_pair_terms), a
@@ -413,6 +405,9 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
     const int n = nc[i], nf = nfc[i];
     double sd[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};   // xx xy xz yy yz zz
     double sw[3] = {0.0, 0.0, 0.0};
+    // this lane's warp sum after the reduce-scatter: value lane >> 1 of
+    // (sd[0..5], sw[0..2]); zero for a row without wall slots
+    double val = 0.0;
     if (n > nf) {
         const long long nb = nptr[i];
         const double rV2 = P.rV * P.rV;
@@ -425,7 +420,7 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
             load_vec<D>(pos, j, xj);
             sep_vec<D>(P, xj, xi, q);
             const double r2 = norm2_exact<D>(q);
-            if (!(r2 != 0.0 && rV2 - r2 > 0)) continue;
+            if (!r2_pos_below(r2, rV2)) continue;
             const double inv = rsqrt(r2);
             const double wd = -P.kfv * (P.m2h_rv * (1.0 - (r2 * inv) * P.inv_rv));
             const double f = P.visc * P.muij[ti][type[j]] * wd * inv;
@@ -445,25 +440,21 @@ __global__ void __launch_bounds__(256) k_wall_terms64(DevParams P, const int* __
             sd[4] += f * e[1] * e[2];
             sd[5] += f * e[2] * e[2];
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-            for (int t = 0; t < 6; ++t) sd[t] += __shfl_xor_sync(0xffffffffu, sd[t], o);
-#pragma unroll
-            for (int r = 0; r < 3; ++r) sw[r] += __shfl_xor_sync(0xffffffffu, sw[r], o);
-        }
-        if (lane == 0)
-#pragma unroll
-            for (int r = 0; r < D; ++r) bvec[(size_t)i * D + r] += sw[r];
+        // the butterfly's sums (the same bits) with 16 FP64 adds a lane, not 45
+        double v[16] = {sd[0], sd[1], sd[2], sd[3], sd[4], sd[5], sw[0], sw[1], sw[2],
+                        0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        val = warp_reduce_scatter<16>(v, lane);
+        const int t = lane >> 1;
+        if ((lane & 1) == 0 && t >= 6 && t < 6 + D) bvec[(size_t)i * D + (t - 6)] += val;
     }
-    if (sdiag32 && lane == 0) {
-        float4* o = reinterpret_cast<float4*>(sdiag32 + (size_t)i * 8);
-        o[0] = make_float4((float)sd[0], (float)sd[1], (float)sd[2], (float)sd[3]);
-        o[1] = make_float4((float)sd[4], (float)sd[5], P.inert32[ti], 0.f);
-        double2* o64 = reinterpret_cast<double2*>(sdiag64 + (size_t)i * 8);
-        o64[0] = make_double2(sd[0], sd[1]);
-        o64[1] = make_double2(sd[2], sd[3]);
-        o64[2] = make_double2(sd[4], sd[5]);
+    if (sdiag32) {   // lane 2 t writes component t: one FP32 conversion a lane
+        const int t = lane >> 1;
+        if ((lane & 1) == 0 && t < 6) {
+            sdiag32[(size_t)i * 8 + t] = (float)val;
+            sdiag64[(size_t)i * 8 + t] = val;
+        }
+        if (lane == 1) sdiag32[(size_t)i * 8 + 6] = P.inert32[ti];
+        if (lane == 3) sdiag32[(size_t)i * 8 + 7] = 0.f;
     }
 }
 
@@ -542,7 +533,7 @@ k_resid_factored(DevParams P, const int* __restrict__ type, const int* __restric
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) y[d] += __shfl_xor_sync(0xffffffffu, y[d], o);
         if (lane == 0) {
-            const double inert = P.density[type[i]] * P.vol / P.vol / P.dt;
+            const double inert = P.inert64[type[i]];
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const size_t k = (size_t)i * D + d;
@@ -590,19 +581,30 @@ __device__ __forceinline__ void ct_apply32_body(int lb, int N, const long long* 
 {
     extern __shared__ float xs_ct[];   // LOC: s of the lists' fluid rows by rank, a float4 (3-D) or float2 (2-D) each
     constexpr int XS = D == 3 ? kXs3 : 2;
-    if (flags[kFlagDone]) return;
-    const int it = flags[kFlagIter];
-    const double tol2 = scal[kSTol2];
-    const double rr0 = scal[kSIn0];
-    const double rr = it == 0 ? rr0 : scal[kSIn];
-    const bool bad = !(rr == rr);
-    if (it >= cap || rr / rr0 < tol2 || bad) {
-        if (lb == 0 && threadIdx.x == 0) {
-            flags[kFlagDone] = 1;
-            if (bad) flags[kFlagBad] = 1;
+    // the flags and the stop test once a block, by one thread (the test's FP64
+    // quotient in every warp took a large share of the kernel's issue: FP64
+    // runs at a small fraction of the FP32 rate on this part)
+    __shared__ int go_s;
+    if (threadIdx.x == 0) {
+        int go = !flags[kFlagDone];
+        if (go) {
+            const int it = flags[kFlagIter];
+            const double tol2 = scal[kSTol2];
+            const double rr0 = scal[kSIn0];
+            const double rr = it == 0 ? rr0 : scal[kSIn];
+            const bool bad = !(rr == rr);
+            if (it >= cap || rr / rr0 < tol2 || bad) {
+                go = 0;
+                if (lb == 0) {
+                    flags[kFlagDone] = 1;
+                    if (bad) flags[kFlagBad] = 1;
+                }
+            }
         }
-        return;
+        go_s = go;
     }
+    __syncthreads();
+    if (!go_s) return;   // block-uniform
     const int k = lb * blockDim.x + threadIdx.x;
     int U = -1;
     if (LOC) {   // block-uniform
@@ -1247,7 +1249,7 @@ k_resid_pairs(DevParams P, int Nf, const int* __restrict__ type, const int* __re
 #pragma unroll
             for (int d = 0; d < D; ++d) y[d] += cval[(pb + a) * D + d] * lt;
         }
-        const double inert = P.density[type[i]] * P.vol / P.vol / P.dt;
+        const double inert = P.inert64[type[i]];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             const size_t k = (size_t)i * D + d;

@@ -112,9 +112,20 @@ __device__ __forceinline__ void pq_jacobi32_body(int lb, int nb, int n, const V*
                               const V* __restrict__ invD, V* __restrict__ u, double* __restrict__ scal,
                               const int* __restrict__ flags, double* __restrict__ partials, unsigned* __restrict__ counter)
 {
-    if (flags[kFlagDone]) return;
-    const int it = flags[kFlagIter];
-    const V beta = it == 0 ? (V)0 : (V)(scal[rho32_slot(it)] / scal[rho32_slot(it - 1)]);
+    // the flags and beta once a block, by one thread: an FP64 quotient in
+    // every warp took a large share of this short kernel (FP64 issues at a
+    // small fraction of the FP32 rate on this part)
+    __shared__ int it_s;
+    __shared__ V beta_s;
+    if (threadIdx.x == 0) {
+        const int it0 = flags[kFlagDone] ? -1 : flags[kFlagIter];
+        if (it0 > 0) beta_s = (V)(scal[rho32_slot(it0)] / scal[rho32_slot(it0 - 1)]);
+        it_s = it0;
+    }
+    __syncthreads();
+    const int it = it_s;
+    if (it < 0) return;   // the solve is done (block-uniform)
+    const V beta = it == 0 ? (V)0 : beta_s;
     // a thread's few terms (q u = q^2 / d >= 0) in FP32, the threads in FP64
     float acc = 0.f;
     for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
@@ -152,13 +163,20 @@ __device__ __forceinline__ void xrs32_body(int lb, int nb, int n, V* __restrict_
                         double* __restrict__ scal, int* __restrict__ flags, double* __restrict__ partials,
                         unsigned* __restrict__ counter, int cap = 0, int use_cond = 0, cudaGraphConditionalHandle cond = 0)
 {
-    if (flags[kFlagDone]) {
+    __shared__ int go_s;   // the flags and alpha once a block, as in pq_jacobi32_body
+    __shared__ V alpha_s;
+    if (threadIdx.x == 0) {
+        const int go = !flags[kFlagDone];
+        if (go) alpha_s = (V)(scal[rho32_slot(flags[kFlagIter])] / scal[kSQU32]);
+        go_s = go;
+    }
+    __syncthreads();
+    if (!go_s) {   // block-uniform
         if constexpr (COND)
             if (use_cond && lb == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
         return;
     }
-    const int it = flags[kFlagIter];
-    const V alpha = (V)(scal[rho32_slot(it)] / scal[kSQU32]);
+    const V alpha = alpha_s;
     float acc = 0.f;   // a thread's few squares in FP32, the threads in FP64
     for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
         z[k] += alpha * p[k];

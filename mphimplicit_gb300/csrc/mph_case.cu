@@ -168,6 +168,9 @@ static int derive(mph_case* c, const mph_particles* parts)
         for (int u = 0; u < kTypeCount; ++u)
             P.muij[t][u] = 2.0 * (P.mu[t] * P.mu[u]) / (P.mu[t] + P.mu[u]);
     for (int t = 0; t < kTypeCount; ++t) {
+        // IEEE products and quotients, no contraction: the kernels' FP64
+        // inertia to the bit, without two divisions a row on the device
+        P.inert64[t] = P.density[t] * P.vol / P.vol / P.dt;
         P.inert32[t] = (float)(P.density[t] * P.vol / P.vol / P.dt);
         P.lambda32[t] = (float)P.lambda[t];
         for (int u = 0; u < kTypeCount; ++u) P.vm32[t][u] = (float)(P.visc * P.muij[t][u]);

@@ -32,12 +32,31 @@ __device__ __forceinline__ double mod_exact(double x, double w)
 
 // Minimum-image component x_j - x_i: Mod(xj - xi + W/2, W) - W/2.  For
 // 0 <= t < wsafe (wsafe = 0.75 W) floor(t/W) is 0 and Mod(t, W) == t exactly,
-// so the division is skipped.
+// so the division is skipped.  The range test compares bit patterns on the
+// integer pipe (FP64 issues at a small fraction of the FP32 rate on this
+// part): non-negative doubles order as their bit patterns; -0 (never formed
+// here: hw > 0) and NaN of either sign take the exact path, which returns the
+// same.
 __device__ __forceinline__ double sep_exact(double xj, double xi, double hw, double w, double wsafe)
 {
     const double t = DADD(DSUB(xj, xi), hw);
-    const double m = (t >= 0.0 && t < wsafe) ? t : mod_exact(t, w);
+    const long long tb = __double_as_longlong(t);
+    const double m = (tb >= 0 && tb < __double_as_longlong(wsafe)) ? t : mod_exact(t, w);
     return DSUB(m, hw);
+}
+
+// Radius tests of a squared distance r2 from norm2_exact (+0, positive, or
+// NaN; never -0) against R2 > 0, by bit patterns as in sep_exact: the same
+// outcome as the FP64 forms named, NaN included.
+__device__ __forceinline__ bool r2_within(double r2, double R2)       // R2 - r2 >= 0
+{
+    const long long b = __double_as_longlong(r2);
+    return b >= 0 && b <= __double_as_longlong(R2);
+}
+__device__ __forceinline__ bool r2_pos_below(double r2, double R2)    // r2 != 0 && R2 - r2 > 0
+{
+    const long long b = __double_as_longlong(r2);
+    return b > 0 && b < __double_as_longlong(R2);
 }
 
 template <int D>
@@ -110,6 +129,66 @@ __device__ __forceinline__ double w_quad(double kf, double r, double h)
 __device__ __forceinline__ double dw_quad(double kf, double r, double h)
 {
     return DMUL(kf, DMUL(DDIV(-2.0, h), DSUB(1.0, DDIV(r, h))));
+}
+
+// The warp sums of D per-lane FP64 values by reduce-scatter: the same pairs,
+// each added once, as the xor butterfly `v += shfl_xor(v, o)` for o = 16 ... 1
+// (FP64 addition commutes, so every partial sum has the butterfly's bits),
+// with 6 FP64 adds a lane in 3-D (5 in 2-D) instead of 15 (10): FP64 issues
+// at a small fraction of the FP32 rate on this part.  Lane l returns the sum
+// of component min(l >> 3, 2) in 3-D, l >> 4 in 2-D.
+template <int D>
+__device__ __forceinline__ double warp_sum_scatter(const double* v, int lane)
+{
+    const unsigned full = 0xffffffffu;
+    const bool hi = (lane & 16) != 0;
+    if (D == 2) {
+        double a = hi ? v[1] : v[0];
+        a += __shfl_xor_sync(full, hi ? v[0] : v[1], 16);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) a += __shfl_xor_sync(full, a, o);
+        return a;
+    }
+    // lanes 0-15 keep components 0 and 1, lanes 16-31 component 2 (twice)
+    double a0 = hi ? v[2] : v[0];
+    double a1 = hi ? v[2] : v[1];
+    a0 += __shfl_xor_sync(full, hi ? v[0] : v[2], 16);
+    a1 += __shfl_xor_sync(full, hi ? v[1] : v[2], 16);
+    // lanes 0-7 component 0, 8-15 component 1, 16-31 component 2
+    const bool b8 = (lane & 8) != 0;
+    double a = b8 ? a1 : a0;
+    a += __shfl_xor_sync(full, b8 ? a0 : a1, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) a += __shfl_xor_sync(full, a, o);
+    return a;
+}
+
+// The same for N (a power of two up to 32) values a lane: at the step of
+// offset o, lanes with bit o set keep the upper half of their values and the
+// others the lower half, each adding the partner's copy of the half it keeps
+// (N - 1 adds, then plain butterfly steps: 16 adds for N = 16 against 80).
+// Lane l returns the warp sum of value l >> (5 - log2 N).
+template <int N>
+__device__ __forceinline__ double warp_reduce_scatter(double (&v)[N], int lane)
+{
+    constexpr int L = N == 2 ? 1 : N == 4 ? 2 : N == 8 ? 3 : N == 16 ? 4 : 5;
+    static_assert((1 << L) == N, "N must be a power of two, at most 32");
+#pragma unroll
+    for (int s = 0; s < L; ++s) {
+        const int o = 16 >> s;
+        const bool up = (lane & o) != 0;
+        const int h = (N >> s) / 2;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const double keep = up ? v[h + k] : v[k];
+            const double send = up ? v[k] : v[h + k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    double a = v[0];
+#pragma unroll
+    for (int o = 16 >> L; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
 }
 
 __device__ __forceinline__ bool is_wall(int t) { return t >= 2 && t < 4; }

@@ -57,6 +57,7 @@ struct DevParams {
     double visc;                               // 8 (2D) or 10 (3D)
     double inv_rv, m2h_rv, inv_rp, m2h_rp;     // 1/h and -2/h of the V and P kernels (assembly)
     double muij[kTypeCount][kTypeCount];       // harmonic mean 2 mu_i mu_j / (mu_i + mu_j)
+    double inert64[kTypeCount];                // density * vol / vol / dt in that order (the reference's inertia), once
     float maxR2_lo, maxR2_hi, rP2_lo, rP2_hi;  // FP32 pre-classification band
     float w32[3], hw32[3];
     float inert32[kTypeCount];                 // FP32 density/dt and bulk viscosity (mixed-form kernels)
