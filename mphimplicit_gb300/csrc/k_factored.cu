@@ -850,7 +850,7 @@ __device__ __forceinline__ void visc_pen32_body(int lb, int nb, int Nf, const in
             __syncthreads();
         }
     }
-    double acc = 0.0;
+    float acc = 0.f;
     if (i < Nf) {
         const int lane = i & 31;
         float xi[3] = {0.f, 0.f, 0.f};
@@ -865,13 +865,13 @@ __device__ __forceinline__ void visc_pen32_body(int lb, int nb, int Nf, const in
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] += in32 * xi[d];
         if (PPART) p_part32<D>(i, lane, ncp, psptr, psrec, t, yv);
-        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
+        float dot = 0.f;   // the row's D terms and a warp's rows in FP32, the warps in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
             dot += xi[d] * yv[d];
         }
-        acc = (double)dot;
+        acc = dot;
     }
     if (PPART) reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it), lb, nb);
 }
@@ -903,19 +903,19 @@ __global__ void __launch_bounds__(256) k_ppart32(int Nf, const int* __restrict__
     if (flags[kFlagDone]) return;
     const int it = flags[kFlagIter];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc = 0.0;
+    float acc = 0.f;
     if (i < Nf) {
         float yv[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < D; ++d) yv[d] = y[(size_t)i * D + d];
         p_part32<D>(i, i & 31, ncp, psptr, psrec, t, yv);
-        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
+        float dot = 0.f;   // the row's D terms and a warp's rows in FP32, the warps in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
             dot += x[(size_t)i * D + d] * yv[d];
         }
-        acc = (double)dot;
+        acc = dot;
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }
@@ -998,7 +998,7 @@ k_visc_rc32(DevParams P, int Nf, const float4* __restrict__ pt32, const int* __r
         }
     }
     const bool wr = *wrap != 0;
-    double acc = 0.0;
+    float acc = 0.f;
     if (i < Nf) {
         const int lane = i & 31;
         float xi[3] = {0.f, 0.f, 0.f};
@@ -1042,13 +1042,13 @@ k_visc_rc32(DevParams P, int Nf, const float4* __restrict__ pt32, const int* __r
                 if (D == 3) yv[2] += r.z * tk;
             }
         }
-        float dot = 0.f;   // the row's D terms in FP32, the rows in FP64
+        float dot = 0.f;   // the row's D terms and a warp's rows in FP32, the warps in FP64
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             y[(size_t)i * D + d] = yv[d];
             dot += xi[d] * yv[d];
         }
-        acc = (double)dot;
+        acc = dot;
     }
     reduce_finalize(acc, partials, counter, scal + rho32_slot_f(it));
 }

@@ -126,7 +126,7 @@ __device__ __forceinline__ void pq_jacobi32_body(int lb, int nb, int n, const V*
     const int it = it_s;
     if (it < 0) return;   // the solve is done (block-uniform)
     const V beta = it == 0 ? (V)0 : beta_s;
-    // a thread's few terms (q u = q^2 / d >= 0) in FP32, the threads in FP64
+    // a thread's few terms (q u = q^2 / d >= 0) and a warp's threads in FP32, the warps in FP64
     float acc = 0.f;
     for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
         const V pk = it == 0 ? s[k] : beta * p[k] + s[k];
@@ -137,7 +137,7 @@ __device__ __forceinline__ void pq_jacobi32_body(int lb, int nb, int n, const V*
         u[k] = uk;
         acc += qk * uk;
     }
-    reduce_finalize((double)acc, partials, counter, scal + kSQU32, lb, nb);
+    reduce_finalize(acc, partials, counter, scal + kSQU32, lb, nb);
 }
 
 template <typename V>
@@ -177,7 +177,7 @@ __device__ __forceinline__ void xrs32_body(int lb, int nb, int n, V* __restrict_
         return;
     }
     const V alpha = alpha_s;
-    float acc = 0.f;   // a thread's few squares in FP32, the threads in FP64
+    float acc = 0.f;   // a thread's few squares and a warp's threads in FP32, the warps in FP64
     for (int k = lb * blockDim.x + threadIdx.x; k < n; k += nb * blockDim.x) {
         z[k] += alpha * p[k];
         const V rk = r[k] - alpha * q[k];
@@ -185,7 +185,7 @@ __device__ __forceinline__ void xrs32_body(int lb, int nb, int n, V* __restrict_
         s[k] -= alpha * u[k];
         acc += rk * rk;
     }
-    const bool last = reduce_finalize_step((double)acc, partials, counter, scal + kSIn, flags + kFlagIter, lb, nb);
+    const bool last = reduce_finalize_step(acc, partials, counter, scal + kSIn, flags + kFlagIter, lb, nb);
     if constexpr (COND) {
         if (use_cond && last) {
             const int it1 = flags[kFlagIter];

@@ -43,11 +43,35 @@ __device__ __forceinline__ double block_sum(double v)
     return v;   // valid in thread 0
 }
 
+// A block's sum of per-thread FP32 values: FP32 within each warp (five more
+// roundings of terms that are FP32 sums already), FP64 across the warps.  An
+// FP64 shuffle tree in every warp took a visible share of the short CR
+// kernels: FP64 issues at a small fraction of the FP32 rate on this part.
+__device__ __forceinline__ double block_sum(float v)
+{
+    __shared__ double wsf[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) wsf[wid] = (double)v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    double d = (threadIdx.x < nw) ? wsf[threadIdx.x] : 0.0;
+    if (wid == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    }
+    return d;   // valid in thread 0
+}
+
 // Store this block's partial; the last block reduces all partials in block
 // order into *out.  Every thread of every block must call it.  lb / nb: the
 // block's index and the block count of its reduction (a launch's own, or one
 // case's share of a launch over several cases).
-__device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+// T: double, or float for per-thread FP32 sums (FP32 warp stage)
+template <typename T>
+__device__ __forceinline__ void reduce_finalize(T v, double* __restrict__ partials, unsigned* __restrict__ counter,
                                                 double* __restrict__ out, int lb, int nb)
 {
     __shared__ bool last;
@@ -69,7 +93,8 @@ __device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ p
         *counter = 0u;
     }
 }
-__device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+template <typename T>
+__device__ __forceinline__ void reduce_finalize(T v, double* __restrict__ partials, unsigned* __restrict__ counter,
                                                 double* __restrict__ out)
 {
     reduce_finalize(v, partials, counter, out, (int)blockIdx.x, (int)gridDim.x);
@@ -78,7 +103,8 @@ __device__ __forceinline__ void reduce_finalize(double v, double* __restrict__ p
 // As reduce_finalize; the last block also advances the device iteration
 // counter *it (every block read it before taking its ticket).  Returns true
 // in thread 0 of the last block, after the stores.
-__device__ __forceinline__ bool reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+template <typename T>
+__device__ __forceinline__ bool reduce_finalize_step(T v, double* __restrict__ partials, unsigned* __restrict__ counter,
                                                      double* __restrict__ out, int* __restrict__ it, int lb, int nb)
 {
     __shared__ bool last;
@@ -102,7 +128,8 @@ __device__ __forceinline__ bool reduce_finalize_step(double v, double* __restric
     }
     return threadIdx.x == 0;
 }
-__device__ __forceinline__ bool reduce_finalize_step(double v, double* __restrict__ partials, unsigned* __restrict__ counter,
+template <typename T>
+__device__ __forceinline__ bool reduce_finalize_step(T v, double* __restrict__ partials, unsigned* __restrict__ counter,
                                                      double* __restrict__ out, int* __restrict__ it)
 {
     return reduce_finalize_step(v, partials, counter, out, it, (int)blockIdx.x, (int)gridDim.x);
