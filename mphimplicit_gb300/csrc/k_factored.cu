@@ -585,13 +585,12 @@ __device__ __forceinline__ void ct_apply32_body(int lb, int N, const long long* 
     // quotient in every warp took a large share of the kernel's issue: FP64
     // runs at a small fraction of the FP32 rate on this part)
     __shared__ int go_s;
-    if (threadIdx.x == 0) {
-        int go = !flags[kFlagDone];
+    if (threadIdx.x == 0) {   // the five loads issued together
+        const int done = flags[kFlagDone], it = flags[kFlagIter];
+        const double tol2 = scal[kSTol2], rr0 = scal[kSIn0], rrn = scal[kSIn];
+        int go = !done;
         if (go) {
-            const int it = flags[kFlagIter];
-            const double tol2 = scal[kSTol2];
-            const double rr0 = scal[kSIn0];
-            const double rr = it == 0 ? rr0 : scal[kSIn];
+            const double rr = it == 0 ? rr0 : rrn;
             const bool bad = !(rr == rr);
             if (it >= cap || rr / rr0 < tol2 || bad) {
                 go = 0;
